@@ -1,0 +1,359 @@
+"""PD step benchmark: tet-iterations/s of the GB300 engine.
+
+Workload (default): 1 m cube, 64^3 hex cells split 5 tets each (274,625
+verts / 1,310,720 tets), vertices jittered +-0.1 cell (seed 2024), E=1e6,
+nu=0.45, rho=1000 kg/m^3 lumped, top face pinned (weight 1e6), dt=1/120,
+Chebyshev-accelerated Jacobi (rho=0.9995), 20 local/global iterations per
+step.  One bench step = one PD time step = 20 iterations over all tets.
+
+  value  device time of the step graph, inputs resident in HBM, L2 flushed
+         (256 MB write) between timed steps.
+  e2e    the same metric through the C ABI with pinned host buffers: every
+         step uploads X, V, runs the step and downloads X, V.
+  roofline  local-step kernel: algorithmic bytes per launch / average launch
+         time (CUDA events around every launch inside the step graph).
+
+`--impl reference` times the CPU implementation of the same iteration (the
+reference's kernels compiled for the CPU when present, else the project's
+float restatement) on all host cores, one PD step of the workload per bench
+step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "soft-body-simulation-cuda_gb300"))
+
+WORKLOAD = {
+    "workload": "pd_jacobi_cube64",
+    "desc": "64^3 hex grid x5 tets (274625 v / 1310720 t), jitter 0.1 cell seed 2024, E=1e6 nu=0.45 rho=1000, "
+            "top face pinned, dt=1/120, Jacobi+Chebyshev rho=0.9995, 20 iterations/step",
+    "grid": 64,
+    "iterations": 20,
+    "rho": 0.9995,
+    "l2": "flushed between timed steps (256 MB write)",
+}
+METRIC = "PD tet-iterations/s"
+UNIT = "tet-iter/s"
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """DRAM bytes per local-step launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "local_kernel_cube64.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["dram_bytes_per_launch"])
+        except (KeyError, ValueError):
+            return None
+    return None
+
+
+def cpu_baseline(body, params, steps: int):
+    """The float CPU restatement of the same iteration (OpenMP, all cores)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    cores = os.cpu_count() or 1
+    tm = {}
+    O.simulate(body, params, steps, precision=32, nthreads=cores, timing=tm)
+    secs = tm["step_seconds"]
+    return {"value": body.num_tets * params.num_iterations * steps / secs, "unit": UNIT, "cores": cores,
+            "kind": "port", "seconds": secs,
+            "sample": f"{steps} PD step(s) of the full workload ({steps * params.num_iterations} iterations x "
+                      f"{body.num_tets} tets), float arithmetic, OpenMP over {cores} host threads"}
+
+
+def run_reference_arm(args, body, params):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+
+    cores = os.cpu_count() or 1
+    use_ref = O.reference_available()
+    kind = "reference" if use_ref else "port"
+    # warm-up steps then timed steps, one PD step per bench step, state carried.
+    X, V = body.X.copy(), np.zeros_like(body.X)
+    t_total = 0.0
+    for k in range(args.warmup + args.steps):
+        if use_ref:
+            t0 = time.perf_counter()
+            X, V, _ = O.reference_simulate(body, params, 1, X=X, V=V)
+            dt = time.perf_counter() - t0
+        else:
+            tm = {}
+            X, V, _ = O.simulate(body, params, 1, precision=32, nthreads=cores, X=X, V=V, timing=tm)
+            dt = tm["step_seconds"]
+        if k >= args.warmup:
+            t_total += dt
+    value = body.num_tets * params.num_iterations * args.steps / t_total
+    sample = (f"one PD step ({params.num_iterations} iterations x {body.num_tets} tets) per bench step, "
+              f"{'reference kernels compiled for the CPU (serial)' if use_ref else 'float CPU restatement, OpenMP'}")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": WORKLOAD,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1 if use_ref else cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="pdgb", choices=["pdgb", "reference"])
+    ap.add_argument("--grid", type=int, default=64, help="cells per axis (64 = the benchmark workload)")
+    ap.add_argument("--cpu-steps", type=int, default=4, help="PD steps in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "pdgb":
+        args.warmup = 3
+
+    from pdgb import mesh
+    from pdgb.engine import SolverParams
+
+    body = mesh.cube_c2(n=args.grid)
+    params = SolverParams(num_iterations=WORKLOAD["iterations"], rho=WORKLOAD["rho"], solver=0)
+    if args.grid != 64:
+        WORKLOAD["grid"] = args.grid
+        WORKLOAD["workload"] = f"pd_jacobi_cube{args.grid}"
+
+    if args.impl == "reference":
+        run_reference_arm(args, body, params)
+        return
+
+    rank, world, local = dist_info()
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = init_dist(world)
+    from pdgb import PdSolver
+
+    eng = PdSolver(body, params)
+    stream = torch.cuda.ExternalStream(eng._lib.pdgb_stream(eng.handle))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)
+
+    eng.prepare()
+    eng.enable_kernel_timing(True)
+    for _ in range(args.warmup):
+        eng.update(1)
+        flush_l2()
+    eng.synchronize()
+    eng.read_timing()  # clear the accumulators
+    barrier(dist)
+    torch.cuda.synchronize()
+    # Timed region: every step graph is bracketed by CUDA events on the
+    # engine's stream (and each local-step launch inside it); the L2 flush
+    # runs between steps, outside the events.
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            eng.update(1)
+            flush_l2()
+        torch.cuda.synchronize()
+    barrier(dist)
+    tm = eng.read_timing()
+    assert tm["steps"] == args.steps
+    local_ms, local_launches = tm["local_ms"], tm["local_launches"]
+    t_local = tm["step_ms"] / 1e3
+    t_max = reduce_max(dist, t_local)
+    tet_iters = reduce_sum(dist, float(body.num_tets * params.num_iterations * args.steps))
+    value = tet_iters / t_max
+
+    # ---- e2e through the C ABI with pinned host buffers
+    import ctypes as C
+
+    from pdgb import _native as N
+
+    eng.enable_kernel_timing(False)
+    eng.prepare()
+    nv = body.num_verts
+    Xh = torch.from_numpy(body.X.copy()).pin_memory()
+    Vh = torch.zeros((nv, 3), dtype=torch.float32).pin_memory()
+    lib, h = eng._lib, eng.handle
+    for _ in range(2):
+        N.check(lib.pdgb_upload_state(h, Xh.data_ptr(), Vh.data_ptr(), N.PDGB_MEM_HOST), "upload")
+        N.check(lib.pdgb_step(h, 1), "step")
+        N.check(lib.pdgb_download_state(h, Xh.data_ptr(), Vh.data_ptr(), N.PDGB_MEM_HOST), "download")
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush_l2()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        N.check(lib.pdgb_upload_state(h, Xh.data_ptr(), Vh.data_ptr(), N.PDGB_MEM_HOST), "upload")
+        N.check(lib.pdgb_step(h, 1), "step")
+        N.check(lib.pdgb_download_state(h, Xh.data_ptr(), Vh.data_ptr(), N.PDGB_MEM_HOST), "download")
+        e2e_s += time.perf_counter() - t0
+    e2e_max = reduce_max(dist, e2e_s)
+    e2e_value = tet_iters / e2e_max
+    finite = bool(torch.isfinite(Xh).all().item())
+    eng.close()
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak_hbm()
+    bytes_per_launch = 56.0 * body.num_tets + 36.0 * body.num_verts
+    avg_local_s = (local_ms / 1e3) / max(local_launches, 1)
+    achieved = bytes_per_launch / avg_local_s / 1e9
+    traffic = ncu_traffic_per_launch() if args.grid == 64 else None
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(body, params, args.cpu_steps)
+    clk = clocks.summary()
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_max * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": dict(WORKLOAD, parallelism=f"replicas{world}" if world > 1 else "single"),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_local<true>",
+                     "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_local_s * 1e6,
+                     "launches": local_launches},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
+                "d2h_bytes_per_step": 2 * 3 * 4 * nv},
+        "gpu_launches": args.steps * (1 + 2 * params.num_iterations),
+        "clocks": clk,
+        "finite": finite,
+        "local_step_share": (local_ms / 1e3) / t_local if t_local > 0 else None,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

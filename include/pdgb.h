@@ -1,0 +1,186 @@
+/*
+ * pdgb — GB300-native projective-dynamics (PD) step engine, C ABI.
+ *
+ * Drop-in replacement for the float PD path of the reference simulator
+ * (GrahamZen/Soft-Body-Simulation-CUDA).  Each entry point names the
+ * reference interface it replaces (paths inside the reference project):
+ *
+ *   Solver<float> / FEMSolver<float>   src/simulation/solver/solver.h:11-28,
+ *                                      src/simulation/solver/femSolver.h:5-15
+ *   PdSolver                           src/simulation/solver/projective/pdSolver.h:12-44
+ *   SolverData<float>, SolverParams    src/def.h:21-56, 82-100
+ *
+ * Conventions
+ *   - Every function returns an int status (PDGB_OK = 0 on success); no C++
+ *     exception crosses this boundary.  pdgb_last_error() gives a message
+ *     for the most recent failure on the calling host thread.
+ *   - Vertex vectors are float[3*num_verts], xyz interleaved (the layout of
+ *     glm::vec3 arrays in SolverData).  Tets are uint32[4*num_tets].
+ *   - `memory` arguments say whether a pointer is host (PDGB_MEM_HOST) or
+ *     device (PDGB_MEM_DEVICE) memory.
+ *   - Work is ordered on the engine's CUDA stream.  pdgb_step() does not
+ *     synchronise the host; pdgb_download_state() to host memory does.
+ *   - One engine per host thread at a time; engines are independent.
+ */
+#ifndef PDGB_H_
+#define PDGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+#define PDGB_OK 0
+#define PDGB_ERR_INVALID_ARGUMENT 1 /* null pointer, bad size, bad enum        */
+#define PDGB_ERR_BAD_MESH 2         /* tet index out of range, degenerate tet  */
+#define PDGB_ERR_NOT_SPD 3          /* system matrix not positive definite     */
+#define PDGB_ERR_CUDA 4             /* a CUDA runtime call failed              */
+#define PDGB_ERR_OUT_OF_MEMORY 5    /* device allocation or HBM budget failed  */
+#define PDGB_ERR_NONFINITE 6        /* NaN/Inf detected in the state           */
+#define PDGB_ERR_UNSUPPORTED 7      /* feature not available for this config   */
+#define PDGB_ERR_TIMEOUT 8          /* a bounded device-side wait gave up      */
+#define PDGB_ERR_NOT_FOUND 9        /* unknown request / body id               */
+#define PDGB_ERR_BUSY 10            /* admission refused (capacity), retry     */
+
+#define PDGB_MEM_HOST 0
+#define PDGB_MEM_DEVICE 1
+
+/* Global solver choice.  Mirrors PdSolver::SolverType {Jacobi,
+ * CuSolverCholesky, EigenCholesky} (pdSolver.h:14-17); both Cholesky forms
+ * map to the engine's own prefactored sparse Cholesky. */
+#define PDGB_SOLVER_JACOBI 0
+#define PDGB_SOLVER_CHOLESKY 1
+
+/* Mirrors SolverParams<float> (def.h:82-100) for the fields PD reads, plus the
+ * pin weight (PdSolver::positional_weight, pdSolver.h:31) and the engine's
+ * refinement count. */
+typedef struct pdgb_params {
+    float dt;                /* time step h (SolverParams::dt)                  */
+    float gravity;           /* g > 0, along -y (SolverParams::gravity)         */
+    int num_iterations;      /* local/global iterations per step                */
+    float tol;               /* Cholesky early exit: stop when sqrt(mean squared
+                                change) < tol (pdSolver.cu:164); 0 = never    */
+    float rho;               /* Chebyshev spectral radius (SolverParams::rho)   */
+    float positional_weight; /* pin weight, reference value 1e6                  */
+    int solver;              /* PDGB_SOLVER_*                                    */
+    int refine_steps;        /* Cholesky: FP64-residual refinement steps 0..3   */
+} pdgb_params;
+
+/* Fills *p with the reference defaults (SolverParams<float> defaults with
+ * positional_weight 1e6, Jacobi, 10 iterations, dt 1/120). */
+void pdgb_default_params(pdgb_params* p);
+
+/* One soft-body system: the arrays SolverData<float> holds for PD. */
+typedef struct pdgb_mesh_desc {
+    int num_verts;
+    int num_tets;
+    const float* X;       /* [3*nv] positions; also the rest shape X0/DBCX    */
+    const float* V;       /* [3*nv] velocities or NULL (zero)                 */
+    const uint32_t* tets; /* [4*nt] vertex indices (SolverData::Tet)          */
+    const float* mass;    /* [nv] per-vertex mass (SolverData::mass)          */
+    const float* mu;      /* [nt] per-tet PD weight (SolverData::mu)          */
+    const float* dbc;     /* [nv] pin flags 0/1 or NULL (SolverData::DBC)      */
+    int memory;           /* PDGB_MEM_HOST or PDGB_MEM_DEVICE, for all above   */
+} pdgb_mesh_desc;
+
+typedef struct pdgb_engine pdgb_engine;
+
+/* Per-phase timing, mirrors Solver::GetPerformanceData() (solver.h:19). */
+typedef struct pdgb_perf {
+    double prepare_ms;       /* last SolverPrepare equivalent (host + device)   */
+    double steps;            /* steps run since create/reset                    */
+    double iterations;       /* local/global iterations run                     */
+    long long factor_nnz;    /* nnz of the scalar Cholesky factor (0: Jacobi)   */
+    long long tiles;         /* tet tiles of the local-step kernel              */
+    long long patch_verts;   /* sum of tile patch sizes                         */
+} pdgb_perf;
+
+/* Replaces PdSolver(int threadsPerBlock, const SolverData<float>&)
+ * (pdSolver.cu:22-27, femSolver.cu:7-17).  Copies the mesh; the caller's
+ * arrays may be freed afterwards.  stream: a cudaStream_t or NULL for a
+ * stream the engine creates. */
+int pdgb_create(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* stream, pdgb_engine** out);
+
+/* Replaces PdSolver::SolverPrepare (pdSolver.cu:40-139): per-tet DmInv/V0,
+ * system assembly, ordering and factorisation, step graph.  pdgb_step calls
+ * it on first use, as PdSolver::Update does (pdSolver.cu:212-216). */
+int pdgb_prepare(pdgb_engine* e);
+
+/* Replaces nsteps calls of PdSolver::Update (pdSolver.cu:210-232) without
+ * collision handling: s_n, local/global iterations, velocity/position update,
+ * X <- XTilde. */
+int pdgb_step(pdgb_engine* e, int nsteps);
+
+/* Replaces PdSolver::SetGlobalSolver (pdSolver.h:20).  Takes effect at the
+ * next prepare (a changed solver forces one). */
+int pdgb_set_solver(pdgb_engine* e, int solver);
+
+/* Updates dt/gravity/iterations/tol/rho/pin weight/refinement.  A change of
+ * dt, pin weight or solver re-prepares on the next step. */
+int pdgb_set_params(pdgb_engine* e, const pdgb_params* params);
+
+/* State transfer in the reference layout (SolverData::X / V). */
+int pdgb_upload_state(pdgb_engine* e, const float* X, const float* V, int memory);
+int pdgb_download_state(pdgb_engine* e, float* X, float* V, int memory);
+
+/* Replaces SimulationCUDAContext::Reset + Solver::Reset
+ * (simulationContext.cu:233-243, solver.h:40-43): X = X0, V = 0, re-prepare. */
+int pdgb_reset(pdgb_engine* e);
+
+int pdgb_get_perf(pdgb_engine* e, pdgb_perf* out);
+
+/* Per-iteration convergence record of the last step (Cholesky path): the
+ * number of iterations run (early exit on tol).  Synchronises. */
+int pdgb_last_step_iterations(pdgb_engine* e, int* iterations);
+
+/* Waits for the engine's stream. */
+int pdgb_synchronize(pdgb_engine* e);
+
+/* Device timing for benchmarks.  When enabled, pdgb_step brackets every
+ * step-graph launch and every local-step kernel inside it with CUDA events
+ * on the engine's stream, waits for each step and accumulates the elapsed
+ * times; pdgb_read_timing returns the sums since the last read and clears
+ * them.  Disabled (the default), pdgb_step never waits. */
+typedef struct pdgb_timing {
+    double step_ms;          /* summed device time of the step graphs          */
+    long long steps;         /* steps timed                                     */
+    double local_ms;         /* summed device time of the local-step launches   */
+    long long local_launches;
+} pdgb_timing;
+int pdgb_enable_kernel_timing(pdgb_engine* e, int enable);
+int pdgb_read_timing(pdgb_engine* e, pdgb_timing* out);
+
+/* Algorithmic bytes of one local-step launch (inputs read once, outputs
+ * written once; see the roofline section of the design notes). */
+int pdgb_local_step_bytes(pdgb_engine* e, double* bytes);
+
+int pdgb_destroy(pdgb_engine* e);
+
+/* Returns the CUDA stream (cudaStream_t) the engine orders its work on. */
+void* pdgb_stream(pdgb_engine* e);
+
+const char* pdgb_status_string(int status);
+const char* pdgb_last_error(void);
+
+/* Host-only inspection of the engine's data layout for a mesh (no GPU
+ * needed): the Morton vertex/tet renumbering and the local-step tiles.
+ * vperm/tperm (nullable) receive internal -> caller maps of length nv / nt. */
+typedef struct pdgb_layout_info {
+    int num_tiles;          /* CTAs of one local-step launch                   */
+    int max_patch;          /* largest tile vertex patch (<= 1024)             */
+    int max_tile_tets;      /* largest tile                                    */
+    int reserved;
+    long long patch_verts;  /* sum of patch sizes (vertex reuse = nv*4/this)   */
+} pdgb_layout_info;
+int pdgb_inspect_layout(const pdgb_mesh_desc* mesh, pdgb_layout_info* info, int* vperm, int* tperm);
+
+/* Library version string. */
+const char* pdgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PDGB_H_ */

@@ -1,0 +1,495 @@
+// C ABI of the pdgb engine (include/pdgb.h).
+//
+// An engine is the GB300 counterpart of one PdSolver bound to one
+// SolverData<float> (pdSolver.h:12-44): it owns a device copy of the mesh in
+// its own layout, the solver scratch, and a CUDA graph holding one full time
+// step (prologue, num_iterations x (local kernel, global kernel), velocity /
+// position update), replayed by pdgb_step.
+#include <chrono>
+#include <cmath>
+#include <algorithm>
+#include <cstring>
+
+#include "engine.h"
+
+namespace pdgb {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(int status, const std::string& msg) {
+    (void)status;
+    g_last_error = msg;
+}
+
+}  // namespace pdgb
+
+using namespace pdgb;
+
+struct pdgb_engine {
+    pdgb_params prm{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int nv = 0, nt = 0;
+    // caller data (host copies, caller order)
+    std::vector<float> X0, mass, mu, dbc;
+    std::vector<uint32_t> tets;
+    bool has_dbc = false;
+    HostLayout L;
+    bool prepared = false;
+    // device: mesh
+    DBuf<uint2> tet_local;
+    DBuf<float> geo;
+    DBuf<int> tile_tet_ptr, tile_vptr, tile_verts, vperm;
+    DBuf<float4> coef, pin_rhs, x0;
+    // device: state + scratch
+    DBuf<float4> x, v, sn, prev, base, b;
+    DBuf<float> staging;  // [6 nv] host <-> device transfers
+    // step graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool timing = false;
+    std::vector<cudaEvent_t> events;  // 2 per local launch
+    cudaEvent_t step_ev[2] = {nullptr, nullptr};
+    double local_ms_acc = 0.0, step_ms_acc = 0.0;
+    long long local_launches = 0, steps_timed = 0;
+    // perf
+    double prepare_ms = 0.0;
+    double steps_run = 0, iters_run = 0;
+
+    ~pdgb_engine() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto ev : events) cudaEventDestroy(ev);
+        for (auto ev : step_ev)
+            if (ev) cudaEventDestroy(ev);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+template <class F> int guarded(F&& f) {
+    try {
+        f();
+        return PDGB_OK;
+    } catch (const Error& e) {
+        set_last_error(e.status, e.msg);
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        set_last_error(PDGB_ERR_OUT_OF_MEMORY, "host allocation failed");
+        return PDGB_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, e.what());
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+}
+
+void check_params(const pdgb_params& p) {
+    if (!(p.dt > 0.f) || !std::isfinite(p.dt)) throw Error{PDGB_ERR_INVALID_ARGUMENT, "dt must be > 0"};
+    if (p.num_iterations < 1 || p.num_iterations > 4096)
+        throw Error{PDGB_ERR_INVALID_ARGUMENT, "num_iterations must be in [1, 4096]"};
+    if (p.solver != PDGB_SOLVER_JACOBI && p.solver != PDGB_SOLVER_CHOLESKY)
+        throw Error{PDGB_ERR_INVALID_ARGUMENT, "unknown solver"};
+    if (p.refine_steps < 0 || p.refine_steps > 3) throw Error{PDGB_ERR_INVALID_ARGUMENT, "refine_steps must be 0..3"};
+    if (!(p.positional_weight >= 0.f)) throw Error{PDGB_ERR_INVALID_ARGUMENT, "positional_weight must be >= 0"};
+}
+
+template <class T>
+void copy_in(std::vector<T>& dst, const T* src, size_t n, int memory) {
+    dst.resize(n);
+    if (n == 0) return;
+    if (memory == PDGB_MEM_DEVICE) PDGB_CUDA_TRY(cudaMemcpy(dst.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost));
+    else std::memcpy(dst.data(), src, n * sizeof(T));
+}
+
+void destroy_graph(pdgb_engine* e) {
+    if (e->gexec) cudaGraphExecDestroy(e->gexec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    e->gexec = nullptr;
+    e->graph = nullptr;
+}
+
+LocalArgs local_args(pdgb_engine* e) {
+    LocalArgs a;
+    a.sn = e->sn.p;
+    a.b = e->b.p;
+    a.tet_local = e->tet_local.p;
+    a.geo = e->geo.p;
+    a.tile_tet_ptr = e->tile_tet_ptr.p;
+    a.tile_vptr = e->tile_vptr.p;
+    a.tile_verts = e->tile_verts.p;
+    a.nt_pad = e->L.nt_pad;
+    return a;
+}
+
+// Records one time step of the Jacobi-Chebyshev path on the stream.
+void record_jacobi_step(pdgb_engine* e) {
+    cudaStream_t s = e->stream;
+    const int n = e->prm.num_iterations;
+    BeginArgs ba{e->nv, e->x.p, e->v.p, e->coef.p, e->sn.p, e->base.p, e->b.p, e->prm.dt, e->prm.gravity};
+    launch_begin(ba, s);
+    const std::vector<float> omega = chebyshev_omegas(n, e->prm.rho);
+    const LocalArgs la = local_args(e);
+    VertexArgs va{e->nv, e->sn.p, e->prev.p, e->b.p, e->base.p, e->coef.p, e->pin_rhs.p, e->x.p, e->v.p, 1.f,
+                  1.0f / e->prm.dt};
+    for (int i = 0; i < n; ++i) {
+        if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i], s, cudaEventRecordExternal));
+        launch_local(la, e->L.ntiles, true, s);
+        if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i + 1], s, cudaEventRecordExternal));
+        int mode = 0;
+        if (i >= 11) mode |= kReadPrev;                 // omega != 1 from iteration 11 on
+        if (i >= 10 && i + 1 < n) mode |= kWritePrev;   // prev is read from iteration 11 on
+        if (i + 1 == n) mode |= kFinal;
+        va.omega = omega[i];
+        launch_jacobi_vertex(va, mode, s);
+    }
+}
+
+void build_graph(pdgb_engine* e) {
+    destroy_graph(e);
+    if (e->timing) {
+        const size_t need = 2 * (size_t)e->prm.num_iterations;
+        while (e->events.size() < need) {
+            cudaEvent_t ev;
+            PDGB_CUDA_TRY(cudaEventCreate(&ev));
+            e->events.push_back(ev);
+        }
+    }
+    PDGB_CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+        if (e->prm.solver == PDGB_SOLVER_JACOBI) record_jacobi_step(e);
+        else throw Error{PDGB_ERR_UNSUPPORTED, "Cholesky global solve not built in this library"};
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(e->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    PDGB_CUDA_TRY(cudaStreamEndCapture(e->stream, &e->graph));
+    PDGB_CUDA_TRY(cudaGraphInstantiate(&e->gexec, e->graph, 0));
+}
+
+void upload_mesh(pdgb_engine* e) {
+    const HostLayout& L = e->L;
+    cudaStream_t s = e->stream;
+    e->tet_local.upload(L.tet_local, s);
+    e->geo.upload(L.geo, s);
+    e->tile_tet_ptr.upload(L.tile_tet_ptr, s);
+    e->tile_vptr.upload(L.tile_vptr, s);
+    e->tile_verts.upload(L.tile_verts, s);
+    e->vperm.upload(L.vperm, s);
+    e->x0.upload(L.x0, s);
+    const size_t nv = e->nv;
+    e->x.alloc(nv);
+    e->v.alloc(nv);
+    e->sn.alloc(nv);
+    e->prev.alloc(nv);
+    e->base.alloc(nv);
+    e->b.alloc(nv);
+    e->coef.alloc(nv);
+    e->pin_rhs.alloc(nv);
+    e->staging.alloc(6 * nv);
+    PDGB_CUDA_TRY(cudaMemsetAsync(e->prev.p, 0, nv * sizeof(float4), s));
+}
+
+void prepare(pdgb_engine* e) {
+    auto t0 = std::chrono::steady_clock::now();
+    build_vertex_coefficients(e->mass.data(), e->has_dbc ? e->dbc.data() : nullptr, e->prm, e->L);
+    e->coef.upload(e->L.coef, e->stream);
+    e->pin_rhs.upload(e->L.pin_rhs, e->stream);
+    build_graph(e);
+    PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->prepared = true;
+    e->prepare_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+extern "C" {
+
+void pdgb_default_params(pdgb_params* p) {
+    if (!p) return;
+    p->dt = 1.0f / 120.0f;
+    p->gravity = 9.8f;
+    p->num_iterations = 10;
+    p->tol = 0.0f;
+    p->rho = 0.9992f;
+    p->positional_weight = 1e6f;
+    p->solver = PDGB_SOLVER_JACOBI;
+    p->refine_steps = 0;
+}
+
+int pdgb_create(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* stream, pdgb_engine** out) {
+    if (!out) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "out is null");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    pdgb_engine* e = nullptr;
+    int st = guarded([&] {
+        if (!mesh || !params) throw Error{PDGB_ERR_INVALID_ARGUMENT, "mesh or params is null"};
+        if (!mesh->X || !mesh->tets || !mesh->mass || !mesh->mu)
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "mesh X, tets, mass and mu are required"};
+        if (mesh->memory != PDGB_MEM_HOST && mesh->memory != PDGB_MEM_DEVICE)
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "mesh memory must be PDGB_MEM_HOST or PDGB_MEM_DEVICE"};
+        if (mesh->num_verts <= 0 || mesh->num_tets <= 0)
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "num_verts and num_tets must be positive"};
+        if (mesh->num_verts > (1 << 28) || mesh->num_tets > (1 << 28))
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "mesh too large (limit 2^28 vertices / tets)"};
+        check_params(*params);
+        e = new pdgb_engine();
+        e->prm = *params;
+        e->nv = mesh->num_verts;
+        e->nt = mesh->num_tets;
+        if (stream) e->stream = (cudaStream_t)stream;
+        else {
+            PDGB_CUDA_TRY(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+            e->own_stream = true;
+        }
+        copy_in(e->X0, mesh->X, 3 * (size_t)e->nv, mesh->memory);
+        copy_in(e->tets, mesh->tets, 4 * (size_t)e->nt, mesh->memory);
+        copy_in(e->mass, mesh->mass, (size_t)e->nv, mesh->memory);
+        copy_in(e->mu, mesh->mu, (size_t)e->nt, mesh->memory);
+        e->has_dbc = mesh->dbc != nullptr;
+        if (e->has_dbc) copy_in(e->dbc, mesh->dbc, (size_t)e->nv, mesh->memory);
+        build_layout(e->nv, e->nt, e->X0.data(), e->tets.data(), e->mass.data(), e->mu.data(),
+                     e->has_dbc ? e->dbc.data() : nullptr, e->prm, e->L);
+        upload_mesh(e);
+        // initial state X (and V) from the descriptor
+        std::vector<float> Vh;
+        if (mesh->V) copy_in(Vh, mesh->V, 3 * (size_t)e->nv, mesh->memory);
+        PDGB_CUDA_TRY(cudaMemcpyAsync(e->staging.p, e->X0.data(), 3 * (size_t)e->nv * sizeof(float),
+                                      cudaMemcpyHostToDevice, e->stream));
+        if (mesh->V)
+            PDGB_CUDA_TRY(cudaMemcpyAsync(e->staging.p + 3 * (size_t)e->nv, Vh.data(),
+                                          3 * (size_t)e->nv * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+        launch_gather_state(e->nv, e->vperm.p, e->staging.p, mesh->V ? e->staging.p + 3 * (size_t)e->nv : nullptr,
+                            e->x.p, e->v.p, e->stream);
+        PDGB_CUDA_TRY(cudaGetLastError());
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    });
+    if (st != PDGB_OK) {
+        delete e;
+        return st;
+    }
+    *out = e;
+    return PDGB_OK;
+}
+
+int pdgb_prepare(pdgb_engine* e) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] { prepare(e); });
+}
+
+int pdgb_step(pdgb_engine* e, int nsteps) {
+    if (!e || nsteps < 0) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or nsteps");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        if (!e->prepared) prepare(e);
+        if (e->timing && !e->step_ev[0]) {
+            PDGB_CUDA_TRY(cudaEventCreate(&e->step_ev[0]));
+            PDGB_CUDA_TRY(cudaEventCreate(&e->step_ev[1]));
+        }
+        for (int k = 0; k < nsteps; ++k) {
+            if (e->timing) PDGB_CUDA_TRY(cudaEventRecord(e->step_ev[0], e->stream));
+            PDGB_CUDA_TRY(cudaGraphLaunch(e->gexec, e->stream));
+            if (e->timing) {
+                PDGB_CUDA_TRY(cudaEventRecord(e->step_ev[1], e->stream));
+                PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+                float ms = 0.f;
+                PDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e->step_ev[0], e->step_ev[1]));
+                e->step_ms_acc += ms;
+                e->steps_timed++;
+                for (int i = 0; i < e->prm.num_iterations; ++i) {
+                    PDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e->events[2 * i], e->events[2 * i + 1]));
+                    e->local_ms_acc += ms;
+                    e->local_launches++;
+                }
+            }
+        }
+        e->steps_run += nsteps;
+        e->iters_run += (double)nsteps * e->prm.num_iterations;
+    });
+}
+
+int pdgb_set_solver(pdgb_engine* e, int solver) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        pdgb_params p = e->prm;
+        p.solver = solver;
+        check_params(p);
+        if (p.solver != e->prm.solver) e->prepared = false;
+        e->prm = p;
+    });
+}
+
+int pdgb_set_params(pdgb_engine* e, const pdgb_params* params) {
+    if (!e || !params) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        check_params(*params);
+        e->prm = *params;
+        e->prepared = false;  // coefficients, omegas and the graph depend on them
+    });
+}
+
+int pdgb_upload_state(pdgb_engine* e, const float* X, const float* V, int memory) {
+    if (!e || !X) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        const size_t n3 = 3 * (size_t)e->nv;
+        if (memory == PDGB_MEM_HOST) {
+            PDGB_CUDA_TRY(cudaMemcpyAsync(e->staging.p, X, n3 * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+            if (V)
+                PDGB_CUDA_TRY(
+                    cudaMemcpyAsync(e->staging.p + n3, V, n3 * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+            launch_gather_state(e->nv, e->vperm.p, e->staging.p, V ? e->staging.p + n3 : nullptr, e->x.p, e->v.p,
+                                e->stream);
+        } else if (memory == PDGB_MEM_DEVICE) {
+            launch_gather_state(e->nv, e->vperm.p, X, V, e->x.p, e->v.p, e->stream);
+        } else {
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "bad memory kind"};
+        }
+        PDGB_CUDA_TRY(cudaGetLastError());
+    });
+}
+
+int pdgb_download_state(pdgb_engine* e, float* X, float* V, int memory) {
+    if (!e || (!X && !V)) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        const size_t n3 = 3 * (size_t)e->nv;
+        if (memory == PDGB_MEM_HOST) {
+            launch_scatter_state(e->nv, e->vperm.p, e->x.p, e->v.p, X ? e->staging.p : nullptr,
+                                 V ? e->staging.p + n3 : nullptr, e->stream);
+            if (X) PDGB_CUDA_TRY(cudaMemcpyAsync(X, e->staging.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+            if (V)
+                PDGB_CUDA_TRY(
+                    cudaMemcpyAsync(V, e->staging.p + n3, n3 * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+            PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        } else if (memory == PDGB_MEM_DEVICE) {
+            launch_scatter_state(e->nv, e->vperm.p, e->x.p, e->v.p, X, V, e->stream);
+        } else {
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "bad memory kind"};
+        }
+        PDGB_CUDA_TRY(cudaGetLastError());
+    });
+}
+
+int pdgb_reset(pdgb_engine* e) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        launch_copy_x0(e->nv, e->x0.p, e->x.p, e->v.p, e->stream);
+        PDGB_CUDA_TRY(cudaGetLastError());
+        e->prepared = false;
+        e->steps_run = 0;
+        e->iters_run = 0;
+    });
+}
+
+int pdgb_get_perf(pdgb_engine* e, pdgb_perf* out) {
+    if (!e || !out) return PDGB_ERR_INVALID_ARGUMENT;
+    out->prepare_ms = e->prepare_ms;
+    out->steps = e->steps_run;
+    out->iterations = e->iters_run;
+    out->factor_nnz = 0;
+    out->tiles = e->L.ntiles;
+    out->patch_verts = (long long)e->L.tile_verts.size();
+    return PDGB_OK;
+}
+
+int pdgb_last_step_iterations(pdgb_engine* e, int* iterations) {
+    if (!e || !iterations) return PDGB_ERR_INVALID_ARGUMENT;
+    *iterations = e->prm.num_iterations;
+    return PDGB_OK;
+}
+
+int pdgb_synchronize(pdgb_engine* e) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] { PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream)); });
+}
+
+int pdgb_enable_kernel_timing(pdgb_engine* e, int enable) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    if ((enable != 0) != e->timing) {
+        e->timing = enable != 0;
+        e->prepared = false;
+    }
+    e->local_ms_acc = e->step_ms_acc = 0.0;
+    e->local_launches = e->steps_timed = 0;
+    return PDGB_OK;
+}
+
+int pdgb_read_timing(pdgb_engine* e, pdgb_timing* out) {
+    if (!e || !out) return PDGB_ERR_INVALID_ARGUMENT;
+    out->step_ms = e->step_ms_acc;
+    out->steps = e->steps_timed;
+    out->local_ms = e->local_ms_acc;
+    out->local_launches = e->local_launches;
+    e->local_ms_acc = e->step_ms_acc = 0.0;
+    e->local_launches = e->steps_timed = 0;
+    return PDGB_OK;
+}
+
+int pdgb_local_step_bytes(pdgb_engine* e, double* bytes) {
+    if (!e || !bytes) return PDGB_ERR_INVALID_ARGUMENT;
+    // per tet: 4 x u32 corner ids + 9 x f32 DmInv + 1 x f32 V0*w = 56 B;
+    // per vertex: read q (12 B), read (M/h^2) s (12 B), write b (12 B) = 36 B.
+    *bytes = 56.0 * e->nt + 36.0 * e->nv;
+    return PDGB_OK;
+}
+
+int pdgb_destroy(pdgb_engine* e) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(e->stream);
+    delete e;
+    return PDGB_OK;
+}
+
+void* pdgb_stream(pdgb_engine* e) { return e ? (void*)e->stream : nullptr; }
+
+const char* pdgb_status_string(int status) {
+    switch (status) {
+        case PDGB_OK: return "ok";
+        case PDGB_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case PDGB_ERR_BAD_MESH: return "bad mesh";
+        case PDGB_ERR_NOT_SPD: return "system matrix not positive definite";
+        case PDGB_ERR_CUDA: return "CUDA error";
+        case PDGB_ERR_OUT_OF_MEMORY: return "out of memory";
+        case PDGB_ERR_NONFINITE: return "non-finite value";
+        case PDGB_ERR_UNSUPPORTED: return "unsupported";
+        case PDGB_ERR_TIMEOUT: return "device wait timed out";
+        case PDGB_ERR_NOT_FOUND: return "not found";
+        case PDGB_ERR_BUSY: return "busy";
+        default: return "unknown status";
+    }
+}
+
+const char* pdgb_last_error(void) { return g_last_error.c_str(); }
+
+int pdgb_inspect_layout(const pdgb_mesh_desc* mesh, pdgb_layout_info* info, int* vperm, int* tperm) {
+    if (!mesh || !info || mesh->memory != PDGB_MEM_HOST || !mesh->X || !mesh->tets || !mesh->mass || !mesh->mu) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "host mesh with X, tets, mass, mu required");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        pdgb_params p;
+        pdgb_default_params(&p);
+        HostLayout L;
+        build_layout(mesh->num_verts, mesh->num_tets, mesh->X, mesh->tets, mesh->mass, mesh->mu, mesh->dbc, p, L);
+        info->num_tiles = L.ntiles;
+        info->patch_verts = (long long)L.tile_verts.size();
+        info->max_patch = 0;
+        info->max_tile_tets = 0;
+        info->reserved = 0;
+        for (int t = 0; t < L.ntiles; ++t) {
+            info->max_patch = std::max(info->max_patch, L.tile_vptr[t + 1] - L.tile_vptr[t]);
+            info->max_tile_tets = std::max(info->max_tile_tets, L.tile_tet_ptr[t + 1] - L.tile_tet_ptr[t]);
+        }
+        if (vperm) std::copy(L.vperm.begin(), L.vperm.end(), vperm);
+        if (tperm) std::copy(L.tperm.begin(), L.tperm.end(), tperm);
+    });
+}
+
+const char* pdgb_version(void) { return "pdgb 0.1 (sm_103a)"; }
+
+}  // extern "C"

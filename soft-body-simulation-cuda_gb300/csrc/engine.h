@@ -1,0 +1,151 @@
+// Internal definitions of the pdgb engine (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/pdgb.h"
+
+namespace pdgb {
+
+// ----------------------------------------------------------------- errors
+struct Error {
+    int status;
+    std::string msg;
+};
+void set_last_error(int status, const std::string& msg);
+
+#define PDGB_CUDA_TRY(call)                                                                       \
+    do {                                                                                          \
+        cudaError_t err__ = (call);                                                               \
+        if (err__ != cudaSuccess)                                                                 \
+            throw ::pdgb::Error{PDGB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(err__)}; \
+    } while (0)
+
+// ------------------------------------------------------- tiling constants
+// Local-step tiles: a CTA owns a run of Morton-ordered tets and the patch of
+// vertices they touch.  kMaxPatch bounds the patch so that its positions and
+// accumulators fit in shared memory (16 + 12 bytes per vertex).
+constexpr int kMaxPatch = 1024;
+constexpr int kLocalThreads = 256;
+
+// Device buffer with RAII.
+template <class T> struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw Error{PDGB_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed"};
+        }
+        n = count;
+    }
+    void upload(const std::vector<T>& h, cudaStream_t s) {
+        if (h.size() > n) alloc(h.size());
+        if (!h.empty()) PDGB_CUDA_TRY(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+};
+
+// Host-side product of prepare: everything the kernels need, in the
+// engine's internal (Morton) vertex and tet order.
+struct HostLayout {
+    int nv = 0, nt = 0, nt_pad = 0, ntiles = 0;
+    std::vector<int> vperm;   // internal vertex -> caller vertex
+    std::vector<int> viperm;  // caller vertex -> internal vertex
+    std::vector<int> tperm;   // internal tet -> caller tet
+    // tiles
+    std::vector<int> tile_tet_ptr;   // [ntiles+1]
+    std::vector<int> tile_vptr;      // [ntiles+1]
+    std::vector<int> tile_verts;     // internal vertex ids of each patch (sorted)
+    std::vector<uint2> tet_local;    // [nt_pad] 4 x u16 patch-local corner ids
+    std::vector<float> geo;          // SoA [10][nt_pad]: DmInv row-major (9), V0*w
+    std::vector<uint32_t> tets_int;  // [4*nt] internal vertex ids (Cholesky assembly, checks)
+    std::vector<double> dminv_d;     // [9*nt] double DmInv (system assembly)
+    std::vector<double> coef_d;      // [nt]   double V0*w
+    // per vertex, internal order
+    std::vector<float4> coef;        // {mdt2, stiffness diag, pin flag, mass}
+    std::vector<float4> pin_rhs;     // x0 * (pin weight / h^2) for pinned vertices
+    std::vector<float4> x0;          // rest positions
+};
+
+// Builds the layout from caller arrays (host memory).  Throws Error.
+void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const float* mass, const float* mu,
+                  const float* dbc, const pdgb_params& prm, HostLayout& L);
+
+// Recomputes the per-vertex coefficients that depend on dt / pin weight.
+void build_vertex_coefficients(const float* mass, const float* dbc, const pdgb_params& prm, HostLayout& L);
+
+// Jacobi-Chebyshev relaxation weights of iterations 0..n-1, computed in float
+// exactly as the reference's host loop does (pdSolver.cu:196-199).
+std::vector<float> chebyshev_omegas(int n, float rho);
+
+// --------------------------------------------------------------- kernels
+struct LocalArgs {
+    const float4* sn;
+    float4* b;
+    const uint2* tet_local;
+    const float* geo;
+    const int* tile_tet_ptr;
+    const int* tile_vptr;
+    const int* tile_verts;
+    int nt_pad;
+};
+
+// Vertex-kernel mode flags.
+enum : int {
+    kReadPrev = 1,    // Chebyshev blend with prev (omega != 1)
+    kWritePrev = 2,   // store sn as prev for the next iteration
+    kFinal = 4,       // last iteration: velocity/position update, no b reset
+};
+
+struct VertexArgs {
+    int nv;
+    float4* sn;
+    float4* prev;
+    float4* b;
+    const float4* base;
+    const float4* coef;
+    const float4* pin_rhs;
+    float4* x;
+    float4* v;
+    float omega;
+    float dt_inv;
+};
+
+struct BeginArgs {
+    int nv;
+    const float4* x;
+    const float4* v;
+    const float4* coef;
+    float4* sn;
+    float4* base;
+    float4* b;
+    float dt;
+    float gravity;
+};
+
+void launch_begin(const BeginArgs& a, cudaStream_t s);
+void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, cudaStream_t s);
+void launch_jacobi_vertex(const VertexArgs& a, int mode, cudaStream_t s);
+void launch_gather_state(int nv, const int* vperm, const float* X, const float* V, float4* x, float4* v,
+                         cudaStream_t s);
+void launch_scatter_state(int nv, const int* vperm, const float4* x, const float4* v, float* X, float* V,
+                          cudaStream_t s);
+void launch_copy_x0(int nv, const float4* x0, float4* x, float4* v, cudaStream_t s);
+
+}  // namespace pdgb

@@ -1,0 +1,215 @@
+// Hot-path kernels of the pdgb PD engine (sm_103a).
+//
+//   k_local        per-tet corotational projection + RHS scatter
+//                  (reference: PdUtil::computeLocal, pdUtil.cu:97-145)
+//   k_jacobi_vertex Jacobi update + Chebyshev blend + pinned-RHS overwrite
+//                  + b reset, fused; last iteration also does the velocity /
+//                  position update (reference: getErrorKern, chebyshevKern,
+//                  computeDBCLocal, addM_h2Sn, updateVelPos; pdUtil.cu:147-226)
+//   k_begin        step prologue: gravity, s_n, M/h^2 s_n (reference:
+//                  pdSolver.cu:154-163, computeSn pdUtil.cu:73-95)
+#include "engine.h"
+#include "rotation.cuh"
+
+namespace pdgb {
+
+// ------------------------------------------------------------ local step
+// One CTA per tile.  The tile's patch of vertex positions is staged in
+// shared memory (one coalesced pass over the sorted patch list), every tet
+// gathers its 4 corners from shared memory, and the 12 RHS contributions are
+// accumulated with shared-memory atomics; one float4 global atomic per patch
+// vertex flushes the tile.  This replaces the reference's 12 global atomics
+// per tet with about one per 3 tets.
+template <bool kJacobiForm>
+__global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
+    __shared__ float4 sq[kMaxPatch];
+    __shared__ float ax[kMaxPatch], ay[kMaxPatch], az[kMaxPatch];
+    const int tile = blockIdx.x;
+    const int vb = a.tile_vptr[tile];
+    const int np = a.tile_vptr[tile + 1] - vb;
+    for (int k = threadIdx.x; k < np; k += kLocalThreads) {
+        sq[k] = __ldg(&a.sn[a.tile_verts[vb + k]]);
+        ax[k] = 0.f;
+        ay[k] = 0.f;
+        az[k] = 0.f;
+    }
+    __syncthreads();
+    const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
+    const int ntp = a.nt_pad;
+    for (int t = t0 + threadIdx.x; t < t1; t += kLocalThreads) {
+        const uint2 li = __ldg(&a.tet_local[t]);
+        const int i0 = li.x & 0xffff, i1 = li.x >> 16, i2 = li.y & 0xffff, i3 = li.y >> 16;
+        float D[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) D[k] = __ldg(&a.geo[k * ntp + t]);
+        const float c = __ldg(&a.geo[9 * ntp + t]);
+        const float4 p0 = sq[i0], p1 = sq[i1], p2 = sq[i2], p3 = sq[i3];
+        // Ds columns = edges; F = Ds * DmInv (row-major F[r][c])
+        const float e[3][3] = {{p1.x - p0.x, p2.x - p0.x, p3.x - p0.x},
+                               {p1.y - p0.y, p2.y - p0.y, p3.y - p0.y},
+                               {p1.z - p0.z, p2.z - p0.z, p3.z - p0.z}};
+        float F[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc)
+                F[3 * r + cc] = e[r][0] * D[cc] + e[r][1] * D[3 + cc] + e[r][2] * D[6 + cc];
+        float R[9];
+        closest_rotation(F, R);
+        if (kJacobiForm) {
+#pragma unroll
+            for (int k = 0; k < 9; ++k) R[k] -= F[k];
+        }
+        // M = (c R) DmInv^T ; contributions: corner 0 = -(M0+M1+M2), corner j = M_{j-1}
+        float M[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const float r0 = c * R[3 * r], r1 = c * R[3 * r + 1], r2 = c * R[3 * r + 2];
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) M[3 * r + cc] = r0 * D[3 * cc] + r1 * D[3 * cc + 1] + r2 * D[3 * cc + 2];
+        }
+        atomicAdd(&ax[i1], M[0]); atomicAdd(&ay[i1], M[3]); atomicAdd(&az[i1], M[6]);
+        atomicAdd(&ax[i2], M[1]); atomicAdd(&ay[i2], M[4]); atomicAdd(&az[i2], M[7]);
+        atomicAdd(&ax[i3], M[2]); atomicAdd(&ay[i3], M[5]); atomicAdd(&az[i3], M[8]);
+        atomicAdd(&ax[i0], -(M[0] + M[1] + M[2]));
+        atomicAdd(&ay[i0], -(M[3] + M[4] + M[5]));
+        atomicAdd(&az[i0], -(M[6] + M[7] + M[8]));
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < np; k += kLocalThreads) {
+        atomicAdd(&a.b[a.tile_verts[vb + k]], make_float4(ax[k], ay[k], az[k], 0.f));
+    }
+}
+
+void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, cudaStream_t s) {
+    if (ntiles <= 0) return;
+    if (jacobi_form) k_local<true><<<ntiles, kLocalThreads, 0, s>>>(a);
+    else k_local<false><<<ntiles, kLocalThreads, 0, s>>>(a);
+}
+
+// ------------------------------------------------------- vertex kernels
+// 0.9 is a double literal in the reference's Chebyshev kernel (pdUtil.cu:221),
+// so 0.9*(x - s) + s is evaluated in double there.  Splitting 0.9 into a
+// float head and tail keeps the product exact to ~1e-15 without FP64 math.
+__device__ __forceinline__ float relax09(float nx, float s) {
+    const float d = nx - s;
+    constexpr float kHi = 0.9f;
+    constexpr float kLo = (float)(0.9 - (double)0.9f);
+    return fmaf(kHi, d, fmaf(kLo, d, s));
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(256) k_jacobi_vertex(VertexArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nv) return;
+    const float4 s = a.sn[i];
+    const float4 cf = __ldg(&a.coef[i]);
+    const float cm = cf.x, md = cf.y;
+    const float4 bb = (cf.z != 0.f) ? __ldg(&a.pin_rhs[i]) : a.b[i];
+    const float den = cm + md;
+    float4 nx;
+    nx.x = relax09((bb.x - cm * s.x) / den + s.x, s.x);
+    nx.y = relax09((bb.y - cm * s.y) / den + s.y, s.y);
+    nx.z = relax09((bb.z - cm * s.z) / den + s.z, s.z);
+    nx.w = 0.f;
+    if (kMode & kReadPrev) {
+        const float4 p = a.prev[i];
+        nx.x = (nx.x - p.x) * a.omega + p.x;
+        nx.y = (nx.y - p.y) * a.omega + p.y;
+        nx.z = (nx.z - p.z) * a.omega + p.z;
+    }
+    if (kMode & kWritePrev) a.prev[i] = s;
+    if (kMode & kFinal) {
+        const float4 xo = a.x[i];
+        a.v[i] = make_float4((nx.x - xo.x) * a.dt_inv, (nx.y - xo.y) * a.dt_inv, (nx.z - xo.z) * a.dt_inv, 0.f);
+        a.x[i] = nx;
+    } else {
+        a.sn[i] = nx;
+        a.b[i] = __ldg(&a.base[i]);
+    }
+}
+
+void launch_jacobi_vertex(const VertexArgs& a, int mode, cudaStream_t s) {
+    const int blocks = (a.nv + 255) / 256;
+    if (blocks == 0) return;
+    switch (mode & 7) {
+        case 0: k_jacobi_vertex<0><<<blocks, 256, 0, s>>>(a); break;
+        case 1: k_jacobi_vertex<1><<<blocks, 256, 0, s>>>(a); break;
+        case 2: k_jacobi_vertex<2><<<blocks, 256, 0, s>>>(a); break;
+        case 3: k_jacobi_vertex<3><<<blocks, 256, 0, s>>>(a); break;
+        case 4: k_jacobi_vertex<4><<<blocks, 256, 0, s>>>(a); break;
+        case 5: k_jacobi_vertex<5><<<blocks, 256, 0, s>>>(a); break;
+        case 6: k_jacobi_vertex<6><<<blocks, 256, 0, s>>>(a); break;
+        default: k_jacobi_vertex<7><<<blocks, 256, 0, s>>>(a); break;
+    }
+}
+
+// Step prologue: f = (0, -g m, 0); s = x + h v + f / (M/h^2); base = b = (M/h^2) s.
+__global__ void __launch_bounds__(256) k_begin(BeginArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nv) return;
+    const float4 x = a.x[i], v = a.v[i], cf = __ldg(&a.coef[i]);
+    const float dt2_m_1 = 1.0f / cf.x;
+    const float fy = -a.gravity * cf.w;
+    float4 s;
+    s.x = x.x + a.dt * v.x + dt2_m_1 * 0.0f;
+    s.y = x.y + a.dt * v.y + dt2_m_1 * fy;
+    s.z = x.z + a.dt * v.z + dt2_m_1 * 0.0f;
+    s.w = 0.f;
+    a.sn[i] = s;
+    const float4 bs = make_float4(cf.x * s.x, cf.x * s.y, cf.x * s.z, 0.f);
+    a.base[i] = bs;
+    a.b[i] = bs;
+}
+
+void launch_begin(const BeginArgs& a, cudaStream_t s) {
+    const int blocks = (a.nv + 255) / 256;
+    if (blocks) k_begin<<<blocks, 256, 0, s>>>(a);
+}
+
+// ------------------------------------------------------- state transfer
+__global__ void k_gather_state(int nv, const int* __restrict__ vperm, const float* __restrict__ X,
+                               const float* __restrict__ V, float4* x, float4* v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const int o = vperm[i];
+    x[i] = make_float4(X[3 * o], X[3 * o + 1], X[3 * o + 2], 0.f);
+    if (V) v[i] = make_float4(V[3 * o], V[3 * o + 1], V[3 * o + 2], 0.f);
+    else v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_scatter_state(int nv, const int* __restrict__ vperm, const float4* __restrict__ x,
+                                const float4* __restrict__ v, float* X, float* V) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const int o = vperm[i];
+    if (X) {
+        const float4 p = x[i];
+        X[3 * o] = p.x; X[3 * o + 1] = p.y; X[3 * o + 2] = p.z;
+    }
+    if (V) {
+        const float4 q = v[i];
+        V[3 * o] = q.x; V[3 * o + 1] = q.y; V[3 * o + 2] = q.z;
+    }
+}
+
+__global__ void k_copy_x0(int nv, const float4* __restrict__ x0, float4* x, float4* v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    x[i] = x0[i];
+    v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+void launch_gather_state(int nv, const int* vperm, const float* X, const float* V, float4* x, float4* v,
+                         cudaStream_t s) {
+    if (nv > 0) k_gather_state<<<(nv + 255) / 256, 256, 0, s>>>(nv, vperm, X, V, x, v);
+}
+void launch_scatter_state(int nv, const int* vperm, const float4* x, const float4* v, float* X, float* V,
+                          cudaStream_t s) {
+    if (nv > 0) k_scatter_state<<<(nv + 255) / 256, 256, 0, s>>>(nv, vperm, x, v, X, V);
+}
+void launch_copy_x0(int nv, const float4* x0, float4* x, float4* v, cudaStream_t s) {
+    if (nv > 0) k_copy_x0<<<(nv + 255) / 256, 256, 0, s>>>(nv, x0, x, v);
+}
+
+}  // namespace pdgb

@@ -1,0 +1,230 @@
+// Host-side layout of a PD system for the engine's kernels.
+//
+// Reference counterparts: the per-tet precompute of FEMSolver's constructor
+// (femSolver.cu:7-17 -> computeInvDmV0, solverUtil.cuh:108-138) and the
+// per-vertex coefficients of PdSolver::SolverPrepare (pdUtil.cu:9-54).
+// What is new here is the data layout: vertices and tets are renumbered
+// along a Morton curve, tets are cut into tiles whose vertex "patch" fits in
+// shared memory, and each tet stores 16-bit patch-local corner ids.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "engine.h"
+
+namespace pdgb {
+
+namespace {
+
+inline uint64_t spread_bits21(uint64_t x) {
+    x &= 0x1fffffULL;
+    x = (x | (x << 32)) & 0x1f00000000ffffULL;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffULL;
+    x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
+    x = (x | (x << 2)) & 0x1249249249249249ULL;
+    return x;
+}
+
+struct Quantizer {
+    double lo[3], scale[3];
+    Quantizer(int nv, const float* X) {
+        double hi[3];
+        for (int d = 0; d < 3; ++d) { lo[d] = 1e300; hi[d] = -1e300; }
+        for (int v = 0; v < nv; ++v)
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = std::min(lo[d], (double)X[3 * v + d]);
+                hi[d] = std::max(hi[d], (double)X[3 * v + d]);
+            }
+        double ext = 0;
+        for (int d = 0; d < 3; ++d) ext = std::max(ext, hi[d] - lo[d]);
+        if (!(ext > 0)) ext = 1;
+        for (int d = 0; d < 3; ++d) scale[d] = 2097151.0 / ext;
+    }
+    uint64_t key(double x, double y, double z) const {
+        auto q = [&](double v, int d) {
+            double t = (v - lo[d]) * scale[d];
+            if (!(t > 0)) t = 0;
+            if (t > 2097151.0) t = 2097151.0;
+            return (uint64_t)t;
+        };
+        return spread_bits21(q(x, 0)) | (spread_bits21(q(y, 1)) << 1) | (spread_bits21(q(z, 2)) << 2);
+    }
+};
+
+}  // namespace
+
+std::vector<float> chebyshev_omegas(int n, float rho) {
+    std::vector<float> w(std::max(n, 0));
+    float omega = 1.0f;
+    for (int i = 0; i < n; ++i) {
+        if (i <= 10) omega = 1;
+        else if (i == 11) omega = 2 / (2 - rho * rho);
+        else omega = 4 / (4 - rho * rho * omega);
+        w[i] = omega;
+    }
+    return w;
+}
+
+void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const float* mass, const float* mu,
+                  const float* dbc, const pdgb_params& prm, HostLayout& L) {
+    if (nv <= 0 || nt <= 0) throw Error{PDGB_ERR_INVALID_ARGUMENT, "num_verts and num_tets must be positive"};
+    for (size_t i = 0; i < (size_t)4 * nt; ++i)
+        if (tets[i] >= (uint32_t)nv)
+            throw Error{PDGB_ERR_BAD_MESH, "tet " + std::to_string(i / 4) + " references vertex " +
+                                               std::to_string(tets[i]) + " >= num_verts"};
+    for (size_t i = 0; i < (size_t)3 * nv; ++i)
+        if (!std::isfinite(X0[i])) throw Error{PDGB_ERR_NONFINITE, "non-finite rest position"};
+    L.nv = nv;
+    L.nt = nt;
+    Quantizer qz(nv, X0);
+    // ---- vertex order
+    {
+        std::vector<std::pair<uint64_t, int>> key(nv);
+        for (int v = 0; v < nv; ++v) key[v] = {qz.key(X0[3 * v], X0[3 * v + 1], X0[3 * v + 2]), v};
+        std::sort(key.begin(), key.end());
+        L.vperm.resize(nv);
+        L.viperm.resize(nv);
+        for (int i = 0; i < nv; ++i) {
+            L.vperm[i] = key[i].second;
+            L.viperm[key[i].second] = i;
+        }
+    }
+    // ---- tet order (centroid Morton)
+    {
+        std::vector<std::pair<uint64_t, int>> key(nt);
+        for (int t = 0; t < nt; ++t) {
+            double c[3] = {0, 0, 0};
+            for (int k = 0; k < 4; ++k)
+                for (int d = 0; d < 3; ++d) c[d] += 0.25 * X0[3 * (size_t)tets[4 * (size_t)t + k] + d];
+            key[t] = {qz.key(c[0], c[1], c[2]), t};
+        }
+        std::sort(key.begin(), key.end());
+        L.tperm.resize(nt);
+        for (int i = 0; i < nt; ++i) L.tperm[i] = key[i].second;
+    }
+    L.tets_int.resize((size_t)4 * nt);
+    for (int i = 0; i < nt; ++i)
+        for (int k = 0; k < 4; ++k) L.tets_int[4 * (size_t)i + k] = (uint32_t)L.viperm[tets[4 * (size_t)L.tperm[i] + k]];
+    // ---- geometry: DmInv and V0 * w (solverUtil.cuh:98-138, pdUtil.cu:19)
+    L.nt_pad = (nt + 31) & ~31;
+    L.geo.assign((size_t)10 * L.nt_pad, 0.f);
+    L.dminv_d.resize((size_t)9 * nt);
+    L.coef_d.resize(nt);
+    for (int i = 0; i < nt; ++i) {
+        const int t = L.tperm[i];
+        const uint32_t* id = tets + 4 * (size_t)t;
+        double D[3][3];
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 3; ++r) D[r][c] = (double)X0[3 * (size_t)id[c + 1] + r] - (double)X0[3 * (size_t)id[0] + r];
+        const double det = D[0][0] * (D[1][1] * D[2][2] - D[1][2] * D[2][1]) -
+                           D[0][1] * (D[1][0] * D[2][2] - D[1][2] * D[2][0]) +
+                           D[0][2] * (D[1][0] * D[2][1] - D[1][1] * D[2][0]);
+        if (!(det != 0.0) || !std::isfinite(det))
+            throw Error{PDGB_ERR_BAD_MESH, "tet " + std::to_string(t) + " has zero rest volume"};
+        double inv[9];
+        inv[0] = (D[1][1] * D[2][2] - D[1][2] * D[2][1]) / det;
+        inv[1] = (D[0][2] * D[2][1] - D[0][1] * D[2][2]) / det;
+        inv[2] = (D[0][1] * D[1][2] - D[0][2] * D[1][1]) / det;
+        inv[3] = (D[1][2] * D[2][0] - D[1][0] * D[2][2]) / det;
+        inv[4] = (D[0][0] * D[2][2] - D[0][2] * D[2][0]) / det;
+        inv[5] = (D[0][2] * D[1][0] - D[0][0] * D[1][2]) / det;
+        inv[6] = (D[1][0] * D[2][1] - D[1][1] * D[2][0]) / det;
+        inv[7] = (D[0][1] * D[2][0] - D[0][0] * D[2][1]) / det;
+        inv[8] = (D[0][0] * D[1][1] - D[0][1] * D[1][0]) / det;
+        const double coef = std::fabs(det) / 6.0 * (double)mu[t];
+        for (int k = 0; k < 9; ++k) {
+            L.dminv_d[9 * (size_t)i + k] = inv[k];
+            L.geo[(size_t)k * L.nt_pad + i] = (float)inv[k];
+        }
+        L.coef_d[i] = coef;
+        L.geo[(size_t)9 * L.nt_pad + i] = (float)coef;
+    }
+    // ---- tiles: greedy runs of Morton-ordered tets, cut at kTileTets tets or
+    // when the patch would exceed kMaxPatch vertices.
+    constexpr int kTileTets = 2 * kLocalThreads;
+    L.tile_tet_ptr.assign(1, 0);
+    L.tile_vptr.assign(1, 0);
+    L.tile_verts.clear();
+    L.tet_local.assign(L.nt_pad, make_uint2(0, 0));
+    std::vector<int> mark(nv, -1), loc(nv, 0);
+    std::vector<int> patch;
+    patch.reserve(kMaxPatch);
+    int tile = 0, start = 0;
+    auto close_tile = [&](int end) {
+        std::sort(patch.begin(), patch.end());
+        for (int k = 0; k < (int)patch.size(); ++k) loc[patch[k]] = k;
+        for (int i = start; i < end; ++i) {
+            const uint32_t* id = &L.tets_int[4 * (size_t)i];
+            uint32_t a0 = loc[id[0]], a1 = loc[id[1]], a2 = loc[id[2]], a3 = loc[id[3]];
+            L.tet_local[i] = make_uint2(a0 | (a1 << 16), a2 | (a3 << 16));
+        }
+        L.tile_verts.insert(L.tile_verts.end(), patch.begin(), patch.end());
+        L.tile_vptr.push_back((int)L.tile_verts.size());
+        L.tile_tet_ptr.push_back(end);
+        patch.clear();
+        ++tile;
+        start = end;
+    };
+    for (int i = 0; i < nt; ++i) {
+        const uint32_t* id = &L.tets_int[4 * (size_t)i];
+        int fresh = 0;
+        for (int k = 0; k < 4; ++k) {
+            bool dup = mark[id[k]] == tile;
+            for (int j = 0; j < k; ++j) dup = dup || id[j] == id[k];
+            fresh += !dup;
+        }
+        if (i - start == kTileTets || (int)patch.size() + fresh > kMaxPatch) close_tile(i);
+        for (int k = 0; k < 4; ++k)
+            if (mark[id[k]] != tile) {
+                mark[id[k]] = tile;
+                patch.push_back((int)id[k]);
+            }
+    }
+    close_tile(nt);
+    L.ntiles = tile;
+    // ---- rest positions (internal order)
+    L.x0.resize(nv);
+    for (int i = 0; i < nv; ++i) {
+        const int o = L.vperm[i];
+        L.x0[i] = make_float4(X0[3 * o], X0[3 * o + 1], X0[3 * o + 2], 0.f);
+    }
+    build_vertex_coefficients(mass, dbc, prm, L);
+}
+
+void build_vertex_coefficients(const float* mass, const float* dbc, const pdgb_params& prm, HostLayout& L) {
+    const int nv = L.nv, nt = L.nt;
+    // stiffness diagonal: sum_t c_t (B_t^T B_t)_jj  (pdUtil.cu:21-24)
+    std::vector<double> md(nv, 0.0);
+    for (int i = 0; i < nt; ++i) {
+        const double* D = &L.dminv_d[9 * (size_t)i];
+        double B[3][4];
+        for (int r = 0; r < 3; ++r) {
+            B[r][1] = D[0 * 3 + r];
+            B[r][2] = D[1 * 3 + r];
+            B[r][3] = D[2 * 3 + r];
+            B[r][0] = -(B[r][1] + B[r][2] + B[r][3]);
+        }
+        for (int j = 0; j < 4; ++j)
+            md[L.tets_int[4 * (size_t)i + j]] += L.coef_d[i] * (B[0][j] * B[0][j] + B[1][j] * B[1][j] + B[2][j] * B[2][j]);
+    }
+    const float dt = prm.dt;
+    const float dt2 = dt * dt;
+    const float dtInv = 1.0f / dt;
+    const float dt2Inv = dtInv * dtInv;
+    const float wpin = prm.positional_weight * dt2Inv;
+    L.coef.resize(nv);
+    L.pin_rhs.resize(nv);
+    for (int i = 0; i < nv; ++i) {
+        const int o = L.vperm[i];
+        const float m = mass[o];
+        const float pin = dbc ? dbc[o] : 0.f;
+        const float mdt2 = (m + pin * prm.positional_weight) / dt2;  // setMDt_2, pdUtil.cu:48
+        L.coef[i] = make_float4(mdt2, (float)md[i], pin > 0.f ? 1.f : 0.f, m);
+        const float4 x0 = L.x0[i];
+        L.pin_rhs[i] = make_float4(x0.x * wpin, x0.y * wpin, x0.z * wpin, 0.f);  // computeDBCLocal, pdUtil.cu:155-157
+    }
+}
+
+}  // namespace pdgb

@@ -1,0 +1,146 @@
+"""ctypes binding of the pdgb C ABI (include/pdgb.h).
+
+The engine lives in ``_lib/libpdgb.so`` next to this file.  There is no
+fallback: if the library is missing or cannot load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpdgb.so"
+
+PDGB_OK = 0
+PDGB_ERR_INVALID_ARGUMENT = 1
+PDGB_ERR_BAD_MESH = 2
+PDGB_ERR_NOT_SPD = 3
+PDGB_ERR_CUDA = 4
+PDGB_ERR_OUT_OF_MEMORY = 5
+PDGB_ERR_NONFINITE = 6
+PDGB_ERR_UNSUPPORTED = 7
+PDGB_ERR_TIMEOUT = 8
+PDGB_ERR_NOT_FOUND = 9
+PDGB_ERR_BUSY = 10
+
+PDGB_MEM_HOST = 0
+PDGB_MEM_DEVICE = 1
+PDGB_SOLVER_JACOBI = 0
+PDGB_SOLVER_CHOLESKY = 1
+
+
+class pdgb_params(C.Structure):
+    _fields_ = [
+        ("dt", C.c_float),
+        ("gravity", C.c_float),
+        ("num_iterations", C.c_int),
+        ("tol", C.c_float),
+        ("rho", C.c_float),
+        ("positional_weight", C.c_float),
+        ("solver", C.c_int),
+        ("refine_steps", C.c_int),
+    ]
+
+
+class pdgb_mesh_desc(C.Structure):
+    _fields_ = [
+        ("num_verts", C.c_int),
+        ("num_tets", C.c_int),
+        ("X", C.c_void_p),
+        ("V", C.c_void_p),
+        ("tets", C.c_void_p),
+        ("mass", C.c_void_p),
+        ("mu", C.c_void_p),
+        ("dbc", C.c_void_p),
+        ("memory", C.c_int),
+    ]
+
+
+class pdgb_perf(C.Structure):
+    _fields_ = [
+        ("prepare_ms", C.c_double),
+        ("steps", C.c_double),
+        ("iterations", C.c_double),
+        ("factor_nnz", C.c_longlong),
+        ("tiles", C.c_longlong),
+        ("patch_verts", C.c_longlong),
+    ]
+
+
+class pdgb_timing(C.Structure):
+    _fields_ = [
+        ("step_ms", C.c_double),
+        ("steps", C.c_longlong),
+        ("local_ms", C.c_double),
+        ("local_launches", C.c_longlong),
+    ]
+
+
+class pdgb_layout_info(C.Structure):
+    _fields_ = [
+        ("num_tiles", C.c_int),
+        ("max_patch", C.c_int),
+        ("max_tile_tets", C.c_int),
+        ("reserved", C.c_int),
+        ("patch_verts", C.c_longlong),
+    ]
+
+
+# name -> (restype, argtypes); every symbol include/pdgb.h declares.
+SIGNATURES = {
+    "pdgb_default_params": (None, [C.POINTER(pdgb_params)]),
+    "pdgb_create": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_params), C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pdgb_prepare": (C.c_int, [C.c_void_p]),
+    "pdgb_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_set_solver": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_set_params": (C.c_int, [C.c_void_p, C.POINTER(pdgb_params)]),
+    "pdgb_upload_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "pdgb_download_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "pdgb_reset": (C.c_int, [C.c_void_p]),
+    "pdgb_get_perf": (C.c_int, [C.c_void_p, C.POINTER(pdgb_perf)]),
+    "pdgb_last_step_iterations": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "pdgb_synchronize": (C.c_int, [C.c_void_p]),
+    "pdgb_enable_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_read_timing": (C.c_int, [C.c_void_p, C.POINTER(pdgb_timing)]),
+    "pdgb_local_step_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "pdgb_destroy": (C.c_int, [C.c_void_p]),
+    "pdgb_stream": (C.c_void_p, [C.c_void_p]),
+    "pdgb_status_string": (C.c_char_p, [C.c_int]),
+    "pdgb_last_error": (C.c_char_p, []),
+    "pdgb_version": (C.c_char_p, []),
+    "pdgb_inspect_layout": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_layout_info), C.c_void_p,
+                                      C.c_void_p]),
+}
+
+_lib = None
+
+
+class PdgbError(RuntimeError):
+    def __init__(self, status: int, where: str, message: str):
+        super().__init__(f"{where}: {message} (status {status})")
+        self.status = status
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def lib() -> C.CDLL:
+    """Loads libpdgb.so (raises if it is not built)."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise RuntimeError(f"pdgb native library not built: {_LIB_PATH} is missing; run "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        h = C.CDLL(str(_LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = h
+    return _lib
+
+
+def check(status: int, where: str) -> None:
+    if status != PDGB_OK:
+        msg = lib().pdgb_last_error().decode(errors="replace")
+        raise PdgbError(status, where, msg or lib().pdgb_status_string(status).decode())

@@ -1,0 +1,113 @@
+"""Build recipes for the native parts of the repository.
+
+- ``libpdgb.so``: the engine (CUDA kernels for sm_103a + C ABI), compiled with
+  nvcc, one translation unit per process in parallel, then linked.
+- ``oracle/liboracle.so``: the CPU oracle (test infrastructure), g++.
+- ``oracle/_ref/libref_pd.so``: the reference's own PD kernels compiled as
+  C++ (only where the reference sources are present; test infrastructure).
+
+Nothing here downloads anything; the only tools used are nvcc and g++.
+"""
+from __future__ import annotations
+
+import concurrent.futures as _cf
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent
+ROOT = PKG_DIR.parent.parent
+CSRC = PKG_DIR.parent / "csrc"
+LIB_DIR = PKG_DIR / "_lib"
+LIB_PATH = LIB_DIR / "libpdgb.so"
+ORACLE_DIR = ROOT / "oracle"
+ORACLE_LIB = ORACLE_DIR / "_build" / "liboracle.so"
+
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str], cwd: Path | None = None) -> None:
+    proc = subprocess.run(cmd, cwd=cwd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError(f"command failed ({proc.returncode}): {' '.join(cmd)}\n{proc.stdout}")
+
+
+def _stale(target: Path, sources: list[Path]) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(s.stat().st_mtime > t for s in sources)
+
+
+def engine_sources() -> list[Path]:
+    return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
+
+
+def build_engine(force: bool = False, verbose: bool = False) -> Path:
+    srcs = engine_sources()
+    deps = srcs + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "pdgb.h"]
+    if not force and not _stale(LIB_PATH, deps):
+        return LIB_PATH
+    nvcc = _nvcc()
+    obj_dir = LIB_DIR / "obj"
+    obj_dir.mkdir(parents=True, exist_ok=True)
+    common = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+                           "-I", str(ROOT / "include")]
+
+    def compile_one(src: Path) -> Path:
+        obj = obj_dir / (src.name + ".o")
+        cmd = [nvcc] + common + ["-c", str(src), "-o", str(obj)]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        _run(cmd)
+        return obj
+
+    with _cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB_PATH.with_suffix(".so.tmp")
+    _run([nvcc] + ARCH_FLAGS + ["-shared", "-o", str(tmp)] + [str(o) for o in objs] + ["-lcudart"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_oracle(force: bool = False) -> Path:
+    src = ORACLE_DIR / "pd_oracle.cpp"
+    deps = [src, ORACLE_DIR / "pd_oracle.h"]
+    if not force and not _stale(ORACLE_LIB, deps):
+        return ORACLE_LIB
+    ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
+    tmp = ORACLE_LIB.with_suffix(".so.tmp")
+    _run(["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", str(src), "-o", str(tmp)])
+    os.replace(tmp, ORACLE_LIB)
+    return ORACLE_LIB
+
+
+def build_reference_harness(force: bool = False) -> Path | None:
+    """Builds oracle/_ref from the reference's sources when they are present."""
+    script = ORACLE_DIR / "build_ref.sh"
+    ref_root = Path(os.environ.get("PDGB_REFERENCE_ROOT", "/root/reference"))
+    if not ref_root.exists() or not script.exists():
+        return None
+    out = ORACLE_DIR / "_ref" / "libref_pd.so"
+    deps = [script, ORACLE_DIR / "refshim" / "shim.h", ORACLE_DIR / "refshim" / "ref_harness.cpp",
+            ORACLE_DIR / "pd_oracle.cpp"]
+    if not force and not _stale(out, [d for d in deps if d.exists()]):
+        return out
+    _run(["bash", str(script), str(ref_root)], cwd=ORACLE_DIR)
+    return out if out.exists() else None
+
+
+def build_all(force: bool = False) -> None:
+    with _cf.ThreadPoolExecutor(max_workers=3) as ex:
+        futs = [ex.submit(build_engine, force), ex.submit(build_oracle, force),
+                ex.submit(build_reference_harness, force)]
+        for f in futs:
+            f.result()

@@ -1,0 +1,151 @@
+"""Python mirror of the reference's PD solver interface over the C ABI.
+
+``PdSolver`` follows the reference's ``PdSolver`` (pdSolver.h:12-44) and
+``Solver<float>`` (solver.h:11-28): construct from a system, ``update``
+advances one step (prepares on first use), ``set_global_solver`` switches
+between Jacobi+Chebyshev and Cholesky, ``reset`` restores the rest shape,
+``get_performance_data`` reports timings.  All compute happens in
+``libpdgb.so``; this module only moves numpy arrays across the C ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+from .mesh import SoftBody
+
+
+class SolverType:
+    """Mirrors PdSolver::SolverType (pdSolver.h:14-17)."""
+
+    Jacobi = N.PDGB_SOLVER_JACOBI
+    CuSolverCholesky = N.PDGB_SOLVER_CHOLESKY
+    EigenCholesky = N.PDGB_SOLVER_CHOLESKY
+    Cholesky = N.PDGB_SOLVER_CHOLESKY
+
+
+@dataclass
+class SolverParams:
+    """Mirrors SolverParams<float> (def.h:82-100) for the fields PD reads."""
+
+    dt: float = 1.0 / 120.0
+    gravity: float = 9.8
+    num_iterations: int = 10
+    tol: float = 0.0
+    rho: float = 0.9992
+    positional_weight: float = 1e6
+    solver: int = SolverType.Jacobi
+    refine_steps: int = 0
+
+    def to_c(self) -> N.pdgb_params:
+        return N.pdgb_params(self.dt, self.gravity, self.num_iterations, self.tol, self.rho,
+                             self.positional_weight, self.solver, self.refine_steps)
+
+
+def _ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
+
+
+class PdSolver:
+    def __init__(self, body: SoftBody, params: SolverParams, stream: int | None = None):
+        self._lib = N.lib()
+        self.params = params
+        self.body = body
+        X = np.ascontiguousarray(body.X, dtype=np.float32)
+        tets = np.ascontiguousarray(body.tets, dtype=np.uint32)
+        mass = np.ascontiguousarray(body.mass, dtype=np.float32)
+        mu = np.ascontiguousarray(body.mu, dtype=np.float32)
+        dbc = None if body.dbc is None else np.ascontiguousarray(body.dbc, dtype=np.float32)
+        V = None if body.V is None else np.ascontiguousarray(body.V, dtype=np.float32)
+        desc = N.pdgb_mesh_desc(X.shape[0], tets.shape[0], _ptr(X), _ptr(V), _ptr(tets), _ptr(mass), _ptr(mu),
+                                _ptr(dbc), N.PDGB_MEM_HOST)
+        h = C.c_void_p()
+        prm = params.to_c()
+        N.check(self._lib.pdgb_create(C.byref(desc), C.byref(prm), stream, C.byref(h)), "pdgb_create")
+        self._h = h
+        self.num_verts = X.shape[0]
+        self.num_tets = tets.shape[0]
+
+    # -- Solver<float> interface
+    def prepare(self) -> None:
+        N.check(self._lib.pdgb_prepare(self._h), "pdgb_prepare")
+
+    def update(self, nsteps: int = 1) -> None:
+        N.check(self._lib.pdgb_step(self._h, int(nsteps)), "pdgb_step")
+
+    def set_global_solver(self, solver: int) -> None:
+        N.check(self._lib.pdgb_set_solver(self._h, int(solver)), "pdgb_set_solver")
+        self.params.solver = int(solver)
+
+    def set_params(self, params: SolverParams) -> None:
+        prm = params.to_c()
+        N.check(self._lib.pdgb_set_params(self._h, C.byref(prm)), "pdgb_set_params")
+        self.params = params
+
+    def reset(self) -> None:
+        N.check(self._lib.pdgb_reset(self._h), "pdgb_reset")
+
+    def synchronize(self) -> None:
+        N.check(self._lib.pdgb_synchronize(self._h), "pdgb_synchronize")
+
+    # -- state
+    def upload_state(self, X: np.ndarray, V: np.ndarray | None = None) -> None:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        V = None if V is None else np.ascontiguousarray(V, dtype=np.float32)
+        N.check(self._lib.pdgb_upload_state(self._h, _ptr(X), _ptr(V), N.PDGB_MEM_HOST), "pdgb_upload_state")
+        self.synchronize()
+
+    def download_state(self) -> tuple[np.ndarray, np.ndarray]:
+        X = np.empty((self.num_verts, 3), dtype=np.float32)
+        V = np.empty((self.num_verts, 3), dtype=np.float32)
+        N.check(self._lib.pdgb_download_state(self._h, _ptr(X), _ptr(V), N.PDGB_MEM_HOST), "pdgb_download_state")
+        return X, V
+
+    def get_performance_data(self) -> dict:
+        p = N.pdgb_perf()
+        N.check(self._lib.pdgb_get_perf(self._h, C.byref(p)), "pdgb_get_perf")
+        return {"prepare_ms": p.prepare_ms, "steps": p.steps, "iterations": p.iterations,
+                "factor_nnz": p.factor_nnz, "tiles": p.tiles, "patch_verts": p.patch_verts}
+
+    def last_step_iterations(self) -> int:
+        it = C.c_int()
+        N.check(self._lib.pdgb_last_step_iterations(self._h, C.byref(it)), "pdgb_last_step_iterations")
+        return it.value
+
+    # -- measurement hooks
+    def enable_kernel_timing(self, on: bool = True) -> None:
+        N.check(self._lib.pdgb_enable_kernel_timing(self._h, int(bool(on))), "pdgb_enable_kernel_timing")
+
+    def read_timing(self) -> dict:
+        t = N.pdgb_timing()
+        N.check(self._lib.pdgb_read_timing(self._h, C.byref(t)), "pdgb_read_timing")
+        return {"step_ms": t.step_ms, "steps": t.steps, "local_ms": t.local_ms, "local_launches": t.local_launches}
+
+    def local_step_bytes(self) -> float:
+        b = C.c_double()
+        N.check(self._lib.pdgb_local_step_bytes(self._h, C.byref(b)), "pdgb_local_step_bytes")
+        return b.value
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.pdgb_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

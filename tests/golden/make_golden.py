@@ -1,0 +1,105 @@
+"""Generates the golden PD fixtures in this directory.
+
+Each case runs the REFERENCE's own PD kernels (src/simulation/solver/
+projective/pdUtil.cu, compiled for the CPU into oracle/_ref by
+oracle/build_ref.sh) through its PdSolver step order, on a small seeded
+synthetic body, and stores inputs and outputs:
+
+  X0, tets, mass, mu, dbc        the system (SolverData<float> arrays)
+  params                         dt, gravity, iterations, tol, rho, solver
+  X, V                           state after `steps` steps
+  iters                          local/global iterations run per step
+
+Also `rotations.npz`: random deformation gradients (including inverted and
+nearly flat ones) with the reference's rotation R = U V^T (svd.cuh:7-14 +
+pdUtil.cu:113-122).
+
+The reference's Cholesky branch calls cuSOLVER; the CPU harness solves the
+same 3n x 3n system exactly in double instead.
+
+Usage (needs the reference sources to build oracle/_ref):
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT / "soft-body-simulation-cuda_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+from pdgb import mesh  # noqa: E402
+from pdgb.engine import SolverParams  # noqa: E402
+import oracle as O  # noqa: E402
+
+CASES = {
+    # name: (body factory, params, steps)
+    "tet1_jacobi": (lambda: mesh.single_tet(mass=0.5, mu=2e3),
+                    SolverParams(num_iterations=20, rho=0.9992, solver=0), 40),
+    "grid3_jacobi": (lambda: mesh.make_grid_body(3, 3, 3, young=1e5, poisson=0.4, jitter=0.1, seed=11),
+                     SolverParams(num_iterations=20, rho=0.9995, solver=0), 30),
+    "grid3_chol": (lambda: mesh.make_grid_body(3, 3, 3, young=1e5, poisson=0.4, jitter=0.1, seed=11),
+                   SolverParams(num_iterations=10, solver=1), 30),
+    "grid3_chol_tol": (lambda: mesh.make_grid_body(3, 3, 3, young=1e5, poisson=0.4, jitter=0.1, seed=11),
+                       SolverParams(num_iterations=10, tol=2e-4, solver=1), 30),
+    "grid435_soft_jacobi": (lambda: mesh.make_grid_body(4, 3, 5, young=2e4, poisson=0.3, jitter=0.15, seed=5,
+                                                        size=(0.4, 0.3, 0.5)),
+                            SolverParams(num_iterations=14, rho=0.999, solver=0), 40),
+    "c1_chol": (mesh.cube_c1, SolverParams(num_iterations=10, solver=1), 10),
+    "c1_jacobi": (mesh.cube_c1, SolverParams(num_iterations=20, rho=0.9995, solver=0), 10),
+}
+
+
+def make_case(name: str) -> Path:
+    factory, params, steps = CASES[name]
+    body = factory()
+    X, V, iters = O.reference_simulate(body, params, steps)
+    out = HERE / f"{name}.npz"
+    np.savez_compressed(
+        out, X0=body.X, tets=body.tets, mass=body.mass, mu=body.mu, dbc=body.dbc,
+        dt=np.float32(params.dt), gravity=np.float32(params.gravity), num_iterations=np.int32(params.num_iterations),
+        tol=np.float32(params.tol), rho=np.float32(params.rho), solver=np.int32(params.solver),
+        steps=np.int32(steps), X=X, V=V, iters=iters)
+    return out
+
+
+def make_rotations() -> Path:
+    rng = np.random.default_rng(7)
+    n = 256
+    F = []
+    for k in range(n):
+        Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        if np.linalg.det(Q) < 0:
+            Q[:, 0] = -Q[:, 0]
+        W, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        s = np.exp(rng.uniform(-1.0, 1.0, size=3))
+        if k % 8 == 3:
+            s[2] = -s[2] * 0.3  # inverted
+        if k % 16 == 7:
+            s[2] = 1e-4        # nearly flat
+        if k % 32 == 5:
+            s = np.array([1.0, 1.0, 1.0]) + rng.uniform(-1e-3, 1e-3, 3)  # near-rotation
+        F.append(Q @ np.diag(s) @ W.T)
+    F = np.asarray(F, dtype=np.float32)
+    R = O.reference_rotation(F)
+    out = HERE / "rotations.npz"
+    np.savez_compressed(out, F=F, R=R)
+    return out
+
+
+def main() -> None:
+    if not O.reference_available():
+        raise SystemExit("oracle/_ref/libref_pd.so is missing: build it with oracle/build_ref.sh")
+    for name in CASES:
+        p = make_case(name)
+        print("wrote", p.relative_to(ROOT), p.stat().st_size, "bytes")
+    p = make_rotations()
+    print("wrote", p.relative_to(ROOT), p.stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main()

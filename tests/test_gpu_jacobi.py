@@ -1,0 +1,183 @@
+"""GPU parity of the Jacobi + Chebyshev PD path (libpdgb.so through the C ABI).
+
+Bar: vertex positions after N steps within 1e-4 relative L2 of (a) the
+reference's own kernels (golden fixtures) and (b) the FP64 oracle.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden, rel_l2
+
+import oracle as O
+from pdgb import PdgbError, PdSolver, SolverParams, mesh
+from pdgb import _native as N
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if c.endswith("jacobi")])
+def test_engine_matches_reference_fixture(name):
+    body, params, steps, Xg, Vg, _ = load_golden(name)
+    with PdSolver(body, params) as e:
+        e.update(steps)
+        X, V = e.download_state()
+    assert np.isfinite(X).all() and np.isfinite(V).all()
+    assert rel_l2(X, Xg) < TOL
+    assert rel_l2(X - body.X, Xg - body.X) < 2e-3
+    Xo, _, _ = O.simulate(body, params, steps, precision=64)
+    assert rel_l2(X, Xo) < TOL
+
+
+def test_engine_vs_fp64_oracle_jittered_grid():
+    body = mesh.make_grid_body(16, 12, 14, young=1e6, poisson=0.45, jitter=0.1, seed=21)
+    params = SolverParams(num_iterations=20, rho=0.9995, solver=0)
+    with PdSolver(body, params) as e:
+        e.update(25)
+        X, V = e.download_state()
+    Xo, Vo, _ = O.simulate(body, params, 25, precision=64)
+    assert rel_l2(X, Xo) < TOL
+    assert rel_l2(X - body.X, Xo - body.X) < 1e-3
+    assert rel_l2(V, Vo) < 1e-2
+
+
+def test_large_grid_first_steps_vs_oracle():
+    """64^3 cells (274,625 verts / 1,310,720 tets): 2 steps vs the FP64 oracle."""
+    body = mesh.cube_c2()
+    params = SolverParams(num_iterations=20, rho=0.9995, solver=0)
+    with PdSolver(body, params) as e:
+        e.update(2)
+        X, V = e.download_state()
+    Xo, Vo, _ = O.simulate(body, params, 2, precision=64)
+    assert rel_l2(X, Xo) < TOL
+    assert rel_l2(X - body.X, Xo - body.X) < 1e-3
+
+
+def test_pinned_vertices_hold_and_body_sags():
+    body = mesh.make_grid_body(8, 8, 8, young=1e5, poisson=0.4)
+    params = SolverParams(num_iterations=20, rho=0.9995, solver=0)
+    with PdSolver(body, params) as e:
+        e.update(30)
+        X, _ = e.download_state()
+    pinned = body.dbc > 0
+    assert np.abs(X[pinned] - body.X[pinned]).max() < 1e-5
+    assert (X[~pinned, 1] <= body.X[~pinned, 1] + 1e-6).all()  # gravity pulls down
+    assert (X[~pinned, 1] < body.X[~pinned, 1] - 1e-4).any()
+
+
+def test_rigid_motion_is_preserved():
+    """No gravity, no pins, rest shape rigidly rotated and moved: R = Q, F = Q, so
+    every PD term is zero and the body must not move."""
+    body = mesh.make_grid_body(5, 6, 7, jitter=0.1, seed=2, pin=None)
+    rng = np.random.default_rng(4)
+    Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    if np.linalg.det(Q) < 0:
+        Q[:, 0] *= -1
+    Xm = (body.X.astype(np.float64) @ Q.T + np.array([0.3, -1.0, 2.0])).astype(np.float32)
+    params = SolverParams(num_iterations=20, rho=0.9995, gravity=0.0, solver=0)
+    with PdSolver(body, params) as e:
+        e.upload_state(Xm, np.zeros_like(Xm))
+        e.update(10)
+        X, V = e.download_state()
+    assert np.abs(X - Xm).max() < 2e-5
+    assert np.abs(V).max() < 2e-3
+
+
+def test_state_roundtrip_reset_and_reprepare():
+    body = mesh.make_grid_body(4, 5, 6, jitter=0.1, seed=8)
+    params = SolverParams(num_iterations=12, rho=0.999, solver=0)
+    rng = np.random.default_rng(0)
+    with PdSolver(body, params) as e:
+        Xr = (body.X + rng.normal(scale=1e-3, size=body.X.shape)).astype(np.float32)
+        Vr = rng.normal(scale=1e-2, size=body.X.shape).astype(np.float32)
+        e.upload_state(Xr, Vr)
+        X, V = e.download_state()
+        assert np.array_equal(X, Xr) and np.array_equal(V, Vr)
+        e.update(5)
+        X1, _ = e.download_state()
+        e.reset()
+        X, V = e.download_state()
+        assert np.array_equal(X, body.X) and not V.any()
+        e.upload_state(Xr, Vr)
+        e.update(5)
+        X2, _ = e.download_state()
+        assert rel_l2(X2, X1) < 1e-6  # same result after reset + re-prepare
+        # changing params re-prepares: iterations change the result
+        e.set_params(SolverParams(num_iterations=20, rho=0.999, solver=0))
+        e.upload_state(Xr, Vr)
+        e.update(5)
+        X3, _ = e.download_state()
+        Xo, _, _ = O.simulate(body, SolverParams(num_iterations=20, rho=0.999, solver=0), 5, 64, X=Xr, V=Vr)
+        assert rel_l2(X3, Xo) < TOL
+
+
+def test_bad_inputs_raise():
+    body = mesh.make_grid_body(2, 2, 2)
+    bad = mesh.make_grid_body(2, 2, 2)
+    bad.tets = bad.tets.copy()
+    bad.tets[0, 0] = 10_000
+    with pytest.raises(PdgbError) as ei:
+        PdSolver(bad, SolverParams())
+    assert ei.value.status == N.PDGB_ERR_BAD_MESH
+    with pytest.raises(PdgbError) as ei:
+        PdSolver(body, SolverParams(dt=-1.0))
+    assert ei.value.status == N.PDGB_ERR_INVALID_ARGUMENT
+    with pytest.raises(PdgbError):
+        PdSolver(body, SolverParams(num_iterations=0))
+
+
+def test_mesh_from_device_memory():
+    torch = pytest.importorskip("torch")
+    body = mesh.make_grid_body(5, 5, 5, jitter=0.1, seed=5)
+    params = SolverParams(num_iterations=20, rho=0.9995, solver=0)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(body, k))).cuda() for k in ("X", "tets", "mass", "mu", "dbc")}
+    torch.cuda.synchronize()
+    lib = N.lib()
+    desc = N.pdgb_mesh_desc(body.num_verts, body.num_tets, dev["X"].data_ptr(), None, dev["tets"].data_ptr(),
+                            dev["mass"].data_ptr(), dev["mu"].data_ptr(), dev["dbc"].data_ptr(), N.PDGB_MEM_DEVICE)
+    h = C.c_void_p()
+    prm = params.to_c()
+    N.check(lib.pdgb_create(C.byref(desc), C.byref(prm), None, C.byref(h)), "create")
+    try:
+        N.check(lib.pdgb_step(h, 8), "step")
+        Xd = torch.empty((body.num_verts, 3), dtype=torch.float32, device="cuda")
+        N.check(lib.pdgb_download_state(h, Xd.data_ptr(), None, N.PDGB_MEM_DEVICE), "download")
+        N.check(lib.pdgb_synchronize(h), "sync")
+        X = Xd.cpu().numpy()
+    finally:
+        lib.pdgb_destroy(h)
+    with PdSolver(body, params) as e:
+        e.update(8)
+        Xh, _ = e.download_state()
+    assert rel_l2(X, Xh) < 1e-6
+
+
+def test_independent_engines_do_not_interfere():
+    a = mesh.make_grid_body(6, 6, 6, jitter=0.1, seed=1)
+    b = mesh.make_grid_body(9, 4, 7, young=3e5, jitter=0.1, seed=2)
+    pa = SolverParams(num_iterations=20, rho=0.9995, solver=0)
+    pb = SolverParams(num_iterations=15, rho=0.999, solver=0)
+    with PdSolver(a, pa) as ea, PdSolver(b, pb) as eb:
+        for _ in range(6):
+            ea.update(1)
+            eb.update(1)
+        Xa, _ = ea.download_state()
+        Xb, _ = eb.download_state()
+    Xa1, _, _ = O.simulate(a, pa, 6, 64)
+    Xb1, _, _ = O.simulate(b, pb, 6, 64)
+    assert rel_l2(Xa, Xa1) < TOL and rel_l2(Xb, Xb1) < TOL
+
+
+def test_kernel_timing_hook_counts_launches():
+    body = mesh.make_grid_body(8, 8, 8)
+    params = SolverParams(num_iterations=7, rho=0.999, solver=0)
+    with PdSolver(body, params) as e:
+        e.enable_kernel_timing(True)
+        e.update(3)
+        t = e.read_timing()
+        assert t["local_launches"] == 21 and t["steps"] == 3
+        assert 0 < t["local_ms"] < t["step_ms"]
+        assert e.local_step_bytes() == 56.0 * body.num_tets + 36.0 * body.num_verts
