@@ -35,15 +35,28 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "soft-body-simulation-cuda_gb300"))
 
-WORKLOAD = {
-    "workload": "pd_jacobi_cube64",
-    "desc": "64^3 hex grid x5 tets (274625 v / 1310720 t), jitter 0.1 cell seed 2024, E=1e6 nu=0.45 rho=1000, "
-            "top face pinned, dt=1/120, Jacobi+Chebyshev rho=0.9995, 20 iterations/step",
-    "grid": 64,
-    "iterations": 20,
-    "rho": 0.9995,
-    "l2": "flushed between timed steps (256 MB write)",
+WORKLOADS = {
+    "c2": {
+        "workload": "pd_jacobi_cube64",
+        "desc": "64^3 hex grid x5 tets (274625 v / 1310720 t), jitter 0.1 cell seed 2024, E=1e6 nu=0.45 rho=1000, "
+                "top face pinned, dt=1/120, Jacobi+Chebyshev rho=0.9995, 20 iterations/step",
+        "grid": 64, "iterations": 20, "rho": 0.9995, "solver": "jacobi",
+    },
+    "c1": {
+        "workload": "pd_cholesky_cube10",
+        "desc": "10^3 hex grid x5 tets (1331 v / 5000 t), E=1e5 nu=0.4 rho=1000, top face pinned, dt=1/120, "
+                "prefactored sparse Cholesky (AMD), 10 iterations/step",
+        "grid": 10, "iterations": 10, "solver": "cholesky",
+    },
+    "c3": {
+        "workload": "pd_cholesky_hetero40",
+        "desc": "40^3 hex grid x5 tets (68921 v / 320000 t), per-tet E log-uniform 1e4..1e7 (seed 3), nu U[0.3,0.45], "
+                "rho=1000, top face pinned, dt=1/120, prefactored sparse Cholesky (AMD, FP64 factor, FP32 solves), "
+                "10 iterations/step",
+        "grid": 40, "iterations": 10, "solver": "cholesky",
+    },
 }
+WORKLOAD = None
 METRIC = "PD tet-iterations/s"
 UNIT = "tet-iter/s"
 
@@ -154,9 +167,9 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch():
+def ncu_traffic_per_launch(workload: str):
     """DRAM bytes per local-step launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "local_kernel_cube64.json"
+    p = ROOT / "profiles" / f"k_local_{workload}.json"
     if p.exists():
         try:
             return float(json.loads(p.read_text())["dram_bytes_per_launch"])
@@ -219,13 +232,23 @@ def run_reference_arm(args, body, params):
     print(json.dumps(line), flush=True)
 
 
+def launches_per_step(info, params) -> int:
+    """Kernels of one step graph: prologue, per iteration local + global
+    (Jacobi: 1 vertex kernel; Cholesky: 2 per solve level + 1 vertex kernel),
+    Cholesky epilogue."""
+    if params.solver == 0:
+        return 1 + 2 * params.num_iterations
+    return 2 + params.num_iterations * (2 + 2 * info["levels"])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pdgb", choices=["pdgb", "reference"])
-    ap.add_argument("--grid", type=int, default=64, help="cells per axis (64 = the benchmark workload)")
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--grid", type=int, default=0, help="override cells per axis (profiling of smaller cases)")
     ap.add_argument("--cpu-steps", type=int, default=4, help="PD steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -235,11 +258,22 @@ def main():
     from pdgb import mesh
     from pdgb.engine import SolverParams
 
-    body = mesh.cube_c2(n=args.grid)
-    params = SolverParams(num_iterations=WORKLOAD["iterations"], rho=WORKLOAD["rho"], solver=0)
-    if args.grid != 64:
+    global WORKLOAD
+    WORKLOAD = dict(WORKLOADS[args.workload])
+    WORKLOAD["l2"] = "flushed between timed steps (256 MB write)"
+    if args.grid:
         WORKLOAD["grid"] = args.grid
-        WORKLOAD["workload"] = f"pd_jacobi_cube{args.grid}"
+        WORKLOAD["workload"] += f"_grid{args.grid}"
+    n = WORKLOAD["grid"]
+    if args.workload == "c2":
+        body = mesh.cube_c2(n=n)
+        params = SolverParams(num_iterations=WORKLOAD["iterations"], rho=WORKLOAD["rho"], solver=0)
+    elif args.workload == "c1":
+        body = mesh.make_grid_body(n, n, n, young=1e5, poisson=0.4, density=1000.0)
+        params = SolverParams(num_iterations=WORKLOAD["iterations"], solver=1)
+    else:
+        body = mesh.cube_c3(n=n)
+        params = SolverParams(num_iterations=WORKLOAD["iterations"], solver=1)
 
     if args.impl == "reference":
         run_reference_arm(args, body, params)
@@ -313,6 +347,8 @@ def main():
     e2e_max = reduce_max(dist, e2e_s)
     e2e_value = tet_iters / e2e_max
     finite = bool(torch.isfinite(Xh).all().item())
+    eng_info = eng.get_performance_data()
+    eng_info["levels"] = eng.solve_levels() if params.solver == 1 else 0
     eng.close()
 
     if rank != 0:
@@ -321,7 +357,7 @@ def main():
     bytes_per_launch = 56.0 * body.num_tets + 36.0 * body.num_verts
     avg_local_s = (local_ms / 1e3) / max(local_launches, 1)
     achieved = bytes_per_launch / avg_local_s / 1e9
-    traffic = ncu_traffic_per_launch() if args.grid == 64 else None
+    traffic = ncu_traffic_per_launch(WORKLOAD["workload"])
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(body, params, args.cpu_steps)
@@ -347,7 +383,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
                 "d2h_bytes_per_step": 2 * 3 * 4 * nv},
-        "gpu_launches": args.steps * (1 + 2 * params.num_iterations),
+        "gpu_launches": args.steps * launches_per_step(eng_info, params),
         "clocks": clk,
         "finite": finite,
         "local_step_share": (local_ms / 1e3) / t_local if t_local > 0 else None,

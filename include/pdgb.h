@@ -177,6 +177,43 @@ typedef struct pdgb_layout_info {
 } pdgb_layout_info;
 int pdgb_inspect_layout(const pdgb_mesh_desc* mesh, pdgb_layout_info* info, int* vperm, int* tperm);
 
+/* Ordering of the Cholesky factor (default AMD, as the reference's
+ * cusolverSpXcsrsymamdHost, cholesky.cu:88-91).  Takes effect at the next
+ * prepare. */
+#define PDGB_ORDER_AMD 0
+#define PDGB_ORDER_ND 1 /* geometric nested dissection */
+int pdgb_set_ordering(pdgb_engine* e, int ordering);
+
+/* Rotation of the local step.  QUAT (default): the closest proper rotation
+ * from the dominant eigenvector of Horn's 4x4 quaternion matrix, converged to
+ * float precision.  SVD: the reference's scheme -- 4 approximate-Givens
+ * Jacobi sweeps of a McAdams-style 3x3 SVD, R = U V^T (svd.cuh:7-14,
+ * pdUtil.cu:113-122) -- which is not fully converged on stretched elements. */
+#define PDGB_ROTATION_QUAT 0
+#define PDGB_ROTATION_SVD 1
+int pdgb_set_rotation(pdgb_engine* e, int rotation);
+
+/* Host-only check of the Cholesky factor for a mesh (no GPU needed): builds
+ * the system for params (dt, pin weight), orders and factors it, and applies
+ * the factor on the host exactly as the GPU solve does (double):
+ * x = K^-1 b for 3 interleaved right-hand sides in caller vertex order. */
+typedef struct pdgb_factor_info {
+    long long nnz_L;        /* nonzeros of the scalar factor                  */
+    long long m_entries;    /* stored FP32 entries of the M_s blocks          */
+    int num_supernodes;
+    int num_levels;         /* levels of the supernodal elimination tree     */
+    int fwd_items;          /* GPU work items, forward pass                   */
+    int bwd_items;          /* GPU work items, backward pass                  */
+    double flops;           /* factorisation flops (approx.)                  */
+    double factor_ms;       /* host time of ordering + factorisation         */
+} pdgb_factor_info;
+/* Factor statistics of a prepared engine on the Cholesky path (zeros
+ * otherwise). */
+int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info);
+
+int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params, int ordering, const double* b,
+                           double* x, pdgb_factor_info* info);
+
 /* Library version string. */
 const char* pdgb_version(void);
 

@@ -3,14 +3,16 @@
 // An engine is the GB300 counterpart of one PdSolver bound to one
 // SolverData<float> (pdSolver.h:12-44): it owns a device copy of the mesh in
 // its own layout, the solver scratch, and a CUDA graph holding one full time
-// step (prologue, num_iterations x (local kernel, global kernel), velocity /
+// step (prologue, num_iterations x (local kernel, global solve), velocity /
 // position update), replayed by pdgb_step.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
-#include <algorithm>
 #include <cstring>
 
+#include "cholesky.h"
 #include "engine.h"
+#include "solve.h"
 
 namespace pdgb {
 
@@ -27,6 +29,8 @@ using namespace pdgb;
 
 struct pdgb_engine {
     pdgb_params prm{};
+    int ordering = PDGB_ORDER_AMD;
+    int rotation = PDGB_ROTATION_QUAT;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int nv = 0, nt = 0;
@@ -37,13 +41,23 @@ struct pdgb_engine {
     HostLayout L;
     bool prepared = false;
     // device: mesh
-    DBuf<uint2> tet_local;
+    DBuf<uint16_t> inc_ent, inc_end;
     DBuf<float> geo;
-    DBuf<int> tile_tet_ptr, tile_vptr, tile_verts, vperm;
+    DBuf<int> tile_tet_ptr, tile_vptr, vperm;
+    DBuf<uint32_t> tile_verts;
     DBuf<float4> coef, pin_rhs, x0;
     // device: state + scratch
-    DBuf<float4> x, v, sn, prev, base, b;
+    DBuf<float4> x, v, sn, prev, base, b, y;
     DBuf<float> staging;  // [6 nv] host <-> device transfers
+    DBuf<StepState> st;   // convergence state of the Cholesky path
+    // Cholesky factor
+    CholFactor chol;
+    int chol_ordering = -1;
+    float chol_dt = 0.f, chol_pw = -1.f;
+    DBuf<int> ch_fwd, ch_bwd, ch_sk, ch_sm, ch_roff, ch_rows;
+    DBuf<int64_t> ch_moff;
+    DBuf<float> ch_mval;
+    double factor_ms = 0.0;
     // step graph
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -92,10 +106,10 @@ void check_params(const pdgb_params& p) {
         throw Error{PDGB_ERR_INVALID_ARGUMENT, "unknown solver"};
     if (p.refine_steps < 0 || p.refine_steps > 3) throw Error{PDGB_ERR_INVALID_ARGUMENT, "refine_steps must be 0..3"};
     if (!(p.positional_weight >= 0.f)) throw Error{PDGB_ERR_INVALID_ARGUMENT, "positional_weight must be >= 0"};
+    if (!(p.tol >= 0.f)) throw Error{PDGB_ERR_INVALID_ARGUMENT, "tol must be >= 0"};
 }
 
-template <class T>
-void copy_in(std::vector<T>& dst, const T* src, size_t n, int memory) {
+template <class T> void copy_in(std::vector<T>& dst, const T* src, size_t n, int memory) {
     dst.resize(n);
     if (n == 0) return;
     if (memory == PDGB_MEM_DEVICE) PDGB_CUDA_TRY(cudaMemcpy(dst.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost));
@@ -109,40 +123,100 @@ void destroy_graph(pdgb_engine* e) {
     e->graph = nullptr;
 }
 
-LocalArgs local_args(pdgb_engine* e) {
+LocalArgs local_args(pdgb_engine* e, const int* done) {
     LocalArgs a;
     a.sn = e->sn.p;
     a.b = e->b.p;
-    a.tet_local = e->tet_local.p;
+    a.inc_ent = e->inc_ent.p;
+    a.inc_end = e->inc_end.p;
     a.geo = e->geo.p;
     a.tile_tet_ptr = e->tile_tet_ptr.p;
     a.tile_vptr = e->tile_vptr.p;
     a.tile_verts = e->tile_verts.p;
     a.nt_pad = e->L.nt_pad;
+    a.done = done;
     return a;
 }
 
-// Records one time step of the Jacobi-Chebyshev path on the stream.
+BeginArgs begin_args(pdgb_engine* e) {
+    BeginArgs ba{};
+    ba.nv = e->nv;
+    ba.x = e->x.p;
+    ba.v = e->v.p;
+    ba.coef = e->coef.p;
+    ba.pin_rhs = e->pin_rhs.p;
+    ba.sn = e->sn.p;
+    ba.base = e->base.p;
+    ba.b = e->b.p;
+    ba.dt = e->prm.dt;
+    ba.gravity = e->prm.gravity;
+    ba.vperm = e->vperm.p;
+    ba.num_iterations = e->prm.num_iterations;
+    return ba;
+}
+
+void record_local(pdgb_engine* e, const LocalArgs& la, bool jacobi_form, int i) {
+    cudaStream_t s = e->stream;
+    if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i], s, cudaEventRecordExternal));
+    launch_local(la, e->L.ntiles, jacobi_form, e->rotation, s);
+    if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i + 1], s, cudaEventRecordExternal));
+}
+
+// One time step of the Jacobi-Chebyshev path (pdSolver.cu:141-208, Jacobi).
 void record_jacobi_step(pdgb_engine* e) {
     cudaStream_t s = e->stream;
     const int n = e->prm.num_iterations;
-    BeginArgs ba{e->nv, e->x.p, e->v.p, e->coef.p, e->sn.p, e->base.p, e->b.p, e->prm.dt, e->prm.gravity};
-    launch_begin(ba, s);
+    launch_begin(begin_args(e), s);
     const std::vector<float> omega = chebyshev_omegas(n, e->prm.rho);
-    const LocalArgs la = local_args(e);
+    const LocalArgs la = local_args(e, nullptr);
     VertexArgs va{e->nv, e->sn.p, e->prev.p, e->b.p, e->base.p, e->coef.p, e->pin_rhs.p, e->x.p, e->v.p, 1.f,
                   1.0f / e->prm.dt};
     for (int i = 0; i < n; ++i) {
-        if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i], s, cudaEventRecordExternal));
-        launch_local(la, e->L.ntiles, true, s);
-        if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i + 1], s, cudaEventRecordExternal));
+        record_local(e, la, true, i);
         int mode = 0;
-        if (i >= 11) mode |= kReadPrev;                 // omega != 1 from iteration 11 on
-        if (i >= 10 && i + 1 < n) mode |= kWritePrev;   // prev is read from iteration 11 on
+        if (i >= 11) mode |= kReadPrev;                // omega != 1 from iteration 11 on
+        if (i >= 10 && i + 1 < n) mode |= kWritePrev;  // prev is read from iteration 11 on
         if (i + 1 == n) mode |= kFinal;
         va.omega = omega[i];
         launch_jacobi_vertex(va, mode, s);
     }
+}
+
+// One time step of the Cholesky path (pdSolver.cu:141-208, cuSOLVER branch).
+void record_chol_step(pdgb_engine* e) {
+    cudaStream_t s = e->stream;
+    const int n = e->prm.num_iterations;
+    const bool use_tol = e->prm.tol > 0.f;
+    StepState* st = e->st.p;
+    BeginArgs ba = begin_args(e);
+    ba.done = &st->done;
+    ba.iterations = &st->iterations;
+    ba.prev = use_tol ? e->prev.p : nullptr;
+    launch_begin(ba, s);
+    const LocalArgs la = local_args(e, &st->done);
+    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_sk.p, e->ch_sm.p, e->ch_moff.p, e->ch_roff.p, e->ch_rows.p,
+                e->ch_mval.p, e->b.p, e->y.p, e->sn.p, &st->done};
+    CholVertexArgs cv{};
+    cv.nv = e->nv;
+    cv.tol = e->prm.tol;
+    cv.st = st;
+    cv.prev = e->prev.p;
+    cv.sn = e->sn.p;
+    cv.y = e->y.p;
+    cv.b = e->b.p;
+    cv.base = e->base.p;
+    cv.coef = e->coef.p;
+    cv.pin_rhs = e->pin_rhs.p;
+    cv.x = e->x.p;
+    cv.v = e->v.p;
+    cv.dt_inv = 1.0f / e->prm.dt;
+    for (int i = 0; i < n; ++i) {
+        record_local(e, la, false, i);
+        launch_chol_solve(ca, e->chol.levels, s);
+        cv.iteration = i;
+        launch_chol_vertex(cv, s);
+    }
+    launch_chol_finish(cv, s);
 }
 
 void build_graph(pdgb_engine* e) {
@@ -158,7 +232,7 @@ void build_graph(pdgb_engine* e) {
     PDGB_CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     try {
         if (e->prm.solver == PDGB_SOLVER_JACOBI) record_jacobi_step(e);
-        else throw Error{PDGB_ERR_UNSUPPORTED, "Cholesky global solve not built in this library"};
+        else record_chol_step(e);
     } catch (...) {
         cudaGraph_t g = nullptr;
         cudaStreamEndCapture(e->stream, &g);
@@ -172,7 +246,8 @@ void build_graph(pdgb_engine* e) {
 void upload_mesh(pdgb_engine* e) {
     const HostLayout& L = e->L;
     cudaStream_t s = e->stream;
-    e->tet_local.upload(L.tet_local, s);
+    e->inc_ent.upload(L.inc_ent, s);
+    e->inc_end.upload(L.inc_end, s);
     e->geo.upload(L.geo, s);
     e->tile_tet_ptr.upload(L.tile_tet_ptr, s);
     e->tile_vptr.upload(L.tile_vptr, s);
@@ -186,10 +261,51 @@ void upload_mesh(pdgb_engine* e) {
     e->prev.alloc(nv);
     e->base.alloc(nv);
     e->b.alloc(nv);
+    e->y.alloc(nv);
     e->coef.alloc(nv);
     e->pin_rhs.alloc(nv);
     e->staging.alloc(6 * nv);
+    e->st.alloc(1);
     PDGB_CUDA_TRY(cudaMemsetAsync(e->prev.p, 0, nv * sizeof(float4), s));
+    PDGB_CUDA_TRY(cudaMemsetAsync(e->y.p, 0, nv * sizeof(float4), s));
+    PDGB_CUDA_TRY(cudaMemsetAsync(e->st.p, 0, sizeof(StepState), s));
+}
+
+// Scalar system K of the engine's vertex order, from the float coefficients
+// the kernels use (M/h^2 incl. the pin weight) and the double geometry.
+SparseSym engine_system(const HostLayout& L) {
+    std::vector<double> mdt2(L.nv);
+    for (int i = 0; i < L.nv; ++i) mdt2[i] = (double)L.coef[i].x;
+    return assemble_system(L.nv, L.nt, L.tets_int.data(), L.dminv_d.data(), L.coef_d.data(), mdt2);
+}
+
+void prepare_cholesky(pdgb_engine* e) {
+    if (e->chol_ordering == e->ordering && e->chol_dt == e->prm.dt && e->chol_pw == e->prm.positional_weight &&
+        e->chol.n == e->nv)
+        return;  // the system matrix depends only on the mesh, dt and the pin weight
+    auto t0 = std::chrono::steady_clock::now();
+    SparseSym K = engine_system(e->L);
+    std::vector<float> xyz(3 * (size_t)e->nv);
+    for (int i = 0; i < e->nv; ++i) {
+        xyz[3 * i] = e->L.x0[i].x;
+        xyz[3 * i + 1] = e->L.x0[i].y;
+        xyz[3 * i + 2] = e->L.x0[i].z;
+    }
+    cholesky_factor(K, e->ordering, xyz.data(), e->chol);
+    e->factor_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    cudaStream_t s = e->stream;
+    const CholFactor& f = e->chol;
+    e->ch_fwd.upload(f.fwd_items, s);
+    e->ch_bwd.upload(f.bwd_items, s);
+    e->ch_sk.upload(f.sk, s);
+    e->ch_sm.upload(f.sm, s);
+    e->ch_roff.upload(f.roff, s);
+    e->ch_rows.upload(f.rows, s);
+    e->ch_moff.upload(f.moff, s);
+    e->ch_mval.upload(f.mval, s);
+    e->chol_ordering = e->ordering;
+    e->chol_dt = e->prm.dt;
+    e->chol_pw = e->prm.positional_weight;
 }
 
 void prepare(pdgb_engine* e) {
@@ -197,6 +313,8 @@ void prepare(pdgb_engine* e) {
     build_vertex_coefficients(e->mass.data(), e->has_dbc ? e->dbc.data() : nullptr, e->prm, e->L);
     e->coef.upload(e->L.coef, e->stream);
     e->pin_rhs.upload(e->L.pin_rhs, e->stream);
+    if (e->prm.solver == PDGB_SOLVER_CHOLESKY) prepare_cholesky(e);
+    PDGB_CUDA_TRY(cudaMemsetAsync(e->y.p, 0, (size_t)e->nv * sizeof(float4), e->stream));
     build_graph(e);
     PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
     e->prepared = true;
@@ -334,6 +452,30 @@ int pdgb_set_params(pdgb_engine* e, const pdgb_params* params) {
     });
 }
 
+int pdgb_set_ordering(pdgb_engine* e, int ordering) {
+    if (!e || (ordering != PDGB_ORDER_AMD && ordering != PDGB_ORDER_ND)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or ordering");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (ordering != e->ordering) {
+        e->ordering = ordering;
+        e->prepared = false;
+    }
+    return PDGB_OK;
+}
+
+int pdgb_set_rotation(pdgb_engine* e, int rotation) {
+    if (!e || (rotation != PDGB_ROTATION_QUAT && rotation != PDGB_ROTATION_SVD)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or rotation mode");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (rotation != e->rotation) {
+        e->rotation = rotation;
+        e->prepared = false;
+    }
+    return PDGB_OK;
+}
+
 int pdgb_upload_state(pdgb_engine* e, const float* X, const float* V, int memory) {
     if (!e || !X) return PDGB_ERR_INVALID_ARGUMENT;
     return guarded([&] {
@@ -379,6 +521,7 @@ int pdgb_reset(pdgb_engine* e) {
     if (!e) return PDGB_ERR_INVALID_ARGUMENT;
     return guarded([&] {
         launch_copy_x0(e->nv, e->x0.p, e->x.p, e->v.p, e->stream);
+        PDGB_CUDA_TRY(cudaMemsetAsync(e->prev.p, 0, (size_t)e->nv * sizeof(float4), e->stream));
         PDGB_CUDA_TRY(cudaGetLastError());
         e->prepared = false;
         e->steps_run = 0;
@@ -391,7 +534,7 @@ int pdgb_get_perf(pdgb_engine* e, pdgb_perf* out) {
     out->prepare_ms = e->prepare_ms;
     out->steps = e->steps_run;
     out->iterations = e->iters_run;
-    out->factor_nnz = 0;
+    out->factor_nnz = e->prm.solver == PDGB_SOLVER_CHOLESKY ? e->chol.nnz_L : 0;
     out->tiles = e->L.ntiles;
     out->patch_verts = (long long)e->L.tile_verts.size();
     return PDGB_OK;
@@ -399,8 +542,16 @@ int pdgb_get_perf(pdgb_engine* e, pdgb_perf* out) {
 
 int pdgb_last_step_iterations(pdgb_engine* e, int* iterations) {
     if (!e || !iterations) return PDGB_ERR_INVALID_ARGUMENT;
-    *iterations = e->prm.num_iterations;
-    return PDGB_OK;
+    return guarded([&] {
+        if (e->prm.solver != PDGB_SOLVER_CHOLESKY) {
+            *iterations = e->prm.num_iterations;
+            return;
+        }
+        StepState h{};
+        PDGB_CUDA_TRY(cudaMemcpyAsync(&h, e->st.p, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        *iterations = h.iterations;
+    });
 }
 
 int pdgb_synchronize(pdgb_engine* e) {
@@ -490,6 +641,66 @@ int pdgb_inspect_layout(const pdgb_mesh_desc* mesh, pdgb_layout_info* info, int*
     });
 }
 
-const char* pdgb_version(void) { return "pdgb 0.1 (sm_103a)"; }
+int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info) {
+    if (!e || !info) return PDGB_ERR_INVALID_ARGUMENT;
+    std::memset(info, 0, sizeof(*info));
+    if (e->prm.solver != PDGB_SOLVER_CHOLESKY || e->chol.n != e->nv) return PDGB_OK;
+    const CholFactor& f = e->chol;
+    info->nnz_L = f.nnz_L;
+    info->m_entries = (long long)f.mval.size();
+    info->num_supernodes = f.nsuper;
+    info->num_levels = f.nlevels;
+    info->fwd_items = (int)(f.fwd_items.size() / 4);
+    info->bwd_items = (int)(f.bwd_items.size() / 4);
+    info->flops = f.flops;
+    info->factor_ms = e->factor_ms;
+    return PDGB_OK;
+}
+
+int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params, int ordering, const double* b,
+                           double* x, pdgb_factor_info* info) {
+    if (!mesh || !params || mesh->memory != PDGB_MEM_HOST || !mesh->X || !mesh->tets || !mesh->mass || !mesh->mu) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "host mesh with X, tets, mass, mu and params required");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        check_params(*params);
+        HostLayout L;
+        build_layout(mesh->num_verts, mesh->num_tets, mesh->X, mesh->tets, mesh->mass, mesh->mu, mesh->dbc, *params,
+                     L);
+        auto t0 = std::chrono::steady_clock::now();
+        SparseSym K = engine_system(L);
+        std::vector<float> xyz(3 * (size_t)L.nv);
+        for (int i = 0; i < L.nv; ++i) {
+            xyz[3 * i] = L.x0[i].x;
+            xyz[3 * i + 1] = L.x0[i].y;
+            xyz[3 * i + 2] = L.x0[i].z;
+        }
+        CholFactor f;
+        cholesky_factor(K, ordering, xyz.data(), f);
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (info) {
+            info->nnz_L = f.nnz_L;
+            info->m_entries = (long long)f.mval.size();
+            info->num_supernodes = f.nsuper;
+            info->num_levels = f.nlevels;
+            info->fwd_items = (int)(f.fwd_items.size() / 4);
+            info->bwd_items = (int)(f.bwd_items.size() / 4);
+            info->flops = f.flops;
+            info->factor_ms = ms;
+        }
+        if (b && x) {
+            const int nv = L.nv;
+            std::vector<double> bi(3 * (size_t)nv), xi(3 * (size_t)nv);
+            for (int i = 0; i < nv; ++i)
+                for (int d = 0; d < 3; ++d) bi[3 * (size_t)i + d] = b[3 * (size_t)L.vperm[i] + d];
+            cholesky_solve_host(f, bi.data(), xi.data());
+            for (int i = 0; i < nv; ++i)
+                for (int d = 0; d < 3; ++d) x[3 * (size_t)L.vperm[i] + d] = xi[3 * (size_t)i + d];
+        }
+    });
+}
+
+const char* pdgb_version(void) { return "pdgb 0.2 (sm_103a)"; }
 
 }  // extern "C"

@@ -1,0 +1,661 @@
+// Sparse Cholesky of the scalar PD system (host side): ordering, symbolic
+// analysis, FP64 supernodal multifrontal factorisation and the per-supernode
+// M_s blocks of the GPU triangular solves.  See cholesky.h.
+#include "cholesky.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+
+#include "engine.h"
+
+namespace pdgb {
+
+// ------------------------------------------------------------ assembly
+SparseSym assemble_system(int nv, int nt, const uint32_t* tets4, const double* dminv, const double* coef,
+                          const std::vector<double>& mdt2) {
+    // count neighbours per row (with duplicates), then sort/merge per row
+    std::vector<int64_t> cnt(nv + 1, 0);
+    for (int t = 0; t < nt; ++t)
+        for (int a = 0; a < 4; ++a) cnt[tets4[4 * (size_t)t + a] + 1] += 4;
+    for (int v = 0; v < nv; ++v) cnt[v + 1] += cnt[v] + 1;  // + diagonal
+    std::vector<int> ci(cnt[nv]);
+    std::vector<double> cx(cnt[nv]);
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    for (int v = 0; v < nv; ++v) {
+        ci[fill[v]] = v;
+        cx[fill[v]++] = mdt2[v];
+    }
+    for (int t = 0; t < nt; ++t) {
+        const double* D = dminv + 9 * (size_t)t;
+        double B[3][4];
+        for (int r = 0; r < 3; ++r) {
+            B[r][1] = D[0 * 3 + r];
+            B[r][2] = D[1 * 3 + r];
+            B[r][3] = D[2 * 3 + r];
+            B[r][0] = -(B[r][1] + B[r][2] + B[r][3]);
+        }
+        const uint32_t* id = tets4 + 4 * (size_t)t;
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) {
+                const double s = coef[t] * (B[0][a] * B[0][b] + B[1][a] * B[1][b] + B[2][a] * B[2][b]);
+                ci[fill[id[a]]] = (int)id[b];
+                cx[fill[id[a]]++] = s;
+            }
+    }
+    SparseSym K;
+    K.n = nv;
+    K.p.assign(nv + 1, 0);
+    K.i.reserve(cnt[nv] / 2);
+    K.x.reserve(cnt[nv] / 2);
+    std::vector<std::pair<int, double>> row;
+    for (int v = 0; v < nv; ++v) {
+        row.clear();
+        for (int64_t e = cnt[v]; e < cnt[v + 1]; ++e) row.push_back({ci[e], cx[e]});
+        std::sort(row.begin(), row.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        int last = -1;
+        for (auto& e : row) {
+            if (e.first == last) K.x.back() += e.second;
+            else {
+                K.i.push_back(e.first);
+                K.x.push_back(e.second);
+                last = e.first;
+            }
+        }
+        K.p[v + 1] = (int64_t)K.i.size();
+    }
+    return K;
+}
+
+// ------------------------------------------------------------------ AMD
+std::vector<int> amd_order(const SparseSym& A) {
+    const int n = A.n;
+    enum : char { VAR = 0, ELEM = 1, DEAD = 2, MERGED = 3 };
+    std::vector<std::vector<int>> vars(n), elems(n), Le(n), merged(n);
+    std::vector<char> state(n, VAR);
+    std::vector<int> nv(n, 1), deg(n, 0), mark(n, 0), tmpdeg(n, 0);
+    std::vector<long long> w(n, 0);
+    for (int i = 0; i < n; ++i) {
+        for (int64_t e = A.p[i]; e < A.p[i + 1]; ++e)
+            if (A.i[e] != i) vars[i].push_back(A.i[e]);
+        deg[i] = (int)vars[i].size();
+    }
+    std::vector<int> head(n + 1, -1), nxt(n, -1), prv(n, -1);
+    auto ins = [&](int i) {
+        const int d = deg[i];
+        nxt[i] = head[d];
+        prv[i] = -1;
+        if (head[d] >= 0) prv[head[d]] = i;
+        head[d] = i;
+    };
+    auto rem = [&](int i) {
+        if (prv[i] >= 0) nxt[prv[i]] = nxt[i];
+        else head[deg[i]] = nxt[i];
+        if (nxt[i] >= 0) prv[nxt[i]] = prv[i];
+        nxt[i] = prv[i] = -1;
+    };
+    for (int i = 0; i < n; ++i) ins(i);
+    int k = 0, mindeg = 0, stamp = 0;
+    long long wflg = 1;
+    std::vector<int> order;
+    order.reserve(n);
+    std::vector<int> Lp, keep;
+    std::vector<std::pair<uint64_t, int>> hashed;
+    while (k < n) {
+        while (mindeg <= n && head[mindeg] < 0) ++mindeg;
+        if (mindeg > n) break;  // cannot happen while k < n
+        const int p = head[mindeg];
+        rem(p);
+        int nvp = nv[p];
+        // ---- new element p: Lp = A_p U (U_{e in E_p} L_e) \ {p}; absorb E_p
+        ++stamp;
+        mark[p] = stamp;
+        Lp.clear();
+        for (int j : vars[p])
+            if (state[j] == VAR && mark[j] != stamp) {
+                mark[j] = stamp;
+                Lp.push_back(j);
+            }
+        for (int e : elems[p])
+            if (state[e] == ELEM) {
+                for (int j : Le[e])
+                    if (state[j] == VAR && mark[j] != stamp) {
+                        mark[j] = stamp;
+                        Lp.push_back(j);
+                    }
+                state[e] = DEAD;
+                std::vector<int>().swap(Le[e]);
+            }
+        std::vector<int>().swap(vars[p]);
+        std::vector<int>().swap(elems[p]);
+        state[p] = ELEM;
+        for (int j : Lp) rem(j);
+        // ---- |L_e \ L_p| for every element adjacent to L_p (w trick)
+        for (int i : Lp)
+            for (int e : elems[i]) {
+                if (state[e] != ELEM) continue;
+                if (w[e] < wflg) {
+                    // first touch this round: prune and weigh L_e
+                    auto& L = Le[e];
+                    size_t q = 0;
+                    long long sz = 0;
+                    for (int j : L)
+                        if (state[j] == VAR) {
+                            L[q++] = j;
+                            sz += nv[j];
+                        }
+                    L.resize(q);
+                    w[e] = wflg + sz;
+                }
+                w[e] -= nv[i];
+            }
+        // ---- prune lists, aggressive absorption, mass elimination
+        keep.clear();
+        for (int i : Lp) {
+            auto& E = elems[i];
+            size_t q = 0;
+            long long de = 0;
+            for (int e : E) {
+                if (state[e] != ELEM) continue;
+                const long long we = w[e] - wflg;
+                if (we <= 0) {  // L_e inside L_p: absorb e into p
+                    state[e] = DEAD;
+                    std::vector<int>().swap(Le[e]);
+                } else {
+                    de += we;
+                    E[q++] = e;
+                }
+            }
+            E.resize(q);
+            auto& Av = vars[i];
+            q = 0;
+            long long da = 0;
+            for (int j : Av)
+                if (state[j] == VAR && mark[j] != stamp) {
+                    da += nv[j];
+                    Av[q++] = j;
+                }
+            Av.resize(q);
+            if (E.empty() && Av.empty()) {  // adjacent to p only: eliminate with p
+                state[i] = MERGED;
+                merged[p].push_back(i);
+                nvp += nv[i];
+                nv[i] = 0;
+                continue;
+            }
+            tmpdeg[i] = (int)std::min<long long>(de + da, n);
+            E.insert(E.begin(), p);
+            keep.push_back(i);
+        }
+        // ---- supervariables: identical (E_i, A_i) lists
+        hashed.clear();
+        for (int i : keep) {
+            uint64_t h = 1469598103934665603ULL;
+            uint64_t s = 0;
+            for (int e : elems[i]) s += (uint64_t)e * 2654435761ULL;
+            for (int j : vars[i]) s += (uint64_t)j * 40503ULL + 7;
+            h ^= s + ((uint64_t)elems[i].size() << 40) + ((uint64_t)vars[i].size() << 20);
+            hashed.push_back({h, i});
+        }
+        std::sort(hashed.begin(), hashed.end());
+        for (size_t a = 0; a < hashed.size();) {
+            size_t b = a + 1;
+            while (b < hashed.size() && hashed[b].first == hashed[a].first) ++b;
+            if (b - a > 1) {
+                for (size_t x = a; x < b; ++x) {
+                    const int i = hashed[x].second;
+                    if (state[i] != VAR) continue;
+                    std::vector<int> ei(elems[i]), vi(vars[i]);
+                    std::sort(ei.begin(), ei.end());
+                    std::sort(vi.begin(), vi.end());
+                    for (size_t y = x + 1; y < b; ++y) {
+                        const int j = hashed[y].second;
+                        if (state[j] != VAR) continue;
+                        if (elems[j].size() != ei.size() || vars[j].size() != vi.size()) continue;
+                        std::vector<int> ej(elems[j]), vj(vars[j]);
+                        std::sort(ej.begin(), ej.end());
+                        std::sort(vj.begin(), vj.end());
+                        if (ej == ei && vj == vi) {
+                            nv[i] += nv[j];
+                            nv[j] = 0;
+                            state[j] = MERGED;
+                            merged[i].push_back(j);
+                            std::vector<int>().swap(elems[j]);
+                            std::vector<int>().swap(vars[j]);
+                        }
+                    }
+                }
+            }
+            a = b;
+        }
+        // ---- approximate degrees and the new element's list
+        int degme = 0;
+        for (int i : keep)
+            if (state[i] == VAR) degme += nv[i];
+        const int remaining = n - k - nvp;
+        auto& Lnew = Le[p];
+        Lnew.clear();
+        for (int i : keep) {
+            if (state[i] != VAR) continue;
+            const int ext = degme - nv[i];
+            long long d = std::min<long long>((long long)deg[i] + ext, (long long)tmpdeg[i] + ext);
+            d = std::min<long long>(d, remaining - nv[i]);
+            deg[i] = (int)std::max<long long>(d, 0);
+            ins(i);
+            mindeg = std::min(mindeg, deg[i]);
+            Lnew.push_back(i);
+        }
+        order.push_back(p);
+        k += nvp;
+        nv[p] = nvp;
+        wflg += (long long)n + 2;
+    }
+    // expand supervariables / mass-eliminated variables after their pivot
+    std::vector<int> perm;
+    perm.reserve(n);
+    std::vector<int> stack;
+    for (int p : order) {
+        stack.assign(1, p);
+        while (!stack.empty()) {
+            const int v = stack.back();
+            stack.pop_back();
+            perm.push_back(v);
+            for (auto it = merged[v].rbegin(); it != merged[v].rend(); ++it) stack.push_back(*it);
+        }
+    }
+    if ((int)perm.size() != n) throw Error{PDGB_ERR_INVALID_ARGUMENT, "internal error: AMD ordering incomplete"};
+    return perm;
+}
+
+// ------------------------------------------------------ nested dissection
+static void nd_rec(std::vector<int>& vs, const SparseSym& A, const float* xyz, std::vector<int>& order,
+                   std::vector<int>& mark, int& stamp) {
+    if (vs.size() <= 32) {
+        order.insert(order.end(), vs.begin(), vs.end());
+        return;
+    }
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    for (int v : vs)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = std::min(lo[d], xyz[3 * v + d]);
+            hi[d] = std::max(hi[d], xyz[3 * v + d]);
+        }
+    int ax = 0;
+    for (int d = 1; d < 3; ++d)
+        if (hi[d] - lo[d] > hi[ax] - lo[ax]) ax = d;
+    const size_t half = vs.size() / 2;
+    std::nth_element(vs.begin(), vs.begin() + half, vs.end(), [&](int a, int b) {
+        const float xa = xyz[3 * a + ax], xb = xyz[3 * b + ax];
+        return xa < xb || (xa == xb && a < b);
+    });
+    const int my = ++stamp;
+    for (size_t q = 0; q < half; ++q) mark[vs[q]] = my;
+    std::vector<int> Lo(vs.begin(), vs.begin() + half), Hi, Sep;
+    for (size_t q = half; q < vs.size(); ++q) {
+        const int v = vs[q];
+        bool sep = false;
+        for (int64_t e = A.p[v]; e < A.p[v + 1] && !sep; ++e) sep = mark[A.i[e]] == my;
+        (sep ? Sep : Hi).push_back(v);
+    }
+    std::vector<int>().swap(vs);
+    nd_rec(Lo, A, xyz, order, mark, stamp);
+    nd_rec(Hi, A, xyz, order, mark, stamp);
+    order.insert(order.end(), Sep.begin(), Sep.end());
+}
+
+std::vector<int> nd_order(const SparseSym& A, const float* xyz) {
+    std::vector<int> vs(A.n), mark(A.n, 0), order;
+    std::iota(vs.begin(), vs.end(), 0);
+    order.reserve(A.n);
+    int stamp = 0;
+    nd_rec(vs, A, xyz, order, mark, stamp);
+    return order;
+}
+
+// ------------------------------------------------------- symbolic tools
+namespace {
+
+// Elimination tree of C = P A P^T (parent[j] > j or -1), Liu's algorithm.
+std::vector<int> etree(const SparseSym& A, const std::vector<int>& perm, const std::vector<int>& iperm) {
+    const int n = A.n;
+    std::vector<int> parent(n, -1), anc(n, -1);
+    for (int k = 0; k < n; ++k) {
+        const int v = perm[k];
+        for (int64_t e = A.p[v]; e < A.p[v + 1]; ++e) {
+            int i = iperm[A.i[e]];
+            while (i != -1 && i < k) {
+                const int nx = anc[i];
+                anc[i] = k;
+                if (nx == -1) {
+                    parent[i] = k;
+                    break;
+                }
+                i = nx;
+            }
+        }
+    }
+    return parent;
+}
+
+std::vector<int> postorder(const std::vector<int>& parent) {
+    const int n = (int)parent.size();
+    std::vector<int> head(n, -1), next(n, -1), post;
+    post.reserve(n);
+    for (int j = n - 1; j >= 0; --j)
+        if (parent[j] != -1) {
+            next[j] = head[parent[j]];
+            head[parent[j]] = j;
+        }
+    std::vector<int> stack;
+    for (int r = 0; r < n; ++r) {
+        if (parent[r] != -1) continue;
+        stack.push_back(r);
+        while (!stack.empty()) {
+            const int p = stack.back();
+            const int c = head[p];
+            if (c == -1) {
+                stack.pop_back();
+                post.push_back(p);
+            } else {
+                head[p] = next[c];
+                stack.push_back(c);
+            }
+        }
+    }
+    return post;
+}
+
+// Dense lower-triangular m x m front (column major, leading dimension m):
+// factor the first k columns in place (right-looking, blocked).
+bool partial_cholesky(double* F, int m, int k) {
+    constexpr int NB = 48;
+    for (int j0 = 0; j0 < k; j0 += NB) {
+        const int j1 = std::min(k, j0 + NB);
+        // panel
+        for (int j = j0; j < j1; ++j) {
+            double* cj = F + (size_t)j * m;
+            const double d = cj[j];
+            if (!(d > 0.0) || !std::isfinite(d)) return false;
+            const double l = std::sqrt(d);
+            cj[j] = l;
+            const double il = 1.0 / l;
+            for (int i = j + 1; i < m; ++i) cj[i] *= il;
+            for (int c = j + 1; c < j1; ++c) {
+                double* cc = F + (size_t)c * m;
+                const double f = cj[c];
+                for (int i = c; i < m; ++i) cc[i] -= cj[i] * f;
+            }
+        }
+        // trailing update with the panel: F[c:, c] -= sum_j L[c:, j] L[c, j]
+        const int nc = m - j1;
+        if (nc <= 0) continue;
+#pragma omp parallel for schedule(dynamic, 8) if ((long long)nc * nc * (j1 - j0) > 2000000)
+        for (int c = j1; c < m; ++c) {
+            double* cc = F + (size_t)c * m;
+            for (int j = j0; j < j1; ++j) {
+                const double* cj = F + (size_t)j * m;
+                const double f = cj[c];
+                if (f == 0.0) continue;
+                for (int i = c; i < m; ++i) cc[i] -= cj[i] * f;
+            }
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out) {
+    const int n = K.n;
+    out = CholFactor();
+    out.n = n;
+    out.K = K;
+    // ---- ordering, then postorder of the elimination tree
+    std::vector<int> perm0 = ordering == 1 ? nd_order(K, xyz) : amd_order(K);
+    std::vector<int> iperm(n);
+    for (int k = 0; k < n; ++k) iperm[perm0[k]] = k;
+    {
+        std::vector<int> parent = etree(K, perm0, iperm);
+        std::vector<int> post = postorder(parent);
+        std::vector<int> perm(n);
+        for (int k = 0; k < n; ++k) perm[k] = perm0[post[k]];
+        perm0.swap(perm);
+        for (int k = 0; k < n; ++k) iperm[perm0[k]] = k;
+    }
+    const std::vector<int>& perm = perm0;
+    std::vector<int> parent = etree(K, perm, iperm);
+    // ---- column counts via row subtrees (ereach)
+    std::vector<int> colcount(n, 1), wmark(n, -1), stk(n);
+    for (int k = 0; k < n; ++k) {
+        wmark[k] = k;
+        const int v = perm[k];
+        for (int64_t e = K.p[v]; e < K.p[v + 1]; ++e) {
+            int i = iperm[K.i[e]];
+            if (i >= k) continue;
+            for (; wmark[i] != k; i = parent[i]) {
+                wmark[i] = k;
+                colcount[i]++;
+            }
+        }
+    }
+    long long nnz = 0;
+    for (int j = 0; j < n; ++j) nnz += colcount[j];
+    out.nnz_L = nnz;
+    // ---- fundamental supernodes
+    std::vector<int> nchild(n, 0);
+    for (int j = 0; j < n; ++j)
+        if (parent[j] >= 0) nchild[parent[j]]++;
+    std::vector<int> sfirst;  // first column of each supernode
+    for (int j = 0; j < n; ++j) {
+        const bool cont = j > 0 && parent[j - 1] == j && colcount[j - 1] == colcount[j] + 1 && nchild[j] == 1;
+        if (!cont) sfirst.push_back(j);
+    }
+    const int ns = (int)sfirst.size();
+    sfirst.push_back(n);
+    std::vector<int> col2s(n);
+    for (int s = 0; s < ns; ++s)
+        for (int j = sfirst[s]; j < sfirst[s + 1]; ++j) col2s[j] = s;
+    std::vector<int> sparent(ns, -1);
+    for (int s = 0; s < ns; ++s) {
+        const int last = sfirst[s + 1] - 1;
+        if (parent[last] >= 0) sparent[s] = col2s[parent[last]];
+    }
+    // ---- row structures (symbolic multifrontal), in permuted indices
+    std::vector<std::vector<int>> sstruct(ns);
+    std::vector<std::vector<int>> schildren(ns);
+    for (int s = 0; s < ns; ++s)
+        if (sparent[s] >= 0) schildren[sparent[s]].push_back(s);
+    std::vector<int> smark(n, -1);
+    for (int s = 0; s < ns; ++s) {
+        const int f = sfirst[s], l = sfirst[s + 1];
+        std::vector<int>& st = sstruct[s];
+        for (int j = f; j < l; ++j) {
+            st.push_back(j);
+            smark[j] = s;
+        }
+        for (int j = f; j < l; ++j) {
+            const int v = perm[j];
+            for (int64_t e = K.p[v]; e < K.p[v + 1]; ++e) {
+                const int i = iperm[K.i[e]];
+                if (i >= l && smark[i] != s) {
+                    smark[i] = s;
+                    st.push_back(i);
+                }
+            }
+        }
+        for (int c : schildren[s])
+            for (int i : sstruct[c])
+                if (i >= l && smark[i] != s) {
+                    smark[i] = s;
+                    st.push_back(i);
+                }
+        std::sort(st.begin() + (l - f), st.end());
+        if ((int)st.size() != colcount[f])
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "internal error: supernode structure mismatch"};
+    }
+    // ---- numeric multifrontal factorisation (FP64) + M_s blocks
+    out.nsuper = ns;
+    out.sk.resize(ns);
+    out.sm.resize(ns);
+    out.moff.resize(ns + 1);
+    out.roff.resize(ns + 1);
+    out.level.assign(ns, 0);
+    int64_t mtot = 0, rtot = 0;
+    for (int s = 0; s < ns; ++s) {
+        out.sk[s] = sfirst[s + 1] - sfirst[s];
+        out.sm[s] = (int)sstruct[s].size();
+        out.moff[s] = mtot;
+        out.roff[s] = (int)rtot;
+        mtot += (int64_t)out.sk[s] * out.sm[s];
+        rtot += out.sm[s];
+    }
+    out.moff[ns] = mtot;
+    out.roff[ns] = (int)rtot;
+    out.mval.assign(mtot, 0.f);
+    out.rows.resize(rtot);
+    for (int s = 0; s < ns; ++s)
+        for (int q = 0; q < out.sm[s]; ++q) out.rows[out.roff[s] + q] = perm[sstruct[s][q]];
+    std::vector<std::vector<double>> upd(ns);  // update matrices (lower, column major)
+    std::vector<int> relpos(n, -1);
+    double flops = 0.0;
+    std::vector<double> F, Linv;
+    for (int s = 0; s < ns; ++s) {
+        const int k = out.sk[s], m = out.sm[s], f = sfirst[s];
+        const std::vector<int>& st = sstruct[s];
+        for (int q = 0; q < m; ++q) relpos[st[q]] = q;
+        F.assign((size_t)m * m, 0.0);
+        for (int jj = 0; jj < k; ++jj) {
+            const int v = perm[f + jj];
+            for (int64_t e = K.p[v]; e < K.p[v + 1]; ++e) {
+                const int i = iperm[K.i[e]];
+                if (i < f + jj) continue;
+                F[(size_t)jj * m + relpos[i]] += K.x[e];
+            }
+        }
+        for (int c : schildren[s]) {
+            const int kc = out.sk[c], mc = out.sm[c], uc = mc - kc;
+            const std::vector<int>& stc = sstruct[c];
+            const std::vector<double>& U = upd[c];
+            for (int b = 0; b < uc; ++b) {
+                const int cb = relpos[stc[kc + b]];
+                for (int a = b; a < uc; ++a) F[(size_t)cb * m + relpos[stc[kc + a]]] += U[(size_t)b * uc + a];
+            }
+            std::vector<double>().swap(upd[c]);
+        }
+        if (!partial_cholesky(F.data(), m, k))
+            throw Error{PDGB_ERR_NOT_SPD, "system matrix is not positive definite (pivot " + std::to_string(f) + ")"};
+        for (int jj = 0; jj < k; ++jj) flops += (double)(m - jj) * (m - jj);
+        const int u = m - k;
+        if (u > 0) {
+            upd[s].assign((size_t)u * u, 0.0);
+            for (int b = 0; b < u; ++b)
+                for (int a = b; a < u; ++a) upd[s][(size_t)b * u + a] = F[(size_t)(k + b) * m + k + a];
+        }
+        // Linv = L_ss^-1 (k x k lower, column major), column-oriented
+        // forward substitution on e_c; then W = L_os Linv by axpys over the
+        // contiguous columns of L.
+        Linv.assign((size_t)k * k, 0.0);
+        float* M = &out.mval[out.moff[s]];
+#pragma omp parallel for schedule(dynamic, 4) if ((long long)k * k * m > 4000000)
+        for (int c = 0; c < k; ++c) {
+            double* x = &Linv[(size_t)c * k];
+            x[c] = 1.0;
+            for (int q = c; q < k; ++q) {
+                const double* Lq = F.data() + (size_t)q * m;
+                const double xq = x[q] / Lq[q];
+                x[q] = xq;
+                if (xq != 0.0)
+                    for (int j = q + 1; j < k; ++j) x[j] -= Lq[j] * xq;
+            }
+            float* Mc = M + (size_t)c * m;
+            for (int r = 0; r < k; ++r) Mc[r] = (float)x[r];
+            if (m > k) {
+                std::vector<double> acc(m - k, 0.0);
+                for (int q = c; q < k; ++q) {
+                    const double* Lq = F.data() + (size_t)q * m;
+                    const double xq = x[q];
+                    if (xq == 0.0) continue;
+                    for (int r = k; r < m; ++r) acc[r - k] += Lq[r] * xq;
+                }
+                for (int r = k; r < m; ++r) Mc[r] = (float)acc[r - k];
+            }
+        }
+        for (int q = 0; q < m; ++q) relpos[st[q]] = -1;
+    }
+    out.flops = flops;
+    // ---- levels (leaves = 0) and GPU work items
+    int nl = 0;
+    for (int s = 0; s < ns; ++s) {
+        for (int c : schildren[s]) out.level[s] = std::max(out.level[s], out.level[c] + 1);
+        nl = std::max(nl, out.level[s] + 1);
+    }
+    out.nlevels = nl;
+    std::vector<std::vector<int>> bylevel(nl);
+    for (int s = 0; s < ns; ++s) bylevel[out.level[s]].push_back(s);
+    constexpr int kRowBlock = 128, kColBlock = 256, kBwdCols = 16;
+    out.levels.resize(nl);
+    for (int L = 0; L < nl; ++L) {
+        SolveLevel lv;
+        lv.fwd_begin = (int)(out.fwd_items.size() / 4);
+        lv.bwd_begin = (int)(out.bwd_items.size() / 4);
+        for (int s : bylevel[L]) {
+            const int k = out.sk[s], m = out.sm[s];
+            for (int r0 = 0; r0 < m; r0 += kRowBlock)
+                for (int c0 = 0; c0 < k; c0 += kColBlock) {
+                    const int c1 = std::min(k, c0 + kColBlock);
+                    out.fwd_items.insert(out.fwd_items.end(), {s, r0, std::min(m, r0 + kRowBlock), c0 | (c1 << 16)});
+                }
+            for (int c0 = 0; c0 < k; c0 += kBwdCols)
+                out.bwd_items.insert(out.bwd_items.end(), {s, c0, std::min(k, c0 + kBwdCols), 0});
+        }
+        lv.fwd_end = (int)(out.fwd_items.size() / 4);
+        lv.bwd_end = (int)(out.bwd_items.size() / 4);
+        out.levels[L] = lv;
+    }
+    for (int s = 0; s < ns; ++s)
+        if (out.sk[s] >= 65535) throw Error{PDGB_ERR_UNSUPPORTED, "supernode wider than 65534 columns"};
+}
+
+void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3) {
+    const int n = f.n;
+    std::vector<double> r(b3, b3 + 3 * (size_t)n), y(3 * (size_t)n, 0.0);
+    for (int L = 0; L < f.nlevels; ++L)
+        for (int it = f.levels[L].fwd_begin; it < f.levels[L].fwd_end; ++it) {
+            const int* w = &f.fwd_items[4 * (size_t)it];
+            const int s = w[0], r0 = w[1], r1 = w[2], c0 = w[3] & 0xffff, c1 = w[3] >> 16;
+            const int k = f.sk[s], m = f.sm[s];
+            const float* M = &f.mval[f.moff[s]];
+            const int* rows = &f.rows[f.roff[s]];
+            for (int row = r0; row < r1; ++row) {
+                double acc[3] = {0, 0, 0};
+                for (int c = c0; c < c1; ++c)
+                    for (int d = 0; d < 3; ++d) acc[d] += (double)M[(size_t)c * m + row] * r[3 * (size_t)rows[c] + d];
+                const size_t o = 3 * (size_t)rows[row];
+                for (int d = 0; d < 3; ++d) {
+                    if (row < k) y[o + d] += acc[d];
+                    else r[o + d] -= acc[d];
+                }
+            }
+        }
+    for (int L = f.nlevels - 1; L >= 0; --L)
+        for (int it = f.levels[L].bwd_begin; it < f.levels[L].bwd_end; ++it) {
+            const int* w = &f.bwd_items[4 * (size_t)it];
+            const int s = w[0], c0 = w[1], c1 = w[2];
+            const int k = f.sk[s], m = f.sm[s];
+            const float* M = &f.mval[f.moff[s]];
+            const int* rows = &f.rows[f.roff[s]];
+            for (int c = c0; c < c1; ++c) {
+                double acc[3] = {0, 0, 0};
+                for (int i = c; i < m; ++i) {
+                    const size_t o = 3 * (size_t)rows[i];
+                    const double mv = M[(size_t)c * m + i];
+                    for (int d = 0; d < 3; ++d) acc[d] += mv * (i < k ? y[o + d] : -x3[o + d]);
+                }
+                for (int d = 0; d < 3; ++d) x3[3 * (size_t)rows[c] + d] = acc[d];
+            }
+        }
+}
+
+}  // namespace pdgb

@@ -1,0 +1,85 @@
+// Sparse Cholesky of the scalar PD system K (host side).
+//
+// The reference assembles A = K (x) I_3 (3n x 3n) from per-tet triplets
+// (pdUtil.cu:9-54), orders it with cuSOLVER's host AMD and factors it in
+// FP32 with cuSOLVER's low-level sparse Cholesky (cholesky.cu:72-158).  The
+// engine factors the n x n scalar K once, in FP64 on the host (approximate
+// minimum degree ordering, supernodal multifrontal LL^T), and solves the
+// three coordinates together on the GPU.
+//
+// Solve representation.  For every supernode s with pivot columns C_s
+// (k_s of them) and off-diagonal rows O_s (m_s - k_s), the GPU stores the
+// m_s x k_s matrix
+//     M_s = [ L_ss^-1 ; L_os L_ss^-1 ]       (column major, FP32)
+// so that the forward step of s is y_s = L_ss^-1 r_s plus the update
+// r_O -= (L_os L_ss^-1) r_s, and the backward step is
+// x_s = (L_ss^-1)^T y_s - (L_os L_ss^-1)^T x_O: both are dense
+// matrix-vector products with M_s.  Supernodes on the same level of the
+// supernodal elimination tree are independent.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace pdgb {
+
+struct SparseSym {
+    int n = 0;
+    std::vector<int64_t> p;  // CSR row pointers (full symmetric pattern, diagonal included)
+    std::vector<int> i;
+    std::vector<double> x;
+};
+
+// Approximate minimum degree ordering (Amestoy, Davis & Duff, SIAM J. Matrix
+// Anal. Appl. 17(4), 1996): quotient graph with element absorption,
+// approximate external degrees, mass elimination and supervariable
+// detection.  Returns perm (perm[k] = row eliminated k-th).
+std::vector<int> amd_order(const SparseSym& A);
+
+// Geometric nested dissection (recursive coordinate bisection), an
+// alternative ordering for meshes.  xyz: 3 floats per row.
+std::vector<int> nd_order(const SparseSym& A, const float* xyz);
+
+struct SolveLevel {
+    int fwd_begin, fwd_end;  // work items of the forward pass for this level
+    int bwd_begin, bwd_end;  // work items of the backward pass
+};
+
+struct CholFactor {
+    int n = 0;
+    long long nnz_L = 0;             // nnz of the scalar factor (incl. diagonal)
+    int nsuper = 0;
+    double flops = 0.0;
+    // per supernode
+    std::vector<int> sk, sm;         // pivot count k_s, row count m_s
+    std::vector<int64_t> moff;       // offset of M_s in mval (column major m x k)
+    std::vector<int> roff;           // offset of the row list in rows
+    std::vector<int> rows;           // row lists (vertex ids; first k = pivots)
+    std::vector<float> mval;         // FP32 M_s blocks
+    std::vector<int> level;          // level of each supernode (leaves = 0)
+    int nlevels = 0;
+    // GPU work items: forward (s, row0, row1, col0 | col1 << 16 packed) and
+    // backward (s, col0, col1, 0), grouped by level.
+    std::vector<int> fwd_items;      // 4 ints per item
+    std::vector<int> bwd_items;      // 4 ints per item
+    std::vector<SolveLevel> levels;
+    // FP64 copy of K for refinement residuals (CSR over vertex ids)
+    SparseSym K;
+};
+
+// Factors K (vertex-indexed, n x n SPD).  ordering: 0 = AMD, 1 = nested
+// dissection (xyz required).  Throws Error(PDGB_ERR_NOT_SPD) if a pivot is
+// not positive.
+void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out);
+
+// Applies the factor on the host exactly as the GPU work items do
+// (forward by levels with M_s, backward by levels), in double: x = K^-1 b
+// for 3 interleaved right-hand sides indexed by vertex id.
+void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3);
+
+// Assembles K = diag(mdt2) + sum_t c_t B_t^T B_t for tets given by internal
+// vertex ids (tets4), DmInv (9 doubles per tet, row major) and c_t.
+SparseSym assemble_system(int nv, int nt, const uint32_t* tets4, const double* dminv, const double* coef,
+                          const std::vector<double>& mdt2);
+
+}  // namespace pdgb

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -31,6 +33,7 @@ void set_last_error(int status, const std::string& msg);
 // accumulators fit in shared memory (16 + 12 bytes per vertex).
 constexpr int kMaxPatch = 1024;
 constexpr int kLocalThreads = 256;
+constexpr int kTileTets = 2 * kLocalThreads;
 
 // Device buffer with RAII.
 template <class T> struct DBuf {
@@ -71,8 +74,12 @@ struct HostLayout {
     // tiles
     std::vector<int> tile_tet_ptr;   // [ntiles+1]
     std::vector<int> tile_vptr;      // [ntiles+1]
-    std::vector<int> tile_verts;     // internal vertex ids of each patch (sorted)
-    std::vector<uint2> tet_local;    // [nt_pad] 4 x u16 patch-local corner ids
+    std::vector<uint32_t> tile_verts;  // internal vertex ids of each patch (sorted) | kPinnedBit
+    // per tile incidence lists: for patch vertex k of a tile, the tet corners
+    // (local tet * 4 + corner) it belongs to are inc_ent[4 t0 + inc_end[k-1]
+    // .. 4 t0 + inc_end[k]) (inc_end[-1] = 0), t0 = first tet of the tile.
+    std::vector<uint16_t> inc_ent;   // [4 nt]
+    std::vector<uint16_t> inc_end;   // [sum of patch sizes]
     std::vector<float> geo;          // SoA [10][nt_pad]: DmInv row-major (9), V0*w
     std::vector<uint32_t> tets_int;  // [4*nt] internal vertex ids (Cholesky assembly, checks)
     std::vector<double> dminv_d;     // [9*nt] double DmInv (system assembly)
@@ -95,15 +102,21 @@ void build_vertex_coefficients(const float* mass, const float* dbc, const pdgb_p
 std::vector<float> chebyshev_omegas(int n, float rho);
 
 // --------------------------------------------------------------- kernels
+// Patch entries: vertex id in the low 31 bits; bit 31 marks a pinned vertex,
+// whose RHS is overwritten by the pin term, so the tile adds nothing to it.
+constexpr uint32_t kPinnedBit = 0x80000000u;
+
 struct LocalArgs {
     const float4* sn;
     float4* b;
-    const uint2* tet_local;
+    const uint16_t* inc_ent;
+    const uint16_t* inc_end;
     const float* geo;
     const int* tile_tet_ptr;
     const int* tile_vptr;
-    const int* tile_verts;
+    const uint32_t* tile_verts;
     int nt_pad;
+    const int* done;  // step early-exit flag (Cholesky tol rule), may be null
 };
 
 // Vertex-kernel mode flags.
@@ -132,15 +145,24 @@ struct BeginArgs {
     const float4* x;
     const float4* v;
     const float4* coef;
+    const float4* pin_rhs;
     float4* sn;
     float4* base;
     float4* b;
     float dt;
     float gravity;
+    // Cholesky path with tol > 0: reproduce the reference's
+    // cudaMemset(prev_x, 0, 3 n) (a byte count, pdSolver.cu:162) on the
+    // interleaved caller-order vector; null otherwise.
+    float4* prev;
+    const int* vperm;
+    int* done;          // reset to 0 at step start (may be null)
+    int* iterations;    // reset to the full count (may be null)
+    int num_iterations;
 };
 
 void launch_begin(const BeginArgs& a, cudaStream_t s);
-void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, cudaStream_t s);
+void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, int rotation, cudaStream_t s);
 void launch_jacobi_vertex(const VertexArgs& a, int mode, cudaStream_t s);
 void launch_gather_state(int nv, const int* vperm, const float* X, const float* V, float4* x, float4* v,
                          cudaStream_t s);

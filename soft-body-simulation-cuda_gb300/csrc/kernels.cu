@@ -14,36 +14,40 @@
 namespace pdgb {
 
 // ------------------------------------------------------------ local step
-// One CTA per tile.  The tile's patch of vertex positions is staged in
-// shared memory (one coalesced pass over the sorted patch list), every tet
-// gathers its 4 corners from shared memory, and the 12 RHS contributions are
-// accumulated with shared-memory atomics; one float4 global atomic per patch
-// vertex flushes the tile.  This replaces the reference's 12 global atomics
-// per tet with about one per 3 tets.
-template <bool kJacobiForm>
+// One CTA per tile of Morton-ordered tets.  Shared memory holds one float4
+// slot per tet corner.  (1) Every patch vertex is loaded once (coalesced
+// over the sorted patch list) and written into the slots of the corners it
+// belongs to, following the tile's incidence list.  (2) Every tet reads its
+// 4 corner slots, computes F = Ds DmInv, the closest rotation R (minus F in
+// the Jacobi residual form) and the corner contributions c R DmInv^T G, and
+// overwrites its slots with them.  (3) Every patch vertex sums its slots in
+// the fixed incidence order and adds the sum to b with one float4 atomic
+// (pinned vertices are skipped: their RHS is the pin term).  No
+// shared-memory atomics; within a tile the sums are deterministic.
+template <bool kJacobiForm, int kRotation>
 __global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
-    __shared__ float4 sq[kMaxPatch];
-    __shared__ float ax[kMaxPatch], ay[kMaxPatch], az[kMaxPatch];
+    __shared__ float4 slot[4 * kTileTets];
+    if (a.done && *a.done) return;
     const int tile = blockIdx.x;
     const int vb = a.tile_vptr[tile];
     const int np = a.tile_vptr[tile + 1] - vb;
+    const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
+    const uint16_t* inc = a.inc_ent + 4 * (size_t)t0;
+    const uint16_t* iend = a.inc_end + vb;
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
-        sq[k] = __ldg(&a.sn[a.tile_verts[vb + k]]);
-        ax[k] = 0.f;
-        ay[k] = 0.f;
-        az[k] = 0.f;
+        const float4 p = __ldg(&a.sn[a.tile_verts[vb + k] & ~kPinnedBit]);
+        const int e0 = k ? __ldg(&iend[k - 1]) : 0, e1 = __ldg(&iend[k]);
+        for (int e = e0; e < e1; ++e) slot[__ldg(&inc[e])] = p;
     }
     __syncthreads();
-    const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
     const int ntp = a.nt_pad;
-    for (int t = t0 + threadIdx.x; t < t1; t += kLocalThreads) {
-        const uint2 li = __ldg(&a.tet_local[t]);
-        const int i0 = li.x & 0xffff, i1 = li.x >> 16, i2 = li.y & 0xffff, i3 = li.y >> 16;
+    for (int lt = threadIdx.x; lt < t1 - t0; lt += kLocalThreads) {
+        const int t = t0 + lt;
         float D[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) D[k] = __ldg(&a.geo[k * ntp + t]);
         const float c = __ldg(&a.geo[9 * ntp + t]);
-        const float4 p0 = sq[i0], p1 = sq[i1], p2 = sq[i2], p3 = sq[i3];
+        const float4 p0 = slot[4 * lt], p1 = slot[4 * lt + 1], p2 = slot[4 * lt + 2], p3 = slot[4 * lt + 3];
         // Ds columns = edges; F = Ds * DmInv (row-major F[r][c])
         const float e[3][3] = {{p1.x - p0.x, p2.x - p0.x, p3.x - p0.x},
                                {p1.y - p0.y, p2.y - p0.y, p3.y - p0.y},
@@ -53,9 +57,10 @@ __global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
         for (int r = 0; r < 3; ++r)
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc)
-                F[3 * r + cc] = e[r][0] * D[cc] + e[r][1] * D[3 + cc] + e[r][2] * D[6 + cc];
+                F[3 * r + cc] = fmaf(e[r][0], D[cc], fmaf(e[r][1], D[3 + cc], e[r][2] * D[6 + cc]));
         float R[9];
-        closest_rotation(F, R);
+        if (kRotation == PDGB_ROTATION_SVD) closest_rotation(F, R);
+        else closest_rotation_horn(F, R);
         if (kJacobiForm) {
 #pragma unroll
             for (int k = 0; k < 9; ++k) R[k] -= F[k];
@@ -66,25 +71,38 @@ __global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
         for (int r = 0; r < 3; ++r) {
             const float r0 = c * R[3 * r], r1 = c * R[3 * r + 1], r2 = c * R[3 * r + 2];
 #pragma unroll
-            for (int cc = 0; cc < 3; ++cc) M[3 * r + cc] = r0 * D[3 * cc] + r1 * D[3 * cc + 1] + r2 * D[3 * cc + 2];
+            for (int cc = 0; cc < 3; ++cc) M[3 * r + cc] = fmaf(r0, D[3 * cc], fmaf(r1, D[3 * cc + 1], r2 * D[3 * cc + 2]));
         }
-        atomicAdd(&ax[i1], M[0]); atomicAdd(&ay[i1], M[3]); atomicAdd(&az[i1], M[6]);
-        atomicAdd(&ax[i2], M[1]); atomicAdd(&ay[i2], M[4]); atomicAdd(&az[i2], M[7]);
-        atomicAdd(&ax[i3], M[2]); atomicAdd(&ay[i3], M[5]); atomicAdd(&az[i3], M[8]);
-        atomicAdd(&ax[i0], -(M[0] + M[1] + M[2]));
-        atomicAdd(&ay[i0], -(M[3] + M[4] + M[5]));
-        atomicAdd(&az[i0], -(M[6] + M[7] + M[8]));
+        slot[4 * lt + 0] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
+        slot[4 * lt + 1] = make_float4(M[0], M[3], M[6], 0.f);
+        slot[4 * lt + 2] = make_float4(M[1], M[4], M[7], 0.f);
+        slot[4 * lt + 3] = make_float4(M[2], M[5], M[8], 0.f);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
-        atomicAdd(&a.b[a.tile_verts[vb + k]], make_float4(ax[k], ay[k], az[k], 0.f));
+        const uint32_t v = a.tile_verts[vb + k];
+        if (v & kPinnedBit) continue;
+        const int e0 = k ? __ldg(&iend[k - 1]) : 0, e1 = __ldg(&iend[k]);
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        for (int e = e0; e < e1; ++e) {
+            const float4 q = slot[__ldg(&inc[e])];
+            sx += q.x;
+            sy += q.y;
+            sz += q.z;
+        }
+        atomicAdd(&a.b[v], make_float4(sx, sy, sz, 0.f));
     }
 }
 
-void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, cudaStream_t s) {
+void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, int rotation, cudaStream_t s) {
     if (ntiles <= 0) return;
-    if (jacobi_form) k_local<true><<<ntiles, kLocalThreads, 0, s>>>(a);
-    else k_local<false><<<ntiles, kLocalThreads, 0, s>>>(a);
+    if (rotation == PDGB_ROTATION_SVD) {
+        if (jacobi_form) k_local<true, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, 0, s>>>(a);
+        else k_local<false, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, 0, s>>>(a);
+    } else {
+        if (jacobi_form) k_local<true, PDGB_ROTATION_QUAT><<<ntiles, kLocalThreads, 0, s>>>(a);
+        else k_local<false, PDGB_ROTATION_QUAT><<<ntiles, kLocalThreads, 0, s>>>(a);
+    }
 }
 
 // ------------------------------------------------------- vertex kernels
@@ -144,9 +162,14 @@ void launch_jacobi_vertex(const VertexArgs& a, int mode, cudaStream_t s) {
     }
 }
 
-// Step prologue: f = (0, -g m, 0); s = x + h v + f / (M/h^2); base = b = (M/h^2) s.
+// Step prologue: f = (0, -g m, 0); s = x + h v + f / (M/h^2); base = (M/h^2) s;
+// b = base (pinned vertices: the pin RHS).
 __global__ void __launch_bounds__(256) k_begin(BeginArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        if (a.done) *a.done = 0;
+        if (a.iterations) *a.iterations = a.num_iterations;
+    }
     if (i >= a.nv) return;
     const float4 x = a.x[i], v = a.v[i], cf = __ldg(&a.coef[i]);
     const float dt2_m_1 = 1.0f / cf.x;
@@ -159,7 +182,25 @@ __global__ void __launch_bounds__(256) k_begin(BeginArgs a) {
     a.sn[i] = s;
     const float4 bs = make_float4(cf.x * s.x, cf.x * s.y, cf.x * s.z, 0.f);
     a.base[i] = bs;
-    a.b[i] = bs;
+    a.b[i] = cf.z != 0.f ? __ldg(&a.pin_rhs[i]) : bs;
+    if (a.prev) {
+        // bytes [0, 3 nv) of the caller-order float[3 nv] vector are zeroed
+        const long long zero_bytes = 3LL * a.nv;
+        const long long o = a.vperm[i];
+        float4 p = a.prev[i];
+        float* pc = &p.x;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const long long b0 = 4 * (3 * o + d);
+            if (b0 + 4 <= zero_bytes) pc[d] = 0.f;
+            else if (b0 < zero_bytes) {
+                const int nz = (int)(zero_bytes - b0);  // low-order bytes cleared (little endian)
+                const unsigned mask = ~((1u << (8 * nz)) - 1u);
+                pc[d] = __uint_as_float(__float_as_uint(pc[d]) & mask);
+            }
+        }
+        a.prev[i] = p;
+    }
 }
 
 void launch_begin(const BeginArgs& a, cudaStream_t s) {

@@ -143,24 +143,35 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
     }
     // ---- tiles: greedy runs of Morton-ordered tets, cut at kTileTets tets or
     // when the patch would exceed kMaxPatch vertices.
-    constexpr int kTileTets = 2 * kLocalThreads;
     L.tile_tet_ptr.assign(1, 0);
     L.tile_vptr.assign(1, 0);
     L.tile_verts.clear();
-    L.tet_local.assign(L.nt_pad, make_uint2(0, 0));
-    std::vector<int> mark(nv, -1), loc(nv, 0);
+    L.inc_end.clear();
+    L.inc_ent.assign((size_t)4 * nt, 0);
+    std::vector<int> mark(nv, -1), loc(nv, 0), cnt;
     std::vector<int> patch;
     patch.reserve(kMaxPatch);
     int tile = 0, start = 0;
     auto close_tile = [&](int end) {
         std::sort(patch.begin(), patch.end());
-        for (int k = 0; k < (int)patch.size(); ++k) loc[patch[k]] = k;
-        for (int i = start; i < end; ++i) {
-            const uint32_t* id = &L.tets_int[4 * (size_t)i];
-            uint32_t a0 = loc[id[0]], a1 = loc[id[1]], a2 = loc[id[2]], a3 = loc[id[3]];
-            L.tet_local[i] = make_uint2(a0 | (a1 << 16), a2 | (a3 << 16));
+        const int np = (int)patch.size();
+        for (int k = 0; k < np; ++k) loc[patch[k]] = k;
+        // incidence lists in patch order
+        cnt.assign(np + 1, 0);
+        for (int i = start; i < end; ++i)
+            for (int c = 0; c < 4; ++c) cnt[loc[L.tets_int[4 * (size_t)i + c]] + 1]++;
+        for (int k = 0; k < np; ++k) cnt[k + 1] += cnt[k];
+        for (int k = 0; k < np; ++k) L.inc_end.push_back((uint16_t)cnt[k + 1]);
+        for (int i = start; i < end; ++i)
+            for (int c = 0; c < 4; ++c) {
+                const int k = loc[L.tets_int[4 * (size_t)i + c]];
+                L.inc_ent[4 * (size_t)start + cnt[k]++] = (uint16_t)(4 * (i - start) + c);
+            }
+        for (int v : patch) {
+            const int o = L.vperm[v];
+            const bool pinned = dbc && dbc[o] > 0.f;
+            L.tile_verts.push_back((uint32_t)v | (pinned ? kPinnedBit : 0u));
         }
-        L.tile_verts.insert(L.tile_verts.end(), patch.begin(), patch.end());
         L.tile_vptr.push_back((int)L.tile_verts.size());
         L.tile_tet_ptr.push_back(end);
         patch.clear();

@@ -161,4 +161,74 @@ __device__ __forceinline__ void closest_rotation(const float F[9], float R[9]) {
     R[8] = u0z * v0z + u1z * v1z + u2z * v2z;
 }
 
+// Closest proper rotation by Horn's quaternion form: for unit q,
+// tr(R(q)^T F) = q^T N(F) q with N the symmetric 4x4 matrix below, so the
+// rotation maximising tr(R^T F) -- the closest proper rotation, the same R as
+// the reference's U V^T with a signed smallest singular value -- is the
+// eigenvector of N's largest eigenvalue.  It is found as the dominant
+// eigenvector of A = N + c I (c = 0.6 |F|_F > |sigma_3| keeps the top
+// eigenvalue dominant even for inverted F) by repeated squaring: 3 squarings
+// unconditionally, then up to kTail more, each preceded by a unit-trace
+// normalisation and stopping once trace(P^2) = 1 to float precision (P is
+// then rank one).  The column of P with the largest diagonal entry is q.
+__device__ __forceinline__ void sym4_square(float a[10]) {
+    // a = {ww, xx, yy, zz, wx, wy, wz, xy, xz, yz}
+    const float ww = a[0], xx = a[1], yy = a[2], zz = a[3], wx = a[4], wy = a[5], wz = a[6], xy = a[7], xz = a[8],
+                yz = a[9];
+    a[0] = fmaf(ww, ww, fmaf(wx, wx, fmaf(wy, wy, wz * wz)));
+    a[1] = fmaf(wx, wx, fmaf(xx, xx, fmaf(xy, xy, xz * xz)));
+    a[2] = fmaf(wy, wy, fmaf(xy, xy, fmaf(yy, yy, yz * yz)));
+    a[3] = fmaf(wz, wz, fmaf(xz, xz, fmaf(yz, yz, zz * zz)));
+    a[4] = fmaf(ww, wx, fmaf(wx, xx, fmaf(wy, xy, wz * xz)));
+    a[5] = fmaf(ww, wy, fmaf(wx, xy, fmaf(wy, yy, wz * yz)));
+    a[6] = fmaf(ww, wz, fmaf(wx, xz, fmaf(wy, yz, wz * zz)));
+    a[7] = fmaf(wx, wy, fmaf(xx, xy, fmaf(xy, yy, xz * yz)));
+    a[8] = fmaf(wx, wz, fmaf(xx, xz, fmaf(xy, yz, xz * zz)));
+    a[9] = fmaf(wy, wz, fmaf(xy, xz, fmaf(yy, yz, yz * zz)));
+}
+
+template <int kTail = 6>
+__device__ __forceinline__ void closest_rotation_horn(const float F[9], float R[9]) {
+    float f2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f2 = fmaf(F[i], F[i], f2);
+    const float c = 0.6f * sqrtf(f2);
+    const float sc = 1.0f / fmaxf(4.0f * c, 1e-30f);
+    float a[10];
+    a[0] = (F[0] + F[4] + F[8] + c) * sc;
+    a[1] = (F[0] - F[4] - F[8] + c) * sc;
+    a[2] = (-F[0] + F[4] - F[8] + c) * sc;
+    a[3] = (-F[0] - F[4] + F[8] + c) * sc;
+    a[4] = (F[7] - F[5]) * sc;
+    a[5] = (F[2] - F[6]) * sc;
+    a[6] = (F[3] - F[1]) * sc;
+    a[7] = (F[1] + F[3]) * sc;
+    a[8] = (F[2] + F[6]) * sc;
+    a[9] = (F[5] + F[7]) * sc;
+    sym4_square(a);
+    sym4_square(a);
+    sym4_square(a);
+    for (int k = 0; k < kTail; ++k) {
+        const float it = 1.0f / (a[0] + a[1] + a[2] + a[3]);
+#pragma unroll
+        for (int i = 0; i < 10; ++i) a[i] *= it;
+        const float off = a[4] * a[4] + a[5] * a[5] + a[6] * a[6] + a[7] * a[7] + a[8] * a[8] + a[9] * a[9];
+        const float t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3] + 2.0f * off;
+        sym4_square(a);
+        if (t2 >= 1.0f - 4e-7f) break;
+    }
+    // column with the largest diagonal entry
+    float qw = a[0], qx = a[4], qy = a[5], qz = a[6], best = a[0];
+    if (a[1] > best) { best = a[1]; qw = a[4]; qx = a[1]; qy = a[7]; qz = a[8]; }
+    if (a[2] > best) { best = a[2]; qw = a[5]; qx = a[7]; qy = a[2]; qz = a[9]; }
+    if (a[3] > best) { qw = a[6]; qx = a[8]; qy = a[9]; qz = a[3]; }
+    const float n = rsqrtf(fmaxf(qw * qw + qx * qx + qy * qy + qz * qz, 1e-37f));
+    qw *= n; qx *= n; qy *= n; qz *= n;
+    const float xx = qx * qx, yy = qy * qy, zz = qz * qz;
+    const float xy = qx * qy, xz = qx * qz, yz = qy * qz, wx = qw * qx, wy = qw * qy, wz = qw * qz;
+    R[0] = 1.f - 2.f * (yy + zz); R[1] = 2.f * (xy - wz);       R[2] = 2.f * (xz + wy);
+    R[3] = 2.f * (xy + wz);       R[4] = 1.f - 2.f * (xx + zz); R[5] = 2.f * (yz - wx);
+    R[6] = 2.f * (xz - wy);       R[7] = 2.f * (yz + wx);       R[8] = 1.f - 2.f * (xx + yy);
+}
+
 }  // namespace pdgb

@@ -26,6 +26,10 @@ PDGB_MEM_HOST = 0
 PDGB_MEM_DEVICE = 1
 PDGB_SOLVER_JACOBI = 0
 PDGB_SOLVER_CHOLESKY = 1
+PDGB_ROTATION_QUAT = 0
+PDGB_ROTATION_SVD = 1
+PDGB_ORDER_AMD = 0
+PDGB_ORDER_ND = 1
 
 
 class pdgb_params(C.Structure):
@@ -75,6 +79,19 @@ class pdgb_timing(C.Structure):
     ]
 
 
+class pdgb_factor_info(C.Structure):
+    _fields_ = [
+        ("nnz_L", C.c_longlong),
+        ("m_entries", C.c_longlong),
+        ("num_supernodes", C.c_int),
+        ("num_levels", C.c_int),
+        ("fwd_items", C.c_int),
+        ("bwd_items", C.c_int),
+        ("flops", C.c_double),
+        ("factor_ms", C.c_double),
+    ]
+
+
 class pdgb_layout_info(C.Structure):
     _fields_ = [
         ("num_tiles", C.c_int),
@@ -107,6 +124,11 @@ SIGNATURES = {
     "pdgb_status_string": (C.c_char_p, [C.c_int]),
     "pdgb_last_error": (C.c_char_p, []),
     "pdgb_version": (C.c_char_p, []),
+    "pdgb_set_ordering": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_get_factor_info": (C.c_int, [C.c_void_p, C.POINTER(pdgb_factor_info)]),
+    "pdgb_set_rotation": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_host_factor_check": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_params), C.c_int, C.c_void_p,
+                                         C.c_void_p, C.POINTER(pdgb_factor_info)]),
     "pdgb_inspect_layout": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_layout_info), C.c_void_p,
                                       C.c_void_p]),
 }

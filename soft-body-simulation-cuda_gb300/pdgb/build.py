@@ -59,7 +59,7 @@ def build_engine(force: bool = False, verbose: bool = False) -> Path:
     nvcc = _nvcc()
     obj_dir = LIB_DIR / "obj"
     obj_dir.mkdir(parents=True, exist_ok=True)
-    common = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+    common = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off,-fopenmp",
                            "-I", str(ROOT / "include")]
 
     def compile_one(src: Path) -> Path:
@@ -73,7 +73,7 @@ def build_engine(force: bool = False, verbose: bool = False) -> Path:
     with _cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    _run([nvcc] + ARCH_FLAGS + ["-shared", "-o", str(tmp)] + [str(o) for o in objs] + ["-lcudart"])
+    _run([nvcc] + ARCH_FLAGS + ["-shared", "-o", str(tmp)] + [str(o) for o in objs] + ["-lcudart", "-lgomp"])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 

@@ -85,6 +85,14 @@ class PdSolver:
         N.check(self._lib.pdgb_set_params(self._h, C.byref(prm)), "pdgb_set_params")
         self.params = params
 
+    def set_ordering(self, ordering: int) -> None:
+        """0 = AMD (default), 1 = geometric nested dissection."""
+        N.check(self._lib.pdgb_set_ordering(self._h, int(ordering)), "pdgb_set_ordering")
+
+    def set_rotation(self, mode: int) -> None:
+        """0 = quaternion (default, converged), 1 = the reference's 4-sweep SVD."""
+        N.check(self._lib.pdgb_set_rotation(self._h, int(mode)), "pdgb_set_rotation")
+
     def reset(self) -> None:
         N.check(self._lib.pdgb_reset(self._h), "pdgb_reset")
 
@@ -109,6 +117,17 @@ class PdSolver:
         N.check(self._lib.pdgb_get_perf(self._h, C.byref(p)), "pdgb_get_perf")
         return {"prepare_ms": p.prepare_ms, "steps": p.steps, "iterations": p.iterations,
                 "factor_nnz": p.factor_nnz, "tiles": p.tiles, "patch_verts": p.patch_verts}
+
+    def solve_levels(self) -> int:
+        """Levels of the supernodal elimination tree (Cholesky path)."""
+        f = N.pdgb_factor_info()
+        N.check(self._lib.pdgb_get_factor_info(self._h, C.byref(f)), "pdgb_get_factor_info")
+        return f.num_levels
+
+    def factor_info(self) -> dict:
+        f = N.pdgb_factor_info()
+        N.check(self._lib.pdgb_get_factor_info(self._h, C.byref(f)), "pdgb_get_factor_info")
+        return {k: getattr(f, k) for k, _ in f._fields_}
 
     def last_step_iterations(self) -> int:
         it = C.c_int()

@@ -1,0 +1,90 @@
+"""GPU parity of the Cholesky PD path: prefactored sparse Cholesky (AMD, FP64
+factor, FP32 level-scheduled supernodal solves) behind the C ABI.
+
+Bar: positions after N steps within 1e-4 relative L2 of the reference's own
+kernels (golden fixtures) and of the FP64 oracle; with tol > 0 the per-step
+iteration counts of the reference's error-based early exit."""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden, rel_l2
+
+import oracle as O
+from pdgb import PdSolver, SolverParams, mesh
+from pdgb import _native as N
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if "chol" in c])
+@pytest.mark.parametrize("rotation", [N.PDGB_ROTATION_QUAT, N.PDGB_ROTATION_SVD])
+def test_engine_matches_reference_fixture(name, rotation):
+    body, params, steps, Xg, Vg, itg = load_golden(name)
+    with PdSolver(body, params) as e:
+        e.set_rotation(rotation)
+        its = []
+        for _ in range(steps):
+            e.update(1)
+            its.append(e.last_step_iterations())
+        X, V = e.download_state()
+    assert np.isfinite(X).all() and np.isfinite(V).all()
+    assert rel_l2(X, Xg) < TOL
+    assert rel_l2(X - body.X, Xg - body.X) < 2e-3
+    if params.tol > 0:
+        # the early exit depends on float rounding near the threshold: allow
+        # a one-iteration difference on a few steps
+        d = np.abs(np.asarray(its) - itg)
+        assert d.max() <= 1 and (d > 0).sum() <= max(1, steps // 10), (its, list(itg))
+    else:
+        assert all(i == params.num_iterations for i in its)
+    Xo, _, _ = O.simulate(body, params, steps, precision=64)
+    assert rel_l2(X, Xo) < TOL
+
+
+@pytest.mark.parametrize("ordering", [N.PDGB_ORDER_AMD, N.PDGB_ORDER_ND])
+def test_heterogeneous_grid_vs_fp64_oracle(ordering):
+    """Per-tet Young's modulus log-uniform 1e4..1e7 (the precision workload's
+    material law) on a 14^3 grid."""
+    body = mesh.cube_c3(n=14, seed=5)
+    params = SolverParams(num_iterations=10, solver=1)
+    with PdSolver(body, params) as e:
+        e.set_ordering(ordering)
+        e.update(20)
+        X, V = e.download_state()
+        perf = e.get_performance_data()
+    assert perf["factor_nnz"] > body.num_verts
+    Xo, Vo, _ = O.simulate(body, params, 20, precision=64)
+    assert rel_l2(X, Xo) < TOL
+    assert rel_l2(X - body.X, Xo - body.X) < 2e-3
+
+
+def test_switch_solver_at_runtime():
+    """SetGlobalSolver between steps (simulationContext.cpp:104-114)."""
+    body = mesh.make_grid_body(6, 5, 4, jitter=0.1, seed=6)
+    pj = SolverParams(num_iterations=20, rho=0.9995, solver=0)
+    with PdSolver(body, pj) as e:
+        e.update(3)
+        e.set_global_solver(1)
+        e.update(3)
+        e.set_global_solver(0)
+        e.update(3)
+        X, _ = e.download_state()
+    Xa, Va, _ = O.simulate(body, pj, 3, 64)
+    pc = SolverParams(num_iterations=20, rho=0.9995, solver=1)
+    Xb, Vb, _ = O.simulate(body, pc, 3, 64, X=Xa, V=Va)
+    Xc, _, _ = O.simulate(body, pj, 3, 64, X=Xb, V=Vb)
+    assert rel_l2(X, Xc) < TOL
+
+
+def test_cholesky_and_jacobi_agree_when_converged():
+    """With many iterations both global solvers approach the same PD fixed point."""
+    body = mesh.make_grid_body(5, 5, 5, young=1e5, jitter=0.1, seed=7)
+    with PdSolver(body, SolverParams(num_iterations=40, solver=1)) as e:
+        e.update(5)
+        Xc, _ = e.download_state()
+    with PdSolver(body, SolverParams(num_iterations=200, rho=0.9995, solver=0)) as e:
+        e.update(5)
+        Xj, _ = e.download_state()
+    assert rel_l2(Xc - body.X, Xj - body.X) < 5e-2
