@@ -214,6 +214,41 @@ int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info);
 int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params, int ordering, const double* b,
                            double* x, pdgb_factor_info* info);
 
+/* ---------------------------------------------------------------------
+ * Allocation-free PD steps.  No counterpart in the reference: it exists for
+ * callers that must not allocate device memory when they advance a body -- a
+ * host application whose own allocator owns the GPU's memory, a frame loop
+ * where cudaMalloc/cudaFree would stall the device, or a plugin that is only
+ * handed device pointers to the simulation arrays.
+ *
+ * pdgb_step_noalloc runs nsteps Jacobi + Chebyshev PD steps (the same
+ * iteration as pdgb_step with PDGB_SOLVER_JACOBI) on caller-owned device
+ * arrays, updating X and V (device, float[3 nv], in place).  It calls no
+ * cudaMalloc, cudaFree or allocating library routine: its scratch is one
+ * fixed device array of about 8 MB inside this library, held by every GPU
+ * that loads it until the process exits.
+ *   - Limits: num_verts <= 32768 and num_tets <= 131072, else
+ *     PDGB_ERR_UNSUPPORTED.  A tet with an out-of-range index or zero rest
+ *     volume gives PDGB_ERR_BAD_MESH.
+ *   - All calls share that scratch array: calls that overlap on the GPU
+ *     (other streams, other host threads) race; serialise them.  Each call
+ *     recomputes or clears everything it reads from the scratch.
+ *   - The first call on a device looks up the scratch's device address for
+ *     that device; make it before any stream capture.
+ *   - The call waits for its stream before returning (it reports mesh
+ *     errors found on the device). */
+typedef struct pdgb_noalloc_mesh {
+    int num_verts;
+    int num_tets;
+    const uint32_t* tets; /* device [4 nt]                                 */
+    const float* X0;      /* device [3 nv] rest shape and pin targets      */
+    const float* mass;    /* device [nv]                                   */
+    const float* mu;      /* device [nt] PD weight                         */
+    const float* dbc;     /* device [nv] pin flags, or NULL                */
+} pdgb_noalloc_mesh;
+int pdgb_step_noalloc(const pdgb_noalloc_mesh* mesh, const pdgb_params* params, float* X, float* V, int nsteps,
+                      void* stream);
+
 /* Library version string. */
 const char* pdgb_version(void);
 

@@ -79,6 +79,18 @@ class pdgb_timing(C.Structure):
     ]
 
 
+class pdgb_noalloc_mesh(C.Structure):
+    _fields_ = [
+        ("num_verts", C.c_int),
+        ("num_tets", C.c_int),
+        ("tets", C.c_void_p),
+        ("X0", C.c_void_p),
+        ("mass", C.c_void_p),
+        ("mu", C.c_void_p),
+        ("dbc", C.c_void_p),
+    ]
+
+
 class pdgb_factor_info(C.Structure):
     _fields_ = [
         ("nnz_L", C.c_longlong),
@@ -129,6 +141,8 @@ SIGNATURES = {
     "pdgb_set_rotation": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_host_factor_check": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_params), C.c_int, C.c_void_p,
                                          C.c_void_p, C.POINTER(pdgb_factor_info)]),
+    "pdgb_step_noalloc": (C.c_int, [C.POINTER(pdgb_noalloc_mesh), C.POINTER(pdgb_params), C.c_void_p, C.c_void_p,
+                                    C.c_int, C.c_void_p]),
     "pdgb_inspect_layout": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_layout_info), C.c_void_p,
                                       C.c_void_p]),
 }
