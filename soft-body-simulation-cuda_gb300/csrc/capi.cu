@@ -54,9 +54,10 @@ struct pdgb_engine {
     CholFactor chol;
     int chol_ordering = -1;
     float chol_dt = 0.f, chol_pw = -1.f;
-    DBuf<int> ch_fwd, ch_bwd, ch_sk, ch_sm, ch_roff, ch_rows;
-    DBuf<int64_t> ch_moff;
+    DBuf<int> ch_fwd, ch_bwd, ch_rows;
+    DBuf<int4> ch_levels;
     DBuf<float> ch_mval;
+    bool cta_solve = false;  // whole solve in one CTA (small systems)
     double factor_ms = 0.0;
     // step graph
     cudaGraph_t graph = nullptr;
@@ -81,6 +82,9 @@ struct pdgb_engine {
 };
 
 namespace {
+
+// Factors up to this many stored entries use the single-CTA solve.
+constexpr size_t kCtaSolveMaxEntries = 1u << 20;
 
 template <class F> int guarded(F&& f) {
     try {
@@ -194,8 +198,8 @@ void record_chol_step(pdgb_engine* e) {
     ba.prev = use_tol ? e->prev.p : nullptr;
     launch_begin(ba, s);
     const LocalArgs la = local_args(e, &st->done);
-    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_sk.p, e->ch_sm.p, e->ch_moff.p, e->ch_roff.p, e->ch_rows.p,
-                e->ch_mval.p, e->b.p, e->y.p, e->sn.p, &st->done};
+    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_rows.p, e->ch_mval.p, e->ch_levels.p, e->chol.nlevels,
+                e->b.p, e->y.p, e->sn.p, &st->done};
     CholVertexArgs cv{};
     cv.nv = e->nv;
     cv.tol = e->prm.tol;
@@ -212,7 +216,8 @@ void record_chol_step(pdgb_engine* e) {
     cv.dt_inv = 1.0f / e->prm.dt;
     for (int i = 0; i < n; ++i) {
         record_local(e, la, false, i);
-        launch_chol_solve(ca, e->chol.levels, s);
+        if (e->cta_solve) launch_chol_solve_cta(ca, s);
+        else launch_chol_solve_levels(ca, e->chol.levels, s);
         cv.iteration = i;
         launch_chol_vertex(cv, s);
     }
@@ -297,12 +302,16 @@ void prepare_cholesky(pdgb_engine* e) {
     const CholFactor& f = e->chol;
     e->ch_fwd.upload(f.fwd_items, s);
     e->ch_bwd.upload(f.bwd_items, s);
-    e->ch_sk.upload(f.sk, s);
-    e->ch_sm.upload(f.sm, s);
-    e->ch_roff.upload(f.roff, s);
     e->ch_rows.upload(f.rows, s);
-    e->ch_moff.upload(f.moff, s);
     e->ch_mval.upload(f.mval, s);
+    std::vector<int4> lv(f.levels.size());
+    for (size_t i = 0; i < lv.size(); ++i)
+        lv[i] = make_int4(f.levels[i].fwd_begin, f.levels[i].fwd_end, f.levels[i].bwd_begin, f.levels[i].bwd_end);
+    e->ch_levels.upload(lv, s);
+    // A single CTA walks the whole tree when the factor is small: the solve
+    // is then bound by the tree depth, not by bandwidth, and launches would
+    // dominate.
+    e->cta_solve = f.mval.size() <= kCtaSolveMaxEntries;
     e->chol_ordering = e->ordering;
     e->chol_dt = e->prm.dt;
     e->chol_pw = e->prm.positional_weight;
@@ -650,8 +659,8 @@ int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info) {
     info->m_entries = (long long)f.mval.size();
     info->num_supernodes = f.nsuper;
     info->num_levels = f.nlevels;
-    info->fwd_items = (int)(f.fwd_items.size() / 4);
-    info->bwd_items = (int)(f.bwd_items.size() / 4);
+    info->fwd_items = (int)(f.fwd_items.size() / kItemInts);
+    info->bwd_items = (int)(f.bwd_items.size() / kItemInts);
     info->flops = f.flops;
     info->factor_ms = e->factor_ms;
     return PDGB_OK;
@@ -684,8 +693,8 @@ int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params
             info->m_entries = (long long)f.mval.size();
             info->num_supernodes = f.nsuper;
             info->num_levels = f.nlevels;
-            info->fwd_items = (int)(f.fwd_items.size() / 4);
-            info->bwd_items = (int)(f.bwd_items.size() / 4);
+            info->fwd_items = (int)(f.fwd_items.size() / kItemInts);
+            info->bwd_items = (int)(f.bwd_items.size() / kItemInts);
             info->flops = f.flops;
             info->factor_ms = ms;
         }

@@ -452,6 +452,49 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         const bool cont = j > 0 && parent[j - 1] == j && colcount[j - 1] == colcount[j] + 1 && nchild[j] == 1;
         if (!cont) sfirst.push_back(j);
     }
+    // ---- relaxed amalgamation: merge a supernode into its parent when its
+    // columns immediately precede the parent's (it is the parent's last child
+    // in postorder) and the explicit zeros stay small.  The merged block has
+    // the parent's off-diagonal rows, so k = k_s + k_p and m = k_s + m_p.
+    // This removes the 1-3 column supernodes that break chains at the top of
+    // AMD trees (each one a level of the solve) and most leaf singletons.
+    {
+        const int nf = (int)sfirst.size();
+        sfirst.push_back(n);
+        std::vector<long long> bk(nf), bm(nf), btrue(nf);
+        for (int s = 0; s < nf; ++s) {
+            bk[s] = sfirst[s + 1] - sfirst[s];
+            bm[s] = colcount[sfirst[s]];
+            long long t = 0;
+            for (int j = sfirst[s]; j < sfirst[s + 1]; ++j) t += colcount[j];
+            btrue[s] = t;
+        }
+        std::vector<int> col2f(n);
+        for (int s = 0; s < nf; ++s)
+            for (int j = sfirst[s]; j < sfirst[s + 1]; ++j) col2f[j] = s;
+        // merged[s] = true if block s was merged into the following block
+        std::vector<char> merged(nf, 0);
+        auto stored = [](long long k, long long m) { return k * m - k * (k - 1) / 2; };
+        for (int s = 0; s + 1 < nf; ++s) {
+            const int last = sfirst[s + 1] - 1;
+            if (parent[last] != sfirst[s + 1]) continue;  // parent block must start right after
+            const int p = s + 1;
+            const long long k = bk[s] + bk[p], m = bk[s] + bm[p];
+            const long long tr = btrue[s] + btrue[p];
+            const long long zeros = stored(k, m) - tr;
+            const long long added = zeros - (stored(bk[s], bm[s]) - btrue[s]) - (stored(bk[p], bm[p]) - btrue[p]);
+            if (added <= 256 || zeros * 8 <= stored(k, m)) {
+                merged[s] = 1;
+                bk[p] = k;
+                bm[p] = m;
+                btrue[p] = tr;
+            }
+        }
+        std::vector<int> sf;
+        for (int s = 0; s < nf; ++s)
+            if (s == 0 || !merged[s - 1]) sf.push_back(sfirst[s]);
+        sfirst.swap(sf);
+    }
     const int ns = (int)sfirst.size();
     sfirst.push_back(n);
     std::vector<int> col2s(n);
@@ -492,7 +535,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
                     st.push_back(i);
                 }
         std::sort(st.begin() + (l - f), st.end());
-        if ((int)st.size() != colcount[f])
+        if ((int)st.size() != (l - f) + colcount[l - 1] - 1)
             throw Error{PDGB_ERR_INVALID_ARGUMENT, "internal error: supernode structure mismatch"};
     }
     // ---- numeric multifrontal factorisation (FP64) + M_s blocks
@@ -585,6 +628,11 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         for (int q = 0; q < m; ++q) relpos[st[q]] = -1;
     }
     out.flops = flops;
+    {
+        long long st_tot = 0;
+        for (int s = 0; s < ns; ++s) st_tot += (long long)out.sk[s] * out.sm[s] - (long long)out.sk[s] * (out.sk[s] - 1) / 2;
+        out.zeros = st_tot - nnz;
+    }
     // ---- levels (leaves = 0) and GPU work items
     int nl = 0;
     for (int s = 0; s < ns; ++s) {
@@ -594,24 +642,26 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
     out.nlevels = nl;
     std::vector<std::vector<int>> bylevel(nl);
     for (int s = 0; s < ns; ++s) bylevel[out.level[s]].push_back(s);
-    constexpr int kRowBlock = 128, kColBlock = 256, kBwdCols = 16;
     out.levels.resize(nl);
     for (int L = 0; L < nl; ++L) {
         SolveLevel lv;
-        lv.fwd_begin = (int)(out.fwd_items.size() / 4);
-        lv.bwd_begin = (int)(out.bwd_items.size() / 4);
+        lv.fwd_begin = (int)(out.fwd_items.size() / kItemInts);
+        lv.bwd_begin = (int)(out.bwd_items.size() / kItemInts);
         for (int s : bylevel[L]) {
             const int k = out.sk[s], m = out.sm[s];
-            for (int r0 = 0; r0 < m; r0 += kRowBlock)
-                for (int c0 = 0; c0 < k; c0 += kColBlock) {
-                    const int c1 = std::min(k, c0 + kColBlock);
-                    out.fwd_items.insert(out.fwd_items.end(), {s, r0, std::min(m, r0 + kRowBlock), c0 | (c1 << 16)});
-                }
-            for (int c0 = 0; c0 < k; c0 += kBwdCols)
-                out.bwd_items.insert(out.bwd_items.end(), {s, c0, std::min(k, c0 + kBwdCols), 0});
+            const int64_t mo = out.moff[s];
+            const int lo = (int)(mo & 0xffffffff), hi = (int)(mo >> 32);
+            for (int r0 = 0; r0 < m; r0 += kFwdItemRows) {
+                // pivot rows only need columns <= row (lower-triangular block)
+                const int cmax = std::min(k, r0 + kFwdItemRows);
+                for (int c0 = 0; c0 < cmax; c0 += kFwdItemCols)
+                    out.fwd_items.insert(out.fwd_items.end(),
+                                         {lo, hi, out.roff[s], m, k, r0, c0, std::min(cmax, c0 + kFwdItemCols)});
+            }
+            for (int c = 0; c < k; ++c) out.bwd_items.insert(out.bwd_items.end(), {lo, hi, out.roff[s], m, k, c, 0, 0});
         }
-        lv.fwd_end = (int)(out.fwd_items.size() / 4);
-        lv.bwd_end = (int)(out.bwd_items.size() / 4);
+        lv.fwd_end = (int)(out.fwd_items.size() / kItemInts);
+        lv.bwd_end = (int)(out.bwd_items.size() / kItemInts);
         out.levels[L] = lv;
     }
     for (int s = 0; s < ns; ++s)
@@ -621,16 +671,17 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
 void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3) {
     const int n = f.n;
     std::vector<double> r(b3, b3 + 3 * (size_t)n), y(3 * (size_t)n, 0.0);
+    auto moff_of = [](const int* w) { return (int64_t)(uint32_t)w[0] | ((int64_t)w[1] << 32); };
     for (int L = 0; L < f.nlevels; ++L)
         for (int it = f.levels[L].fwd_begin; it < f.levels[L].fwd_end; ++it) {
-            const int* w = &f.fwd_items[4 * (size_t)it];
-            const int s = w[0], r0 = w[1], r1 = w[2], c0 = w[3] & 0xffff, c1 = w[3] >> 16;
-            const int k = f.sk[s], m = f.sm[s];
-            const float* M = &f.mval[f.moff[s]];
-            const int* rows = &f.rows[f.roff[s]];
-            for (int row = r0; row < r1; ++row) {
+            const int* w = &f.fwd_items[kItemInts * (size_t)it];
+            const int roff = w[2], m = w[3], k = w[4], r0 = w[5], c0 = w[6], c1 = w[7];
+            const float* M = &f.mval[moff_of(w)];
+            const int* rows = &f.rows[roff];
+            for (int row = r0; row < std::min(m, r0 + kFwdItemRows); ++row) {
                 double acc[3] = {0, 0, 0};
-                for (int c = c0; c < c1; ++c)
+                const int cend = row < k ? std::min(c1, row + 1) : c1;
+                for (int c = c0; c < cend; ++c)
                     for (int d = 0; d < 3; ++d) acc[d] += (double)M[(size_t)c * m + row] * r[3 * (size_t)rows[c] + d];
                 const size_t o = 3 * (size_t)rows[row];
                 for (int d = 0; d < 3; ++d) {
@@ -641,20 +692,17 @@ void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3) {
         }
     for (int L = f.nlevels - 1; L >= 0; --L)
         for (int it = f.levels[L].bwd_begin; it < f.levels[L].bwd_end; ++it) {
-            const int* w = &f.bwd_items[4 * (size_t)it];
-            const int s = w[0], c0 = w[1], c1 = w[2];
-            const int k = f.sk[s], m = f.sm[s];
-            const float* M = &f.mval[f.moff[s]];
-            const int* rows = &f.rows[f.roff[s]];
-            for (int c = c0; c < c1; ++c) {
-                double acc[3] = {0, 0, 0};
-                for (int i = c; i < m; ++i) {
-                    const size_t o = 3 * (size_t)rows[i];
-                    const double mv = M[(size_t)c * m + i];
-                    for (int d = 0; d < 3; ++d) acc[d] += mv * (i < k ? y[o + d] : -x3[o + d]);
-                }
-                for (int d = 0; d < 3; ++d) x3[3 * (size_t)rows[c] + d] = acc[d];
+            const int* w = &f.bwd_items[kItemInts * (size_t)it];
+            const int roff = w[2], m = w[3], k = w[4], c = w[5];
+            const float* M = &f.mval[moff_of(w)];
+            const int* rows = &f.rows[roff];
+            double acc[3] = {0, 0, 0};
+            for (int i = c; i < m; ++i) {
+                const size_t o = 3 * (size_t)rows[i];
+                const double mv = M[(size_t)c * m + i];
+                for (int d = 0; d < 3; ++d) acc[d] += mv * (i < k ? y[o + d] : -x3[o + d]);
             }
+            for (int d = 0; d < 3; ++d) x3[3 * (size_t)rows[c] + d] = acc[d];
         }
 }
 

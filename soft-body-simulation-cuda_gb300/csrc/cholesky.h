@@ -45,6 +45,14 @@ struct SolveLevel {
     int bwd_begin, bwd_end;  // work items of the backward pass
 };
 
+// Warp work items, 8 ints each (two int4 loads, no dependent metadata loads):
+//   forward : {moff_lo, moff_hi, roff, m, k, r0, c0, c1}: rows r0 .. min(r0+32, m)
+//             of M_s times the right-hand side of pivot columns c0 .. c1
+//   backward: {moff_lo, moff_hi, roff, m, k, c, 0, 0}: pivot column c
+constexpr int kItemInts = 8;
+constexpr int kFwdItemRows = 32;
+constexpr int kFwdItemCols = 256;
+
 struct CholFactor {
     int n = 0;
     long long nnz_L = 0;             // nnz of the scalar factor (incl. diagonal)
@@ -58,11 +66,11 @@ struct CholFactor {
     std::vector<float> mval;         // FP32 M_s blocks
     std::vector<int> level;          // level of each supernode (leaves = 0)
     int nlevels = 0;
-    // GPU work items: forward (s, row0, row1, col0 | col1 << 16 packed) and
-    // backward (s, col0, col1, 0), grouped by level.
-    std::vector<int> fwd_items;      // 4 ints per item
-    std::vector<int> bwd_items;      // 4 ints per item
+    // GPU warp work items grouped by level (see kItemInts).
+    std::vector<int> fwd_items;
+    std::vector<int> bwd_items;
     std::vector<SolveLevel> levels;
+    long long zeros = 0;             // explicit zeros stored by amalgamated supernodes
     // FP64 copy of K for refinement residuals (CSR over vertex ids)
     SparseSym K;
 };

@@ -12,107 +12,130 @@
 
 namespace pdgb {
 
-// Forward item (s, r0, r1, c0 | c1 << 16): rows r0..r1 of M_s times the
-// right-hand side of the pivot columns c0..c1.  Pivot rows accumulate into y,
-// off-diagonal rows subtract from r (ancestor columns, solved at a later level).
-__global__ void __launch_bounds__(kFwdThreads) k_chol_forward(CholArgs a, int item0) {
-    __shared__ float4 rs[kFwdCols];
-    if (a.done && *a.done) return;
-    const int4 it = __ldg(reinterpret_cast<const int4*>(a.fwd_items) + item0 + blockIdx.x);
-    const int s = it.x, r0 = it.y, r1 = it.z, c0 = it.w & 0xffff, c1 = it.w >> 16;
-    const int k = __ldg(&a.sk[s]), m = __ldg(&a.sm[s]);
-    const int* rows = a.rows + __ldg(&a.roff[s]);
-    const float* M = a.mval + __ldg(&a.moff[s]);
-    for (int c = c0 + threadIdx.x; c < c1; c += kFwdThreads) rs[c - c0] = a.r[__ldg(&rows[c])];
-    __syncthreads();
-    const int row = r0 + threadIdx.x;
-    if (row >= r1) return;
-    // inverse of the lower-triangular pivot block is lower triangular
-    const int cend = row < k ? min(c1, row + 1) : c1;
+// Forward warp item {moff, roff, m, k, r0, c0, c1}: lane = row r0 + lane of
+// M_s; sum over pivot columns c0..c1 of M_s[row, c] r[pivot c]; pivot rows
+// add the sum to y, off-diagonal rows subtract it from r (ancestor columns,
+// solved at a later level).  The chunk's pivot right-hand sides are staged
+// in warp-private shared memory (32 at a time).
+__device__ __forceinline__ void fwd_warp_item(const CholArgs& a, const int* w, float4* stage, int lane) {
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
+    const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
+    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+    const int roff = h0.z, m = h0.w, k = h1.x, r0 = h1.y, c0 = h1.z, c1 = h1.w;
+    const int* rows = a.rows + roff;
+    const float* M = a.mval + moff;
+    const int row = r0 + lane;
+    const bool valid = row < m;
+    const int cend = !valid ? c0 : (row < k ? min(c1, row + 1) : c1);
     float ax = 0.f, ay = 0.f, az = 0.f;
-    const float* Mr = M + row;
+    for (int cb = c0; cb < c1; cb += 32) {
+        const int nc = min(32, c1 - cb);
+        __syncwarp();
+        if (lane < nc) stage[lane] = a.r[__ldg(&rows[cb + lane])];
+        __syncwarp();
+        const int ce = min(cend, cb + nc);
+        const float* Mr = M + row;
 #pragma unroll 4
-    for (int c = c0; c < cend; ++c) {
-        const float mv = __ldg(Mr + (size_t)c * m);
-        const float4 v = rs[c - c0];
-        ax = fmaf(mv, v.x, ax);
-        ay = fmaf(mv, v.y, ay);
-        az = fmaf(mv, v.z, az);
+        for (int c = cb; c < ce; ++c) {
+            const float mv = __ldg(Mr + (size_t)c * m);
+            const float4 v = stage[c - cb];
+            ax = fmaf(mv, v.x, ax);
+            ay = fmaf(mv, v.y, ay);
+            az = fmaf(mv, v.z, az);
+        }
     }
+    if (!valid) return;
     const int vid = __ldg(&rows[row]);
     if (row < k) atomicAdd(&a.y[vid], make_float4(ax, ay, az, 0.f));
     else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
 }
 
-// Backward item (s, c0, c1): x[pivot c] = sum_i M_s[i, c] z_i with
-// z = [y_pivots ; -x_offdiag], one warp per column, z staged in shared
-// memory in chunks of kBwdChunk rows.
-__global__ void __launch_bounds__(kBwdThreads) k_chol_backward(CholArgs a, int item0) {
-    __shared__ float4 zs[kBwdChunk];
-    if (a.done && *a.done) return;
-    const int4 it = __ldg(reinterpret_cast<const int4*>(a.bwd_items) + item0 + blockIdx.x);
-    const int s = it.x, c0 = it.y, c1 = it.z;
-    const int k = __ldg(&a.sk[s]), m = __ldg(&a.sm[s]);
-    const int* rows = a.rows + __ldg(&a.roff[s]);
-    const float* M = a.mval + __ldg(&a.moff[s]);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int kWarps = kBwdThreads / 32;
-    constexpr int kPer = (kBwdColsPerItem + kWarps - 1) / kWarps;
-    float acc[kPer][3];
-#pragma unroll
-    for (int q = 0; q < kPer; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.f;
-    // rows below c0 are zero in every column of this item (lower triangle)
-    for (int base = c0; base < m; base += kBwdChunk) {
-        const int nrow = min(kBwdChunk, m - base);
-        __syncthreads();
-        for (int i = threadIdx.x; i < nrow; i += kBwdThreads) {
-            const int g = base + i;
-            const int vid = __ldg(&rows[g]);
-            if (g < k) zs[i] = a.y[vid];
-            else {
-                const float4 xv = a.x[vid];
-                zs[i] = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
-            }
+// Backward warp item {moff, roff, m, k, c}: x[pivot c] = sum_{i >= c}
+// M_s[i, c] z_i with z = [y_pivots ; -x_offdiag]; lanes stride over rows
+// (coalesced column of M_s), then a warp reduction.  No atomics.
+__device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, int lane) {
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
+    const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
+    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+    const int roff = h0.z, m = h0.w, k = h1.x, c = h1.y;
+    const int* rows = a.rows + roff;
+    const float* Mc = a.mval + moff + (size_t)c * m;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll 2
+    for (int i = c + lane; i < m; i += 32) {
+        const int vid = __ldg(&rows[i]);
+        const float mv = __ldg(Mc + i);
+        float4 z;
+        if (i < k) z = a.y[vid];
+        else {
+            const float4 xv = a.x[vid];
+            z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
         }
-        __syncthreads();
-#pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            const int c = c0 + warp + q * kWarps;
-            if (c >= c1) continue;
-            const float* Mc = M + (size_t)c * m;
-            const int i0 = max(c, base);
-            for (int g = i0 + lane; g < base + nrow; g += 32) {
-                const float mv = __ldg(Mc + g);
-                const float4 z = zs[g - base];
-                acc[q][0] = fmaf(mv, z.x, acc[q][0]);
-                acc[q][1] = fmaf(mv, z.y, acc[q][1]);
-                acc[q][2] = fmaf(mv, z.z, acc[q][2]);
-            }
-        }
+        ax = fmaf(mv, z.x, ax);
+        ay = fmaf(mv, z.y, ay);
+        az = fmaf(mv, z.z, az);
     }
 #pragma unroll
-    for (int q = 0; q < kPer; ++q) {
-        const int c = c0 + warp + q * kWarps;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            acc[q][0] += __shfl_xor_sync(0xffffffffu, acc[q][0], off);
-            acc[q][1] += __shfl_xor_sync(0xffffffffu, acc[q][1], off);
-            acc[q][2] += __shfl_xor_sync(0xffffffffu, acc[q][2], off);
-        }
-        if (lane == 0 && c < c1) a.x[__ldg(&rows[c])] = make_float4(acc[q][0], acc[q][1], acc[q][2], 0.f);
+    for (int off = 16; off > 0; off >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, off);
+        ay += __shfl_xor_sync(0xffffffffu, ay, off);
+        az += __shfl_xor_sync(0xffffffffu, az, off);
     }
+    if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
 }
 
-void launch_chol_solve(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
+// ---- one launch per level: each warp takes one item.
+__global__ void __launch_bounds__(kLevelThreads) k_chol_fwd_level(CholArgs a, int item0, int nitems) {
+    __shared__ float4 stage[kLevelThreads / 32][32];
+    if (a.done && *a.done) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int it = blockIdx.x * (kLevelThreads / 32) + warp;
+    if (it >= nitems) return;
+    fwd_warp_item(a, a.fwd_items + (size_t)kItemInts * (item0 + it), stage[warp], lane);
+}
+
+__global__ void __launch_bounds__(kLevelThreads) k_chol_bwd_level(CholArgs a, int item0, int nitems) {
+    if (a.done && *a.done) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int it = blockIdx.x * (kLevelThreads / 32) + warp;
+    if (it >= nitems) return;
+    bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * (item0 + it), lane);
+}
+
+void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
+    constexpr int kWarps = kLevelThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
         const int n = levels[L].fwd_end - levels[L].fwd_begin;
-        if (n > 0) k_chol_forward<<<n, kFwdThreads, 0, s>>>(a, levels[L].fwd_begin);
+        if (n > 0) k_chol_fwd_level<<<(n + kWarps - 1) / kWarps, kLevelThreads, 0, s>>>(a, levels[L].fwd_begin, n);
     }
     for (size_t L = levels.size(); L-- > 0;) {
         const int n = levels[L].bwd_end - levels[L].bwd_begin;
-        if (n > 0) k_chol_backward<<<n, kBwdThreads, 0, s>>>(a, levels[L].bwd_begin);
+        if (n > 0) k_chol_bwd_level<<<(n + kWarps - 1) / kWarps, kLevelThreads, 0, s>>>(a, levels[L].bwd_begin, n);
     }
 }
+
+// ---- the whole solve in one CTA: warps stride over the items of a level,
+// __syncthreads between levels (global writes of the block become visible
+// to the whole block at the barrier).
+__global__ void __launch_bounds__(kCtaSolveThreads) k_chol_solve_cta(CholArgs a) {
+    __shared__ float4 stage[kCtaSolveThreads / 32][32];
+    if (a.done && *a.done) return;
+    constexpr int kWarps = kCtaSolveThreads / 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int L = 0; L < a.nlevels; ++L) {
+        const int4 lv = __ldg(&a.levels[L]);
+        for (int it = lv.x + warp; it < lv.y; it += kWarps)
+            fwd_warp_item(a, a.fwd_items + (size_t)kItemInts * it, stage[warp], lane);
+        __syncthreads();
+    }
+    for (int L = a.nlevels - 1; L >= 0; --L) {
+        const int4 lv = __ldg(&a.levels[L]);
+        for (int it = lv.z + warp; it < lv.w; it += kWarps) bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * it, lane);
+        __syncthreads();
+    }
+}
+
+void launch_chol_solve_cta(const CholArgs& a, cudaStream_t s) { k_chol_solve_cta<<<1, kCtaSolveThreads, 0, s>>>(a); }
 
 // Cholesky-path vertex kernel after each solve (new positions in sn, written
 // by the backward pass): resets b for the next local step (pinned vertices

@@ -10,21 +10,16 @@
 
 namespace pdgb {
 
-constexpr int kFwdThreads = 128;       // rows per forward item (one row per thread)
-constexpr int kFwdCols = 256;          // pivot columns per forward item
-constexpr int kBwdThreads = 128;       // 4 warps; one warp per column
-constexpr int kBwdColsPerItem = 16;    // pivot columns per backward item
-constexpr int kBwdChunk = 2048;        // rows of z staged per pass (32 KB)
+constexpr int kLevelThreads = 128;     // per-level launches: 4 warps, one warp item each
+constexpr int kCtaSolveThreads = 1024; // whole-solve-in-one-CTA kernel: 32 warps
 
 struct CholArgs {
-    const int* fwd_items;  // int4 per item
-    const int* bwd_items;  // int4 per item
-    const int* sk;
-    const int* sm;
-    const int64_t* moff;
-    const int* roff;
+    const int* fwd_items;  // kItemInts per item
+    const int* bwd_items;  // kItemInts per item
     const int* rows;
     const float* mval;
+    const int4* levels;    // {fwd_begin, fwd_end, bwd_begin, bwd_end} per level (CTA solve)
+    int nlevels;
     float4* r;  // right-hand side in, destroyed (forward updates)
     float4* y;  // forward result (must be zero on entry)
     float4* x;  // solution out
@@ -56,7 +51,10 @@ struct CholVertexArgs {
     float dt_inv;
 };
 
-void launch_chol_solve(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s);
+// One launch per level and direction (large systems).
+void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s);
+// The whole solve in one CTA, levels separated by __syncthreads (small systems).
+void launch_chol_solve_cta(const CholArgs& a, cudaStream_t s);
 void launch_chol_vertex(const CholVertexArgs& a, cudaStream_t s);
 void launch_chol_finish(const CholVertexArgs& a, cudaStream_t s);
 
