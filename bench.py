@@ -48,6 +48,14 @@ WORKLOADS = {
                 "prefactored sparse Cholesky (AMD), 10 iterations/step",
         "grid": 10, "iterations": 10, "solver": "cholesky",
     },
+    "c4": {
+        "workload": "pd_cholesky_batch512",
+        "desc": "512 independent hex-grid bodies, dims uniform 4..24 per axis (seed 4), cells 1/16 m, E log-uniform "
+                "1e4..1e7, nu U[0.3,0.45], rho U[800,1200], top faces pinned, dt=1/120, per-body prefactored sparse "
+                "Cholesky (AMD), 10 iterations/step, one engine: 1 local launch + 1 solve launch (one CTA per body) "
+                "+ 1 vertex launch per iteration, CUDA graph per step",
+        "nbodies": 512, "iterations": 10, "solver": "cholesky",
+    },
     "c3": {
         "workload": "pd_cholesky_hetero40",
         "desc": "40^3 hex grid x5 tets (68921 v / 320000 t), per-tet E log-uniform 1e4..1e7 (seed 3), nu U[0.3,0.45], "
@@ -193,7 +201,7 @@ def cpu_baseline(body, params, steps: int):
                       f"{body.num_tets} tets), float arithmetic, OpenMP over {cores} host threads"}
 
 
-def run_reference_arm(args, body, params):
+def run_reference_arm(args, body, params, scale=1.0):
     rank, world, _ = dist_info()
     if rank != 0:
         return
@@ -249,6 +257,7 @@ def main():
     ap.add_argument("--impl", default="pdgb", choices=["pdgb", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--grid", type=int, default=0, help="override cells per axis (profiling of smaller cases)")
+    ap.add_argument("--bodies", type=int, default=0, help="override the number of bodies of the batch workload")
     ap.add_argument("--cpu-steps", type=int, default=4, help="PD steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -264,8 +273,15 @@ def main():
     if args.grid:
         WORKLOAD["grid"] = args.grid
         WORKLOAD["workload"] += f"_grid{args.grid}"
-    n = WORKLOAD["grid"]
-    if args.workload == "c2":
+    n = WORKLOAD.get("grid", 0)
+    bodies = None
+    if args.workload == "c4":
+        bodies = mesh.batch_c4(nbodies=args.bodies or WORKLOAD["nbodies"])
+        WORKLOAD["nbodies"] = len(bodies)
+        body = mesh.concat(bodies)
+        WORKLOAD["tets"], WORKLOAD["verts"] = body.num_tets, body.num_verts
+        params = SolverParams(num_iterations=WORKLOAD["iterations"], solver=1)
+    elif args.workload == "c2":
         body = mesh.cube_c2(n=n)
         params = SolverParams(num_iterations=WORKLOAD["iterations"], rho=WORKLOAD["rho"], solver=0)
     elif args.workload == "c1":
@@ -275,8 +291,9 @@ def main():
         body = mesh.cube_c3(n=n)
         params = SolverParams(num_iterations=WORKLOAD["iterations"], solver=1)
 
+    cpu_body = body if bodies is None else mesh.concat(bodies[:16])  # bounded CPU sample of the batch
     if args.impl == "reference":
-        run_reference_arm(args, body, params)
+        run_reference_arm(args, cpu_body, params, scale=1.0)
         return
 
     rank, world, local = dist_info()
@@ -286,7 +303,7 @@ def main():
     dist = init_dist(world)
     from pdgb import PdSolver
 
-    eng = PdSolver(body, params)
+    eng = PdSolver(body if bodies is None else bodies, params)
     stream = torch.cuda.ExternalStream(eng._lib.pdgb_stream(eng.handle))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
@@ -360,7 +377,9 @@ def main():
     traffic = ncu_traffic_per_launch(WORKLOAD["workload"])
     cpu = None
     if not args.no_cpu_baseline:
-        cpu = cpu_baseline(body, params, args.cpu_steps)
+        cpu = cpu_baseline(cpu_body, params, args.cpu_steps)
+        if bodies is not None:
+            cpu["sample"] += f"; the first 16 of the {len(bodies)} bodies"
     clk = clocks.summary()
     line = {
         "metric": METRIC,

@@ -104,6 +104,20 @@ typedef struct pdgb_perf {
  * stream the engine creates. */
 int pdgb_create(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* stream, pdgb_engine** out);
 
+/* Batch of independent soft bodies advanced together (SURVEY "batching";
+ * the reference's own multi-body mode concatenates bodies into one system,
+ * dataLoader.cu:291-378).  Vertices of body b are caller ids
+ * sum_{i<b} nv_i .. + nv_b in pdgb_upload_state / pdgb_download_state.  Per
+ * step: one local-step launch over the tiles of all bodies and, on the
+ * Cholesky path, one solve launch with one CTA per body (each body has its own
+ * factor, largest first).  The early-exit tolerance applies to single-body
+ * engines only; batches run num_iterations iterations. */
+int pdgb_create_batch(int nbodies, const pdgb_mesh_desc* bodies, const pdgb_params* params, void* stream,
+                      pdgb_engine** out);
+int pdgb_num_bodies(pdgb_engine* e);
+/* State of one body of a batch (caller layout, nv_b x 3 floats each). */
+int pdgb_download_body(pdgb_engine* e, int body, float* X, float* V, int memory);
+
 /* Replaces PdSolver::SolverPrepare (pdSolver.cu:40-139): per-tet DmInv/V0,
  * system assembly, ordering and factorisation, step graph.  pdgb_step calls
  * it on first use, as PdSolver::Update does (pdSolver.cu:212-216). */

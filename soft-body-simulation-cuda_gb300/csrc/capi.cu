@@ -34,6 +34,8 @@ struct pdgb_engine {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int nv = 0, nt = 0;
+    int nbodies = 1;
+    std::vector<int> body_vstart, body_tstart;  // caller order, [nbodies + 1]
     // caller data (host copies, caller order)
     std::vector<float> X0, mass, mu, dbc;
     std::vector<uint32_t> tets;
@@ -54,7 +56,7 @@ struct pdgb_engine {
     CholFactor chol;
     int chol_ordering = -1;
     float chol_dt = 0.f, chol_pw = -1.f;
-    DBuf<int> ch_fwd, ch_bwd, ch_rows;
+    DBuf<int> ch_fwd, ch_bwd, ch_rows, ch_body_level, ch_body_order;
     DBuf<int4> ch_levels;
     DBuf<float> ch_mval;
     bool cta_solve = false;  // whole solve in one CTA (small systems)
@@ -190,7 +192,7 @@ void record_jacobi_step(pdgb_engine* e) {
 void record_chol_step(pdgb_engine* e) {
     cudaStream_t s = e->stream;
     const int n = e->prm.num_iterations;
-    const bool use_tol = e->prm.tol > 0.f;
+    const bool use_tol = e->prm.tol > 0.f && e->nbodies == 1;  // batches: fixed iteration count
     StepState* st = e->st.p;
     BeginArgs ba = begin_args(e);
     ba.done = &st->done;
@@ -198,11 +200,11 @@ void record_chol_step(pdgb_engine* e) {
     ba.prev = use_tol ? e->prev.p : nullptr;
     launch_begin(ba, s);
     const LocalArgs la = local_args(e, &st->done);
-    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_rows.p, e->ch_mval.p, e->ch_levels.p, e->chol.nlevels,
-                e->b.p, e->y.p, e->sn.p, &st->done};
+    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_rows.p, e->ch_mval.p, e->ch_levels.p, e->ch_body_level.p,
+                e->ch_body_order.p, e->b.p, e->y.p, e->sn.p, &st->done};
     CholVertexArgs cv{};
     cv.nv = e->nv;
-    cv.tol = e->prm.tol;
+    cv.tol = use_tol ? e->prm.tol : 0.f;
     cv.st = st;
     cv.prev = e->prev.p;
     cv.sn = e->sn.p;
@@ -216,7 +218,7 @@ void record_chol_step(pdgb_engine* e) {
     cv.dt_inv = 1.0f / e->prm.dt;
     for (int i = 0; i < n; ++i) {
         record_local(e, la, false, i);
-        if (e->cta_solve) launch_chol_solve_cta(ca, s);
+        if (e->cta_solve) launch_chol_solve_cta(ca, e->nbodies, s);
         else launch_chol_solve_levels(ca, e->chol.levels, s);
         cv.iteration = i;
         launch_chol_vertex(cv, s);
@@ -289,14 +291,22 @@ void prepare_cholesky(pdgb_engine* e) {
         e->chol.n == e->nv)
         return;  // the system matrix depends only on the mesh, dt and the pin weight
     auto t0 = std::chrono::steady_clock::now();
-    SparseSym K = engine_system(e->L);
+    SparseSym K;
+    if (e->nbodies == 1) K = engine_system(e->L);
     std::vector<float> xyz(3 * (size_t)e->nv);
     for (int i = 0; i < e->nv; ++i) {
         xyz[3 * i] = e->L.x0[i].x;
         xyz[3 * i + 1] = e->L.x0[i].y;
         xyz[3 * i + 2] = e->L.x0[i].z;
     }
-    cholesky_factor(K, e->ordering, xyz.data(), e->chol);
+    if (e->nbodies > 1) {
+        std::vector<double> mdt2(e->nv);
+        for (int i = 0; i < e->nv; ++i) mdt2[i] = (double)e->L.coef[i].x;
+        cholesky_factor_bodies(e->nbodies, e->L.body_ivstart, e->L.body_itstart, e->L.tets_int.data(),
+                               e->L.dminv_d.data(), e->L.coef_d.data(), mdt2, e->ordering, xyz.data(), e->chol);
+    } else {
+        cholesky_factor(K, e->ordering, xyz.data(), e->chol);
+    }
     e->factor_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     cudaStream_t s = e->stream;
     const CholFactor& f = e->chol;
@@ -308,10 +318,12 @@ void prepare_cholesky(pdgb_engine* e) {
     for (size_t i = 0; i < lv.size(); ++i)
         lv[i] = make_int4(f.levels[i].fwd_begin, f.levels[i].fwd_end, f.levels[i].bwd_begin, f.levels[i].bwd_end);
     e->ch_levels.upload(lv, s);
-    // A single CTA walks the whole tree when the factor is small: the solve
-    // is then bound by the tree depth, not by bandwidth, and launches would
-    // dominate.
-    e->cta_solve = f.mval.size() <= kCtaSolveMaxEntries;
+    e->ch_body_level.upload(f.body_level, s);
+    e->ch_body_order.upload(f.body_order, s);
+    // A single CTA walks a body's whole tree when the factor is small (the
+    // solve is then bound by the tree depth, not by bandwidth, and launches
+    // would dominate); batches of bodies always run one CTA per body.
+    e->cta_solve = e->nbodies > 1 || f.mval.size() <= kCtaSolveMaxEntries;
     e->chol_ordering = e->ordering;
     e->chol_dt = e->prm.dt;
     e->chol_pw = e->prm.positional_weight;
@@ -346,7 +358,12 @@ void pdgb_default_params(pdgb_params* p) {
     p->refine_steps = 0;
 }
 
-int pdgb_create(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* stream, pdgb_engine** out) {
+}  // extern "C"
+
+namespace {
+
+int create_impl(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* stream, pdgb_engine** out,
+                const std::vector<int>* body_vstart) {
     if (!out) {
         set_last_error(PDGB_ERR_INVALID_ARGUMENT, "out is null");
         return PDGB_ERR_INVALID_ARGUMENT;
@@ -379,8 +396,15 @@ int pdgb_create(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* str
         copy_in(e->mu, mesh->mu, (size_t)e->nt, mesh->memory);
         e->has_dbc = mesh->dbc != nullptr;
         if (e->has_dbc) copy_in(e->dbc, mesh->dbc, (size_t)e->nv, mesh->memory);
+        if (body_vstart) {
+            e->nbodies = (int)body_vstart->size() - 1;
+            e->body_vstart = *body_vstart;
+        } else {
+            e->body_vstart = {0, e->nv};
+        }
         build_layout(e->nv, e->nt, e->X0.data(), e->tets.data(), e->mass.data(), e->mu.data(),
-                     e->has_dbc ? e->dbc.data() : nullptr, e->prm, e->L);
+                     e->has_dbc ? e->dbc.data() : nullptr, e->prm, e->L, e->nbodies,
+                     e->nbodies > 1 ? e->body_vstart.data() : nullptr);
         upload_mesh(e);
         // initial state X (and V) from the descriptor
         std::vector<float> Vh;
@@ -401,6 +425,93 @@ int pdgb_create(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* str
     }
     *out = e;
     return PDGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pdgb_create(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* stream, pdgb_engine** out) {
+    return create_impl(mesh, params, stream, out, nullptr);
+}
+
+int pdgb_create_batch(int nbodies, const pdgb_mesh_desc* bodies, const pdgb_params* params, void* stream,
+                      pdgb_engine** out) {
+    if (!out || !bodies || !params || nbodies < 1) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad batch arguments");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    // concatenate the bodies (host copies), vertex ids offset per body
+    std::vector<float> X, V, mass, mu, dbc;
+    std::vector<uint32_t> tets;
+    std::vector<int> vstart(1, 0);
+    bool anyV = false;
+    int st = guarded([&] {
+        long long nv_tot = 0, nt_tot = 0;
+        for (int b = 0; b < nbodies; ++b) {
+            const pdgb_mesh_desc& d = bodies[b];
+            if (!d.X || !d.tets || !d.mass || !d.mu || d.num_verts <= 0 || d.num_tets <= 0 ||
+                (d.memory != PDGB_MEM_HOST && d.memory != PDGB_MEM_DEVICE))
+                throw Error{PDGB_ERR_INVALID_ARGUMENT, "body " + std::to_string(b) + ": bad descriptor"};
+            nv_tot += d.num_verts;
+            nt_tot += d.num_tets;
+            anyV = anyV || d.V;
+        }
+        if (nv_tot > (1 << 28) || nt_tot > (1 << 28)) throw Error{PDGB_ERR_INVALID_ARGUMENT, "batch too large"};
+        X.reserve(3 * nv_tot);
+        for (int b = 0; b < nbodies; ++b) {
+            const pdgb_mesh_desc& d = bodies[b];
+            std::vector<float> tmp;
+            std::vector<uint32_t> tt;
+            copy_in(tmp, d.X, 3 * (size_t)d.num_verts, d.memory);
+            X.insert(X.end(), tmp.begin(), tmp.end());
+            if (anyV) {
+                if (d.V) copy_in(tmp, d.V, 3 * (size_t)d.num_verts, d.memory);
+                else tmp.assign(3 * (size_t)d.num_verts, 0.f);
+                V.insert(V.end(), tmp.begin(), tmp.end());
+            }
+            copy_in(tmp, d.mass, (size_t)d.num_verts, d.memory);
+            mass.insert(mass.end(), tmp.begin(), tmp.end());
+            copy_in(tmp, d.mu, (size_t)d.num_tets, d.memory);
+            mu.insert(mu.end(), tmp.begin(), tmp.end());
+            if (d.dbc) copy_in(tmp, d.dbc, (size_t)d.num_verts, d.memory);
+            else tmp.assign((size_t)d.num_verts, 0.f);
+            dbc.insert(dbc.end(), tmp.begin(), tmp.end());
+            copy_in(tt, d.tets, 4 * (size_t)d.num_tets, d.memory);
+            for (uint32_t& t : tt) {
+                if (t >= (uint32_t)d.num_verts)
+                    throw Error{PDGB_ERR_BAD_MESH, "body " + std::to_string(b) + ": tet index out of range"};
+                t += (uint32_t)vstart.back();
+            }
+            tets.insert(tets.end(), tt.begin(), tt.end());
+            vstart.push_back(vstart.back() + d.num_verts);
+        }
+    });
+    if (st != PDGB_OK) return st;
+    pdgb_mesh_desc all{vstart.back(), (int)(tets.size() / 4), X.data(), anyV ? V.data() : nullptr, tets.data(),
+                       mass.data(), mu.data(), dbc.data(), PDGB_MEM_HOST};
+    return create_impl(&all, params, stream, out, &vstart);
+}
+
+int pdgb_num_bodies(pdgb_engine* e) { return e ? e->nbodies : 0; }
+
+int pdgb_download_body(pdgb_engine* e, int body, float* X, float* V, int memory) {
+    if (!e || body < 0 || body >= e->nbodies || (!X && !V)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine, body or outputs");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        const size_t n3 = 3 * (size_t)e->nv;
+        const size_t o = 3 * (size_t)e->body_vstart[body];
+        const size_t c = 3 * (size_t)(e->body_vstart[body + 1] - e->body_vstart[body]);
+        launch_scatter_state(e->nv, e->vperm.p, e->x.p, e->v.p, e->staging.p, e->staging.p + n3, e->stream);
+        const cudaMemcpyKind kind = memory == PDGB_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        if (X) PDGB_CUDA_TRY(cudaMemcpyAsync(X, e->staging.p + o, c * sizeof(float), kind, e->stream));
+        if (V) PDGB_CUDA_TRY(cudaMemcpyAsync(V, e->staging.p + n3 + o, c * sizeof(float), kind, e->stream));
+        if (memory == PDGB_MEM_HOST) PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        PDGB_CUDA_TRY(cudaGetLastError());
+    });
 }
 
 int pdgb_prepare(pdgb_engine* e) {

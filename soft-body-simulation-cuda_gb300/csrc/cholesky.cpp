@@ -664,15 +664,102 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         lv.bwd_end = (int)(out.bwd_items.size() / kItemInts);
         out.levels[L] = lv;
     }
-    for (int s = 0; s < ns; ++s)
-        if (out.sk[s] >= 65535) throw Error{PDGB_ERR_UNSUPPORTED, "supernode wider than 65534 columns"};
+    out.body_level = {0, nl};
+    out.body_order = {0};
+}
+
+void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const std::vector<int>& tstart,
+                            const uint32_t* tets4, const double* dminv, const double* coef,
+                            const std::vector<double>& mdt2, int ordering, const float* xyz, CholFactor& out) {
+    std::vector<CholFactor> fs(nbodies);
+    std::vector<int> order(nbodies);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        return tstart[a + 1] - tstart[a] > tstart[b + 1] - tstart[b];
+    });
+    std::vector<int> failed(nbodies, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int q = 0; q < nbodies; ++q) {
+        const int b = order[q];
+        const int v0 = vstart[b], nvb = vstart[b + 1] - v0, t0 = tstart[b], ntb = tstart[b + 1] - t0;
+        try {
+            std::vector<uint32_t> lt(4 * (size_t)ntb);
+            for (size_t i = 0; i < lt.size(); ++i) lt[i] = tets4[4 * (size_t)t0 + i] - (uint32_t)v0;
+            std::vector<double> md(mdt2.begin() + v0, mdt2.begin() + v0 + nvb);
+            SparseSym Kb = assemble_system(nvb, ntb, lt.data(), dminv + 9 * (size_t)t0, coef + t0, md);
+            cholesky_factor(Kb, ordering, xyz ? xyz + 3 * (size_t)v0 : nullptr, fs[b]);
+        } catch (const Error& e) {
+            failed[b] = e.status;
+        } catch (...) {
+            failed[b] = PDGB_ERR_OUT_OF_MEMORY;
+        }
+    }
+    for (int b = 0; b < nbodies; ++b)
+        if (failed[b])
+            throw Error{failed[b], "factorisation of body " + std::to_string(b) + " failed (" +
+                                       (failed[b] == PDGB_ERR_NOT_SPD ? "not positive definite" : "error") + ")"};
+    out = CholFactor();
+    out.n = vstart[nbodies];
+    int64_t mbase = 0, rbase = 0;
+    int sbase = 0;
+    out.body_level.assign(1, 0);
+    for (int b = 0; b < nbodies; ++b) {
+        CholFactor& f = fs[b];
+        const int v0 = vstart[b];
+        out.nnz_L += f.nnz_L;
+        out.zeros += f.zeros;
+        out.flops += f.flops;
+        out.nlevels = std::max(out.nlevels, f.nlevels);
+        for (int s = 0; s < f.nsuper; ++s) {
+            out.sk.push_back(f.sk[s]);
+            out.sm.push_back(f.sm[s]);
+            out.moff.push_back(f.moff[s] + mbase);
+            out.roff.push_back(f.roff[s] + (int)rbase);
+            out.level.push_back(f.level[s]);
+        }
+        out.nsuper += f.nsuper;
+        out.mval.insert(out.mval.end(), f.mval.begin(), f.mval.end());
+        for (int r : f.rows) out.rows.push_back(r + v0);
+        auto shift = [&](std::vector<int>& dst, const std::vector<int>& src) {
+            const int base_item = (int)(dst.size() / kItemInts);
+            for (size_t i = 0; i < src.size(); i += kItemInts) {
+                const int64_t mo = ((int64_t)(uint32_t)src[i] | ((int64_t)src[i + 1] << 32)) + mbase;
+                dst.push_back((int)(mo & 0xffffffff));
+                dst.push_back((int)(mo >> 32));
+                dst.push_back(src[i + 2] + (int)rbase);
+                for (int j = 3; j < kItemInts; ++j) dst.push_back(src[i + j]);
+            }
+            return base_item;
+        };
+        const int fb = shift(out.fwd_items, f.fwd_items);
+        const int bb = shift(out.bwd_items, f.bwd_items);
+        for (const SolveLevel& lv : f.levels)
+            out.levels.push_back({lv.fwd_begin + fb, lv.fwd_end + fb, lv.bwd_begin + bb, lv.bwd_end + bb});
+        out.body_level.push_back((int)out.levels.size());
+        mbase += (int64_t)f.mval.size();
+        rbase += (int64_t)f.rows.size();
+        sbase += f.nsuper;
+        out.K.n = 0;  // per-body systems are not kept
+        f = CholFactor();  // release the per-body copy
+    }
+    (void)sbase;
+    std::vector<std::pair<int64_t, int>> sz(nbodies);
+    for (int b = 0; b < nbodies; ++b) {
+        int64_t e = 0;
+        for (int L = out.body_level[b]; L < out.body_level[b + 1]; ++L)
+            e += (int64_t)(out.levels[L].fwd_end - out.levels[L].fwd_begin) + (out.levels[L].bwd_end - out.levels[L].bwd_begin);
+        sz[b] = {-e, b};
+    }
+    std::sort(sz.begin(), sz.end());
+    out.body_order.resize(nbodies);
+    for (int b = 0; b < nbodies; ++b) out.body_order[b] = sz[b].second;
 }
 
 void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3) {
     const int n = f.n;
     std::vector<double> r(b3, b3 + 3 * (size_t)n), y(3 * (size_t)n, 0.0);
     auto moff_of = [](const int* w) { return (int64_t)(uint32_t)w[0] | ((int64_t)w[1] << 32); };
-    for (int L = 0; L < f.nlevels; ++L)
+    for (int L = 0; L < (int)f.levels.size(); ++L)
         for (int it = f.levels[L].fwd_begin; it < f.levels[L].fwd_end; ++it) {
             const int* w = &f.fwd_items[kItemInts * (size_t)it];
             const int roff = w[2], m = w[3], k = w[4], r0 = w[5], c0 = w[6], c1 = w[7];
@@ -690,7 +777,9 @@ void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3) {
                 }
             }
         }
-    for (int L = f.nlevels - 1; L >= 0; --L)
+    // bodies are independent: walk each body's levels top-down
+    for (size_t b = 0; b + 1 < f.body_level.size(); ++b)
+    for (int L = f.body_level[b + 1] - 1; L >= f.body_level[b]; --L)
         for (int it = f.levels[L].bwd_begin; it < f.levels[L].bwd_end; ++it) {
             const int* w = &f.bwd_items[kItemInts * (size_t)it];
             const int roff = w[2], m = w[3], k = w[4], c = w[5];

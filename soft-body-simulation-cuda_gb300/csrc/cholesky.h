@@ -69,7 +69,9 @@ struct CholFactor {
     // GPU warp work items grouped by level (see kItemInts).
     std::vector<int> fwd_items;
     std::vector<int> bwd_items;
-    std::vector<SolveLevel> levels;
+    std::vector<SolveLevel> levels;  // body-major: body b owns levels[body_level[b] .. body_level[b+1])
+    std::vector<int> body_level;     // [nbodies + 1]
+    std::vector<int> body_order;     // bodies by decreasing stored factor size (batch solve order)
     long long zeros = 0;             // explicit zeros stored by amalgamated supernodes
     // FP64 copy of K for refinement residuals (CSR over vertex ids)
     SparseSym K;
@@ -79,6 +81,15 @@ struct CholFactor {
 // dissection (xyz required).  Throws Error(PDGB_ERR_NOT_SPD) if a pivot is
 // not positive.
 void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out);
+
+// Factors the block-diagonal system of independent bodies, one block per
+// body (vertex range vstart[b]..vstart[b+1], tets tstart[b]..tstart[b+1] in
+// the engine's order), in parallel over bodies, and concatenates the
+// factors: rows keep engine vertex ids, work items and levels are grouped
+// per body.
+void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const std::vector<int>& tstart,
+                            const uint32_t* tets4, const double* dminv, const double* coef,
+                            const std::vector<double>& mdt2, int ordering, const float* xyz, CholFactor& out);
 
 // Applies the factor on the host exactly as the GPU work items do
 // (forward by levels with M_s, backward by levels), in double: x = K^-1 b

@@ -71,6 +71,9 @@ struct HostLayout {
     std::vector<int> vperm;   // internal vertex -> caller vertex
     std::vector<int> viperm;  // caller vertex -> internal vertex
     std::vector<int> tperm;   // internal tet -> caller tet
+    int nbodies = 1;
+    std::vector<int> body_ivstart;  // [nbodies+1] internal vertex range of each body
+    std::vector<int> body_itstart;  // [nbodies+1] internal tet range of each body
     // tiles
     std::vector<int> tile_tet_ptr;   // [ntiles+1]
     std::vector<int> tile_vptr;      // [ntiles+1]
@@ -91,8 +94,13 @@ struct HostLayout {
 };
 
 // Builds the layout from caller arrays (host memory).  Throws Error.
+// body_vstart (nullable, nbodies + 1 entries): vertex ranges of independent
+// bodies; vertices and tets are then ordered body-major (Morton within a
+// body), so tiles never mix bodies and each body's internal vertices are
+// contiguous.
 void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const float* mass, const float* mu,
-                  const float* dbc, const pdgb_params& prm, HostLayout& L);
+                  const float* dbc, const pdgb_params& prm, HostLayout& L, int nbodies = 1,
+                  const int* body_vstart = nullptr);
 
 // Recomputes the per-vertex coefficients that depend on dt / pin weight.
 void build_vertex_coefficients(const float* mass, const float* dbc, const pdgb_params& prm, HostLayout& L);

@@ -8,6 +8,7 @@
 // shared memory, and each tet stores 16-bit patch-local corner ids.
 #include <algorithm>
 #include <cmath>
+#include <tuple>
 #include <cstring>
 #include <numeric>
 
@@ -68,7 +69,7 @@ std::vector<float> chebyshev_omegas(int n, float rho) {
 }
 
 void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const float* mass, const float* mu,
-                  const float* dbc, const pdgb_params& prm, HostLayout& L) {
+                  const float* dbc, const pdgb_params& prm, HostLayout& L, int nbodies, const int* body_vstart) {
     if (nv <= 0 || nt <= 0) throw Error{PDGB_ERR_INVALID_ARGUMENT, "num_verts and num_tets must be positive"};
     for (size_t i = 0; i < (size_t)4 * nt; ++i)
         if (tets[i] >= (uint32_t)nv)
@@ -79,30 +80,54 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
     L.nv = nv;
     L.nt = nt;
     Quantizer qz(nv, X0);
-    // ---- vertex order
+    // body of every caller vertex (all 0 for a single body)
+    if (nbodies < 1) throw Error{PDGB_ERR_INVALID_ARGUMENT, "nbodies must be >= 1"};
+    std::vector<int> vbody(nv, 0);
+    if (body_vstart) {
+        if (body_vstart[0] != 0 || body_vstart[nbodies] != nv)
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "body vertex ranges must cover all vertices"};
+        for (int b = 0; b < nbodies; ++b) {
+            if (body_vstart[b + 1] <= body_vstart[b]) throw Error{PDGB_ERR_INVALID_ARGUMENT, "empty body"};
+            for (int v = body_vstart[b]; v < body_vstart[b + 1]; ++v) vbody[v] = b;
+        }
+    }
+    L.nbodies = nbodies;
+    // ---- vertex order (body, Morton)
     {
-        std::vector<std::pair<uint64_t, int>> key(nv);
-        for (int v = 0; v < nv; ++v) key[v] = {qz.key(X0[3 * v], X0[3 * v + 1], X0[3 * v + 2]), v};
+        std::vector<std::tuple<int, uint64_t, int>> key(nv);
+        for (int v = 0; v < nv; ++v) key[v] = {vbody[v], qz.key(X0[3 * v], X0[3 * v + 1], X0[3 * v + 2]), v};
         std::sort(key.begin(), key.end());
         L.vperm.resize(nv);
         L.viperm.resize(nv);
         for (int i = 0; i < nv; ++i) {
-            L.vperm[i] = key[i].second;
-            L.viperm[key[i].second] = i;
+            L.vperm[i] = std::get<2>(key[i]);
+            L.viperm[std::get<2>(key[i])] = i;
         }
+        L.body_ivstart.assign(nbodies + 1, 0);
+        for (int v = 0; v < nv; ++v) L.body_ivstart[vbody[v] + 1]++;
+        for (int b = 0; b < nbodies; ++b) L.body_ivstart[b + 1] += L.body_ivstart[b];
     }
-    // ---- tet order (centroid Morton)
+    // ---- tet order (body, centroid Morton); a tet must not span bodies
     {
-        std::vector<std::pair<uint64_t, int>> key(nt);
+        std::vector<std::tuple<int, uint64_t, int>> key(nt);
         for (int t = 0; t < nt; ++t) {
             double c[3] = {0, 0, 0};
-            for (int k = 0; k < 4; ++k)
-                for (int d = 0; d < 3; ++d) c[d] += 0.25 * X0[3 * (size_t)tets[4 * (size_t)t + k] + d];
-            key[t] = {qz.key(c[0], c[1], c[2]), t};
+            const int b = vbody[tets[4 * (size_t)t]];
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t v = tets[4 * (size_t)t + k];
+                if (vbody[v] != b) throw Error{PDGB_ERR_BAD_MESH, "tet " + std::to_string(t) + " spans two bodies"};
+                for (int d = 0; d < 3; ++d) c[d] += 0.25 * X0[3 * (size_t)v + d];
+            }
+            key[t] = {b, qz.key(c[0], c[1], c[2]), t};
         }
         std::sort(key.begin(), key.end());
         L.tperm.resize(nt);
-        for (int i = 0; i < nt; ++i) L.tperm[i] = key[i].second;
+        L.body_itstart.assign(nbodies + 1, 0);
+        for (int i = 0; i < nt; ++i) {
+            L.tperm[i] = std::get<2>(key[i]);
+            L.body_itstart[std::get<0>(key[i]) + 1]++;
+        }
+        for (int b = 0; b < nbodies; ++b) L.body_itstart[b + 1] += L.body_itstart[b];
     }
     L.tets_int.resize((size_t)4 * nt);
     for (int i = 0; i < nt; ++i)
@@ -152,6 +177,7 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
     std::vector<int> patch;
     patch.reserve(kMaxPatch);
     int tile = 0, start = 0;
+    int body_cursor = 0, next_body_start = nbodies > 1 ? L.body_itstart[1] : nt;
     auto close_tile = [&](int end) {
         std::sort(patch.begin(), patch.end());
         const int np = (int)patch.size();
@@ -186,7 +212,9 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
             for (int j = 0; j < k; ++j) dup = dup || id[j] == id[k];
             fresh += !dup;
         }
-        if (i - start == kTileTets || (int)patch.size() + fresh > kMaxPatch) close_tile(i);
+        const bool new_body = i > start && i == next_body_start;
+        if (i - start == kTileTets || (int)patch.size() + fresh > kMaxPatch || new_body) close_tile(i);
+        while (i >= next_body_start && body_cursor < nbodies) next_body_start = L.body_itstart[++body_cursor];
         for (int k = 0; k < 4; ++k)
             if (mark[id[k]] != tile) {
                 mark[id[k]] = tile;

@@ -114,28 +114,33 @@ void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& 
     }
 }
 
-// ---- the whole solve in one CTA: warps stride over the items of a level,
+// ---- one body per CTA: warps stride over the items of a level,
 // __syncthreads between levels (global writes of the block become visible
-// to the whole block at the barrier).
+// to the whole block at the barrier).  Bodies are independent, so CTAs
+// never wait on each other.
 __global__ void __launch_bounds__(kCtaSolveThreads) k_chol_solve_cta(CholArgs a) {
     __shared__ float4 stage[kCtaSolveThreads / 32][32];
     if (a.done && *a.done) return;
     constexpr int kWarps = kCtaSolveThreads / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int L = 0; L < a.nlevels; ++L) {
+    const int body = __ldg(&a.body_order[blockIdx.x]);
+    const int L0 = __ldg(&a.body_level[body]), L1 = __ldg(&a.body_level[body + 1]);
+    for (int L = L0; L < L1; ++L) {
         const int4 lv = __ldg(&a.levels[L]);
         for (int it = lv.x + warp; it < lv.y; it += kWarps)
             fwd_warp_item(a, a.fwd_items + (size_t)kItemInts * it, stage[warp], lane);
         __syncthreads();
     }
-    for (int L = a.nlevels - 1; L >= 0; --L) {
+    for (int L = L1 - 1; L >= L0; --L) {
         const int4 lv = __ldg(&a.levels[L]);
         for (int it = lv.z + warp; it < lv.w; it += kWarps) bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * it, lane);
         __syncthreads();
     }
 }
 
-void launch_chol_solve_cta(const CholArgs& a, cudaStream_t s) { k_chol_solve_cta<<<1, kCtaSolveThreads, 0, s>>>(a); }
+void launch_chol_solve_cta(const CholArgs& a, int nbodies, cudaStream_t s) {
+    if (nbodies > 0) k_chol_solve_cta<<<nbodies, kCtaSolveThreads, 0, s>>>(a);
+}
 
 // Cholesky-path vertex kernel after each solve (new positions in sn, written
 // by the backward pass): resets b for the next local step (pinned vertices

@@ -18,8 +18,9 @@ struct CholArgs {
     const int* bwd_items;  // kItemInts per item
     const int* rows;
     const float* mval;
-    const int4* levels;    // {fwd_begin, fwd_end, bwd_begin, bwd_end} per level (CTA solve)
-    int nlevels;
+    const int4* levels;      // {fwd_begin, fwd_end, bwd_begin, bwd_end} per level, body-major
+    const int* body_level;   // [nbodies + 1]: levels of body b (CTA solve)
+    const int* body_order;   // CTA -> body (largest factor first)
     float4* r;  // right-hand side in, destroyed (forward updates)
     float4* y;  // forward result (must be zero on entry)
     float4* x;  // solution out
@@ -53,8 +54,9 @@ struct CholVertexArgs {
 
 // One launch per level and direction (large systems).
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s);
-// The whole solve in one CTA, levels separated by __syncthreads (small systems).
-void launch_chol_solve_cta(const CholArgs& a, cudaStream_t s);
+// The whole solve of one body in one CTA, levels separated by
+// __syncthreads; one CTA per body (small systems and batches of bodies).
+void launch_chol_solve_cta(const CholArgs& a, int nbodies, cudaStream_t s);
 void launch_chol_vertex(const CholVertexArgs& a, cudaStream_t s);
 void launch_chol_finish(const CholVertexArgs& a, cudaStream_t s);
 

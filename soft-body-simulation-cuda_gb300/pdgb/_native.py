@@ -119,6 +119,10 @@ SIGNATURES = {
     "pdgb_default_params": (None, [C.POINTER(pdgb_params)]),
     "pdgb_create": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_params), C.c_void_p, C.POINTER(C.c_void_p)]),
     "pdgb_prepare": (C.c_int, [C.c_void_p]),
+    "pdgb_create_batch": (C.c_int, [C.c_int, C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_params), C.c_void_p,
+                                    C.POINTER(C.c_void_p)]),
+    "pdgb_num_bodies": (C.c_int, [C.c_void_p]),
+    "pdgb_download_body": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
     "pdgb_step": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_set_solver": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_set_params": (C.c_int, [C.c_void_p, C.POINTER(pdgb_params)]),

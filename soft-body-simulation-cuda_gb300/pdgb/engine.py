@@ -49,25 +49,41 @@ def _ptr(a: np.ndarray | None) -> int | None:
     return None if a is None else a.ctypes.data
 
 
+def _host_desc(body: SoftBody, keep: list) -> N.pdgb_mesh_desc:
+    X = np.ascontiguousarray(body.X, dtype=np.float32)
+    tets = np.ascontiguousarray(body.tets, dtype=np.uint32)
+    mass = np.ascontiguousarray(body.mass, dtype=np.float32)
+    mu = np.ascontiguousarray(body.mu, dtype=np.float32)
+    dbc = None if body.dbc is None else np.ascontiguousarray(body.dbc, dtype=np.float32)
+    V = None if body.V is None else np.ascontiguousarray(body.V, dtype=np.float32)
+    keep.extend([X, tets, mass, mu, dbc, V])
+    return N.pdgb_mesh_desc(X.shape[0], tets.shape[0], _ptr(X), _ptr(V), _ptr(tets), _ptr(mass), _ptr(mu),
+                            _ptr(dbc), N.PDGB_MEM_HOST)
+
+
 class PdSolver:
-    def __init__(self, body: SoftBody, params: SolverParams, stream: int | None = None):
+    def __init__(self, body: SoftBody | list, params: SolverParams, stream: int | None = None):
+        """One body, or a list of independent bodies advanced as one batch."""
         self._lib = N.lib()
         self.params = params
         self.body = body
-        X = np.ascontiguousarray(body.X, dtype=np.float32)
-        tets = np.ascontiguousarray(body.tets, dtype=np.uint32)
-        mass = np.ascontiguousarray(body.mass, dtype=np.float32)
-        mu = np.ascontiguousarray(body.mu, dtype=np.float32)
-        dbc = None if body.dbc is None else np.ascontiguousarray(body.dbc, dtype=np.float32)
-        V = None if body.V is None else np.ascontiguousarray(body.V, dtype=np.float32)
-        desc = N.pdgb_mesh_desc(X.shape[0], tets.shape[0], _ptr(X), _ptr(V), _ptr(tets), _ptr(mass), _ptr(mu),
-                                _ptr(dbc), N.PDGB_MEM_HOST)
+        keep: list = []
         h = C.c_void_p()
         prm = params.to_c()
-        N.check(self._lib.pdgb_create(C.byref(desc), C.byref(prm), stream, C.byref(h)), "pdgb_create")
+        if isinstance(body, (list, tuple)):
+            descs = (N.pdgb_mesh_desc * len(body))(*[_host_desc(b, keep) for b in body])
+            N.check(self._lib.pdgb_create_batch(len(body), descs, C.byref(prm), stream, C.byref(h)),
+                    "pdgb_create_batch")
+            self.body_verts = np.cumsum([0] + [b.num_verts for b in body])
+            self.num_verts = int(self.body_verts[-1])
+            self.num_tets = int(sum(b.num_tets for b in body))
+        else:
+            desc = _host_desc(body, keep)
+            N.check(self._lib.pdgb_create(C.byref(desc), C.byref(prm), stream, C.byref(h)), "pdgb_create")
+            self.body_verts = np.array([0, body.num_verts])
+            self.num_verts = body.num_verts
+            self.num_tets = body.num_tets
         self._h = h
-        self.num_verts = X.shape[0]
-        self.num_tets = tets.shape[0]
 
     # -- Solver<float> interface
     def prepare(self) -> None:
@@ -110,6 +126,13 @@ class PdSolver:
         X = np.empty((self.num_verts, 3), dtype=np.float32)
         V = np.empty((self.num_verts, 3), dtype=np.float32)
         N.check(self._lib.pdgb_download_state(self._h, _ptr(X), _ptr(V), N.PDGB_MEM_HOST), "pdgb_download_state")
+        return X, V
+
+    def download_body(self, b: int) -> tuple[np.ndarray, np.ndarray]:
+        n = int(self.body_verts[b + 1] - self.body_verts[b])
+        X = np.empty((n, 3), dtype=np.float32)
+        V = np.empty((n, 3), dtype=np.float32)
+        N.check(self._lib.pdgb_download_body(self._h, int(b), _ptr(X), _ptr(V), N.PDGB_MEM_HOST), "pdgb_download_body")
         return X, V
 
     def get_performance_data(self) -> dict:

@@ -147,6 +147,37 @@ def cube_c2(n: int = 64, seed: int = 2024) -> SoftBody:
     return make_grid_body(n, n, n, young=1e6, poisson=0.45, density=1000.0, jitter=0.1, seed=seed)
 
 
+def batch_c4(nbodies: int = 512, seed: int = 4, lo: int = 4, hi: int = 24, cell: float = 1.0 / 16.0) -> list:
+    """Independent hex-grid bodies, dims uniform lo..hi per axis (seeded),
+    E log-uniform 1e4..1e7, nu uniform 0.3..0.45, density uniform 800..1200,
+    cells of `cell` metres, top faces pinned; bodies laid out on a square
+    grid in the x-z plane (they never touch; there is no collision)."""
+    rng = np.random.default_rng(seed)
+    side = int(math.ceil(math.sqrt(nbodies)))
+    bodies = []
+    for b in range(nbodies):
+        nx, ny, nz = (int(v) for v in rng.integers(lo, hi + 1, size=3))
+        E = float(np.exp(rng.uniform(math.log(1e4), math.log(1e7))))
+        nu = float(rng.uniform(0.3, 0.45))
+        rho = float(rng.uniform(800.0, 1200.0))
+        ox, oz = (b % side) * (hi + 4) * cell, (b // side) * (hi + 4) * cell
+        bodies.append(make_grid_body(nx, ny, nz, size=(nx * cell, ny * cell, nz * cell), origin=(ox, 0.0, oz),
+                                     young=E, poisson=nu, density=rho, seed=seed * 100003 + b))
+    return bodies
+
+
+def concat(bodies: list) -> SoftBody:
+    """One disconnected system holding all bodies (vertex ids offset per body):
+    the reference's multi-body layout (dataLoader.cu:291-378)."""
+    offs = np.cumsum([0] + [b.num_verts for b in bodies])
+    return SoftBody(X=np.concatenate([b.X for b in bodies]).astype(np.float32),
+                    tets=np.concatenate([b.tets + np.uint32(o) for b, o in zip(bodies, offs[:-1])]).astype(np.uint32),
+                    mass=np.concatenate([b.mass for b in bodies]).astype(np.float32),
+                    mu=np.concatenate([b.mu for b in bodies]).astype(np.float32),
+                    dbc=np.concatenate([b.dbc for b in bodies]).astype(np.float32),
+                    meta={"bodies": len(bodies), "vstart": offs})
+
+
 def cube_c3(n: int = 40, seed: int = 3) -> SoftBody:
     """1 m cube, n^3 cells, per-tet E log-uniform [1e4, 1e7], nu uniform [0.3, 0.45]."""
     rng = np.random.default_rng(seed)
