@@ -240,6 +240,31 @@ def run_reference_arm(args, body, params, scale=1.0):
     print(json.dumps(line), flush=True)
 
 
+def accuracy_vs_fp64(body, params, steps: int, refine_sweep: bool = False) -> dict:
+    """Engine vs the FP64 oracle from the rest state, `steps` steps of the
+    workload (a bounded sample); relative L2 errors of positions and of
+    displacements.  With refine_sweep: one entry per refinement count 0..3."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    from pdgb import PdSolver
+    from pdgb.engine import SolverParams
+
+    Xo, _, _ = O.simulate(body, params, steps, precision=64, nthreads=os.cpu_count() or 1)
+    X0 = body.X.astype(np.float64)
+    out = {"steps": steps, "oracle": "fp64"}
+    counts = range(4) if refine_sweep else [params.refine_steps]
+    for r in counts:
+        p = SolverParams(**{**params.__dict__, "refine_steps": r})
+        with PdSolver(body, p) as e:
+            e.update(steps)
+            X, _ = e.download_state()
+        X = X.astype(np.float64)
+        key = f"refine{r}" if refine_sweep else "engine"
+        out[key] = {"rel_err_x": float(np.linalg.norm(X - Xo) / np.linalg.norm(Xo)),
+                    "rel_err_disp": float(np.linalg.norm(X - Xo) / max(np.linalg.norm(Xo - X0), 1e-30))}
+    return out
+
+
 def launches_per_step(info, params) -> int:
     """Kernels of one step graph: prologue, per iteration local + global
     (Jacobi: 1 vertex kernel; Cholesky: 2 per solve level + 1 vertex kernel),
@@ -260,6 +285,7 @@ def main():
     ap.add_argument("--bodies", type=int, default=0, help="override the number of bodies of the batch workload")
     ap.add_argument("--cpu-steps", type=int, default=4, help="PD steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-oracle error report")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "pdgb":
         args.warmup = 3
@@ -381,6 +407,12 @@ def main():
         if bodies is not None:
             cpu["sample"] += f"; the first 16 of the {len(bodies)} bodies"
     clk = clocks.summary()
+    acc = None
+    if not args.no_accuracy:
+        acc_steps = {"c1": 20, "c2": 2, "c3": 3, "c4": 5}[args.workload]
+        acc = accuracy_vs_fp64(cpu_body, params, acc_steps, refine_sweep=args.workload == "c3")
+        if bodies is not None:
+            acc["sample"] = "first 16 bodies of the batch"
     line = {
         "metric": METRIC,
         "value": value,
@@ -406,6 +438,7 @@ def main():
         "clocks": clk,
         "finite": finite,
         "local_step_share": (local_ms / 1e3) / t_local if t_local > 0 else None,
+        "accuracy": acc,
     }
     print(json.dumps(line), flush=True)
 

@@ -58,7 +58,10 @@ struct pdgb_engine {
     float chol_dt = 0.f, chol_pw = -1.f;
     DBuf<int> ch_fwd, ch_bwd, ch_rows, ch_body_level, ch_body_order;
     DBuf<int4> ch_levels;
-    DBuf<float> ch_mval;
+    DBuf<float> ch_mval, ch_mvalT;
+    DBuf<int> k_rowptr, k_colind;  // FP64 K for refinement residuals
+    DBuf<double> k_val;
+    DBuf<float4> bsave, dx;
     bool cta_solve = false;  // whole solve in one CTA (small systems)
     double factor_ms = 0.0;
     // step graph
@@ -111,6 +114,7 @@ void check_params(const pdgb_params& p) {
     if (p.solver != PDGB_SOLVER_JACOBI && p.solver != PDGB_SOLVER_CHOLESKY)
         throw Error{PDGB_ERR_INVALID_ARGUMENT, "unknown solver"};
     if (p.refine_steps < 0 || p.refine_steps > 3) throw Error{PDGB_ERR_INVALID_ARGUMENT, "refine_steps must be 0..3"};
+    // refinement applies to the Cholesky path of single-body engines
     if (!(p.positional_weight >= 0.f)) throw Error{PDGB_ERR_INVALID_ARGUMENT, "positional_weight must be >= 0"};
     if (!(p.tol >= 0.f)) throw Error{PDGB_ERR_INVALID_ARGUMENT, "tol must be >= 0"};
 }
@@ -200,7 +204,7 @@ void record_chol_step(pdgb_engine* e) {
     ba.prev = use_tol ? e->prev.p : nullptr;
     launch_begin(ba, s);
     const LocalArgs la = local_args(e, &st->done);
-    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_rows.p, e->ch_mval.p, e->ch_levels.p, e->ch_body_level.p,
+    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_rows.p, e->ch_mval.p, e->ch_mvalT.p, e->ch_levels.p, e->ch_body_level.p,
                 e->ch_body_order.p, e->b.p, e->y.p, e->sn.p, &st->done};
     CholVertexArgs cv{};
     cv.nv = e->nv;
@@ -216,10 +220,24 @@ void record_chol_step(pdgb_engine* e) {
     cv.x = e->x.p;
     cv.v = e->v.p;
     cv.dt_inv = 1.0f / e->prm.dt;
+    const int refine = e->nbodies == 1 ? e->prm.refine_steps : 0;
+    CholArgs cd = ca;  // refinement solves write the correction into dx
+    cd.x = e->dx.p;
+    RefineArgs ra{e->nv, e->k_rowptr.p, e->k_colind.p, e->k_val.p, e->bsave.p, e->sn.p, e->b.p, e->y.p,
+                  e->dx.p, e->sn.p, &st->done};
+    auto solve = [&](const CholArgs& args) {
+        if (e->cta_solve) launch_chol_solve_cta(args, e->nbodies, s);
+        else launch_chol_solve_levels(args, e->chol.levels, s);
+    };
     for (int i = 0; i < n; ++i) {
         record_local(e, la, false, i);
-        if (e->cta_solve) launch_chol_solve_cta(ca, e->nbodies, s);
-        else launch_chol_solve_levels(ca, e->chol.levels, s);
+        if (refine > 0) launch_copy_rhs(e->nv, e->b.p, e->bsave.p, &st->done, s);
+        solve(ca);
+        for (int r = 0; r < refine; ++r) {
+            launch_refine_residual(ra, s);
+            solve(cd);
+            launch_refine_update(ra, s);
+        }
         cv.iteration = i;
         launch_chol_vertex(cv, s);
     }
@@ -314,10 +332,19 @@ void prepare_cholesky(pdgb_engine* e) {
     e->ch_bwd.upload(f.bwd_items, s);
     e->ch_rows.upload(f.rows, s);
     e->ch_mval.upload(f.mval, s);
+    e->ch_mvalT.upload(f.mvalT, s);
     std::vector<int4> lv(f.levels.size());
     for (size_t i = 0; i < lv.size(); ++i)
         lv[i] = make_int4(f.levels[i].fwd_begin, f.levels[i].fwd_end, f.levels[i].bwd_begin, f.levels[i].bwd_end);
     e->ch_levels.upload(lv, s);
+    if (f.K.n == e->nv) {  // FP64 copy of K for refinement residuals (single body)
+        std::vector<int> rp(f.K.p.begin(), f.K.p.end());
+        e->k_rowptr.upload(rp, s);
+        e->k_colind.upload(f.K.i, s);
+        e->k_val.upload(f.K.x, s);
+        e->bsave.alloc(e->nv);
+        e->dx.alloc(e->nv);
+    }
     e->ch_body_level.upload(f.body_level, s);
     e->ch_body_order.upload(f.body_order, s);
     // A single CTA walks a body's whole tree when the factor is small (the

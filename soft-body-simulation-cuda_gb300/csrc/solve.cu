@@ -16,72 +16,90 @@ namespace pdgb {
 // M_s; sum over pivot columns c0..c1 of M_s[row, c] r[pivot c]; pivot rows
 // add the sum to y, off-diagonal rows subtract it from r (ancestor columns,
 // solved at a later level).  The chunk's pivot right-hand sides are staged
-// in warp-private shared memory (32 at a time).
+// in warp-private shared memory 32 at a time; the column loop issues 8
+// independent loads of M before using them (memory-level parallelism for
+// the few, large supernodes at the top of the tree).
 __device__ __forceinline__ void fwd_warp_item(const CholArgs& a, const int* w, float4* stage, int lane) {
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
     const int roff = h0.z, m = h0.w, k = h1.x, r0 = h1.y, c0 = h1.z, c1 = h1.w;
     const int* rows = a.rows + roff;
-    const float* M = a.mval + moff;
     const int row = r0 + lane;
     const bool valid = row < m;
     const int cend = !valid ? c0 : (row < k ? min(c1, row + 1) : c1);
+    const float* Mr = a.mval + moff + row;
+    const int vid = valid ? __ldg(&rows[row]) : 0;
     float ax = 0.f, ay = 0.f, az = 0.f;
     for (int cb = c0; cb < c1; cb += 32) {
         const int nc = min(32, c1 - cb);
         __syncwarp();
         if (lane < nc) stage[lane] = a.r[__ldg(&rows[cb + lane])];
         __syncwarp();
-        const int ce = min(cend, cb + nc);
-        const float* Mr = M + row;
-#pragma unroll 4
-        for (int c = cb; c < ce; ++c) {
-            const float mv = __ldg(Mr + (size_t)c * m);
-            const float4 v = stage[c - cb];
-            ax = fmaf(mv, v.x, ax);
-            ay = fmaf(mv, v.y, ay);
-            az = fmaf(mv, v.z, az);
+        for (int c = cb; c < cb + nc; c += 8) {
+            float mv[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) mv[q] = (c + q < cend) ? __ldg(Mr + (size_t)(c + q) * m) : 0.f;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                if (c + q < cb + nc) {
+                    const float4 v = stage[c + q - cb];
+                    ax = fmaf(mv[q], v.x, ax);
+                    ay = fmaf(mv[q], v.y, ay);
+                    az = fmaf(mv[q], v.z, az);
+                }
+            }
         }
     }
     if (!valid) return;
-    const int vid = __ldg(&rows[row]);
     if (row < k) atomicAdd(&a.y[vid], make_float4(ax, ay, az, 0.f));
     else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
 }
 
-// Backward warp item {moff, roff, m, k, c}: x[pivot c] = sum_{i >= c}
-// M_s[i, c] z_i with z = [y_pivots ; -x_offdiag]; lanes stride over rows
-// (coalesced column of M_s), then a warp reduction.  No atomics.
-__device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, int lane) {
+// Backward warp item {moff, roff, m, k, c0, c1}: lane = pivot column
+// c0 + lane; x[pivot c] = sum_{i >= c0} M_s[i, c] z_i with z = [y_pivots ;
+// -x_offdiag] (entries above the diagonal of the pivot block are stored
+// zeros).  The row-major copy makes each row's 32 columns one coalesced
+// load; z is staged 32 rows at a time.  No atomics, no reductions.
+__device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, float4* stage, int lane) {
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
-    const int roff = h0.z, m = h0.w, k = h1.x, c = h1.y;
+    const int roff = h0.z, m = h0.w, k = h1.x, c0 = h1.y, c1 = h1.z;
     const int* rows = a.rows + roff;
-    const float* Mc = a.mval + moff + (size_t)c * m;
+    const int c = c0 + lane;
+    const bool cvalid = c < c1;
+    const float* Tc = a.mvalT + moff + c;
     float ax = 0.f, ay = 0.f, az = 0.f;
-#pragma unroll 2
-    for (int i = c + lane; i < m; i += 32) {
-        const int vid = __ldg(&rows[i]);
-        const float mv = __ldg(Mc + i);
-        float4 z;
-        if (i < k) z = a.y[vid];
-        else {
-            const float4 xv = a.x[vid];
-            z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+    for (int i0 = c0; i0 < m; i0 += 32) {
+        const int n = min(32, m - i0);
+        __syncwarp();
+        if (lane < n) {
+            const int i = i0 + lane;
+            const int v = __ldg(&rows[i]);
+            if (i < k) stage[lane] = a.y[v];
+            else {
+                const float4 xv = a.x[v];
+                stage[lane] = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+            }
         }
-        ax = fmaf(mv, z.x, ax);
-        ay = fmaf(mv, z.y, ay);
-        az = fmaf(mv, z.z, az);
-    }
+        __syncwarp();
+        for (int j = 0; j < n; j += 8) {
+            float mv[8];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        ax += __shfl_xor_sync(0xffffffffu, ax, off);
-        ay += __shfl_xor_sync(0xffffffffu, ay, off);
-        az += __shfl_xor_sync(0xffffffffu, az, off);
+            for (int q = 0; q < 8; ++q) mv[q] = (cvalid && j + q < n) ? __ldg(Tc + (size_t)(i0 + j + q) * k) : 0.f;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                if (j + q < n) {
+                    const float4 z = stage[j + q];
+                    ax = fmaf(mv[q], z.x, ax);
+                    ay = fmaf(mv[q], z.y, ay);
+                    az = fmaf(mv[q], z.z, az);
+                }
+            }
+        }
     }
-    if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
+    if (cvalid) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
 }
 
 // ---- one launch per level: each warp takes one item.
@@ -95,11 +113,12 @@ __global__ void __launch_bounds__(kLevelThreads) k_chol_fwd_level(CholArgs a, in
 }
 
 __global__ void __launch_bounds__(kLevelThreads) k_chol_bwd_level(CholArgs a, int item0, int nitems) {
+    __shared__ float4 stage[kLevelThreads / 32][32];
     if (a.done && *a.done) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int it = blockIdx.x * (kLevelThreads / 32) + warp;
     if (it >= nitems) return;
-    bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * (item0 + it), lane);
+    bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * (item0 + it), stage[warp], lane);
 }
 
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
@@ -133,7 +152,8 @@ __global__ void __launch_bounds__(kCtaSolveThreads) k_chol_solve_cta(CholArgs a)
     }
     for (int L = L1 - 1; L >= L0; --L) {
         const int4 lv = __ldg(&a.levels[L]);
-        for (int it = lv.z + warp; it < lv.w; it += kWarps) bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * it, lane);
+        for (int it = lv.z + warp; it < lv.w; it += kWarps)
+            bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * it, stage[warp], lane);
         __syncthreads();
     }
 }
@@ -204,6 +224,60 @@ __global__ void __launch_bounds__(256) k_chol_finish(CholVertexArgs a) {
     a.v[i] = make_float4((s.x - xo.x) * a.dt_inv, (s.y - xo.y) * a.dt_inv, (s.z - xo.z) * a.dt_inv, 0.f);
     a.x[i] = s;
     a.y[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// ---- iterative refinement
+__global__ void __launch_bounds__(256) k_copy_rhs(int nv, const float4* __restrict__ b, float4* bsave,
+                                                  const int* done) {
+    if (done && *done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nv) bsave[i] = b[i];
+}
+
+// One warp per row: r = bsave - K x0 accumulated in double over the row's
+// nonzeros (lanes stride the row, then a warp reduction).
+__global__ void __launch_bounds__(256) k_refine_residual(RefineArgs a) {
+    if (a.done && *a.done) return;
+    const int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= a.nv) return;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int e = __ldg(&a.rowptr[row]) + lane; e < __ldg(&a.rowptr[row + 1]); e += 32) {
+        const double kv = __ldg(&a.val[e]);
+        const float4 xv = a.x0[__ldg(&a.colind[e])];
+        sx = fma(kv, (double)xv.x, sx);
+        sy = fma(kv, (double)xv.y, sy);
+        sz = fma(kv, (double)xv.z, sz);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, off);
+        sy += __shfl_xor_sync(0xffffffffu, sy, off);
+        sz += __shfl_xor_sync(0xffffffffu, sz, off);
+    }
+    if (lane == 0) {
+        const float4 b = a.bsave[row];
+        a.b[row] = make_float4((float)((double)b.x - sx), (float)((double)b.y - sy), (float)((double)b.z - sz), 0.f);
+        a.y[row] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_refine_update(RefineArgs a) {
+    if (a.done && *a.done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nv) return;
+    const float4 x = a.x[i], d = a.dx[i];
+    a.x[i] = make_float4(x.x + d.x, x.y + d.y, x.z + d.z, 0.f);
+}
+
+void launch_copy_rhs(int nv, const float4* b, float4* bsave, const int* done, cudaStream_t s) {
+    if (nv > 0) k_copy_rhs<<<(nv + 255) / 256, 256, 0, s>>>(nv, b, bsave, done);
+}
+void launch_refine_residual(const RefineArgs& a, cudaStream_t s) {
+    if (a.nv > 0) k_refine_residual<<<(a.nv + 7) / 8, 256, 0, s>>>(a);
+}
+void launch_refine_update(const RefineArgs& a, cudaStream_t s) {
+    if (a.nv > 0) k_refine_update<<<(a.nv + 255) / 256, 256, 0, s>>>(a);
 }
 
 void launch_chol_vertex(const CholVertexArgs& a, cudaStream_t s) {

@@ -17,7 +17,8 @@ struct CholArgs {
     const int* fwd_items;  // kItemInts per item
     const int* bwd_items;  // kItemInts per item
     const int* rows;
-    const float* mval;
+    const float* mval;       // M_s column major (forward)
+    const float* mvalT;      // M_s row major (backward)
     const int4* levels;      // {fwd_begin, fwd_end, bwd_begin, bwd_end} per level, body-major
     const int* body_level;   // [nbodies + 1]: levels of body b (CTA solve)
     const int* body_order;   // CTA -> body (largest factor first)
@@ -57,6 +58,27 @@ void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& 
 // The whole solve of one body in one CTA, levels separated by
 // __syncthreads; one CTA per body (small systems and batches of bodies).
 void launch_chol_solve_cta(const CholArgs& a, int nbodies, cudaStream_t s);
+// FP64-residual iterative refinement of the global solve:
+//   bsave = b (before the solve destroys it);
+//   r = bsave - K x0 in double (K: FP64 CSR over vertex ids), b = r, y = 0;
+//   solve K dx = b with the FP32 factor; x0 += dx.
+struct RefineArgs {
+    int nv;
+    const int* rowptr;
+    const int* colind;
+    const double* val;
+    const float4* bsave;
+    const float4* x0;
+    float4* b;
+    float4* y;
+    float4* dx;
+    float4* x;
+    const int* done;
+};
+void launch_copy_rhs(int nv, const float4* b, float4* bsave, const int* done, cudaStream_t s);
+void launch_refine_residual(const RefineArgs& a, cudaStream_t s);
+void launch_refine_update(const RefineArgs& a, cudaStream_t s);
+
 void launch_chol_vertex(const CholVertexArgs& a, cudaStream_t s);
 void launch_chol_finish(const CholVertexArgs& a, cudaStream_t s);
 

