@@ -58,7 +58,7 @@ struct pdgb_engine {
     float chol_dt = 0.f, chol_pw = -1.f;
     DBuf<int> ch_fwd, ch_bwd, ch_rows, ch_body_level, ch_body_order;
     DBuf<int4> ch_levels;
-    DBuf<float> ch_mval, ch_mvalT;
+    DBuf<float> ch_mval;
     DBuf<int> k_rowptr, k_colind;  // FP64 K for refinement residuals
     DBuf<double> k_val;
     DBuf<float4> bsave, dx;
@@ -204,7 +204,7 @@ void record_chol_step(pdgb_engine* e) {
     ba.prev = use_tol ? e->prev.p : nullptr;
     launch_begin(ba, s);
     const LocalArgs la = local_args(e, &st->done);
-    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_rows.p, e->ch_mval.p, e->ch_mvalT.p, e->ch_levels.p, e->ch_body_level.p,
+    CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_rows.p, e->ch_mval.p, e->ch_levels.p, e->ch_body_level.p,
                 e->ch_body_order.p, e->b.p, e->y.p, e->sn.p, &st->done};
     CholVertexArgs cv{};
     cv.nv = e->nv;
@@ -332,7 +332,6 @@ void prepare_cholesky(pdgb_engine* e) {
     e->ch_bwd.upload(f.bwd_items, s);
     e->ch_rows.upload(f.rows, s);
     e->ch_mval.upload(f.mval, s);
-    e->ch_mvalT.upload(f.mvalT, s);
     std::vector<int4> lv(f.levels.size());
     for (size_t i = 0; i < lv.size(); ++i)
         lv[i] = make_int4(f.levels[i].fwd_begin, f.levels[i].fwd_end, f.levels[i].bwd_begin, f.levels[i].bwd_end);

@@ -628,14 +628,6 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         for (int q = 0; q < m; ++q) relpos[st[q]] = -1;
     }
     out.flops = flops;
-    out.mvalT.resize(out.mval.size());
-    for (int s = 0; s < ns; ++s) {
-        const int k = out.sk[s], m = out.sm[s];
-        const float* M = &out.mval[out.moff[s]];
-        float* T = &out.mvalT[out.moff[s]];
-        for (int c = 0; c < k; ++c)
-            for (int i = 0; i < m; ++i) T[(size_t)i * k + c] = M[(size_t)c * m + i];
-    }
     {
         long long st_tot = 0;
         for (int s = 0; s < ns; ++s) st_tot += (long long)out.sk[s] * out.sm[s] - (long long)out.sk[s] * (out.sk[s] - 1) / 2;
@@ -666,8 +658,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
                     out.fwd_items.insert(out.fwd_items.end(),
                                          {lo, hi, out.roff[s], m, k, r0, c0, std::min(cmax, c0 + kFwdItemCols)});
             }
-            for (int c0 = 0; c0 < k; c0 += kBwdItemCols)
-                out.bwd_items.insert(out.bwd_items.end(), {lo, hi, out.roff[s], m, k, c0, std::min(k, c0 + kBwdItemCols), 0});
+            for (int c = 0; c < k; ++c) out.bwd_items.insert(out.bwd_items.end(), {lo, hi, out.roff[s], m, k, c, 0, 0});
         }
         lv.fwd_end = (int)(out.fwd_items.size() / kItemInts);
         lv.bwd_end = (int)(out.bwd_items.size() / kItemInts);
@@ -728,7 +719,6 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         }
         out.nsuper += f.nsuper;
         out.mval.insert(out.mval.end(), f.mval.begin(), f.mval.end());
-        out.mvalT.insert(out.mvalT.end(), f.mvalT.begin(), f.mvalT.end());
         for (int r : f.rows) out.rows.push_back(r + v0);
         auto shift = [&](std::vector<int>& dst, const std::vector<int>& src) {
             const int base_item = (int)(dst.size() / kItemInts);
@@ -792,18 +782,16 @@ void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3) {
     for (int L = f.body_level[b + 1] - 1; L >= f.body_level[b]; --L)
         for (int it = f.levels[L].bwd_begin; it < f.levels[L].bwd_end; ++it) {
             const int* w = &f.bwd_items[kItemInts * (size_t)it];
-            const int roff = w[2], m = w[3], k = w[4], c0 = w[5], c1 = w[6];
-            const float* T = &f.mvalT[moff_of(w)];
+            const int roff = w[2], m = w[3], k = w[4], c = w[5];
+            const float* M = &f.mval[moff_of(w)];
             const int* rows = &f.rows[roff];
-            for (int c = c0; c < c1; ++c) {
-                double acc[3] = {0, 0, 0};
-                for (int i = c0; i < m; ++i) {
-                    const size_t o = 3 * (size_t)rows[i];
-                    const double mv = T[(size_t)i * k + c];
-                    for (int d = 0; d < 3; ++d) acc[d] += mv * (i < k ? y[o + d] : -x3[o + d]);
-                }
-                for (int d = 0; d < 3; ++d) x3[3 * (size_t)rows[c] + d] = acc[d];
+            double acc[3] = {0, 0, 0};
+            for (int i = c; i < m; ++i) {
+                const size_t o = 3 * (size_t)rows[i];
+                const double mv = M[(size_t)c * m + i];
+                for (int d = 0; d < 3; ++d) acc[d] += mv * (i < k ? y[o + d] : -x3[o + d]);
             }
+            for (int d = 0; d < 3; ++d) x3[3 * (size_t)rows[c] + d] = acc[d];
         }
 }
 

@@ -49,12 +49,10 @@ struct SolveLevel {
 //   forward : {moff_lo, moff_hi, roff, m, k, r0, c0, c1}: rows r0 .. min(r0+32, m)
 //             of M_s (column major) times the right-hand side of pivot
 //             columns c0 .. c1
-//   backward: {moff_lo, moff_hi, roff, m, k, c0, c1, 0}: pivot columns
-//             c0 .. c1 (at most 32, one per lane) from the row-major copy
+//   backward: {moff_lo, moff_hi, roff, m, k, c, 0, 0}: pivot column c
 constexpr int kItemInts = 8;
 constexpr int kFwdItemRows = 32;
 constexpr int kFwdItemCols = 64;
-constexpr int kBwdItemCols = 32;
 
 struct CholFactor {
     int n = 0;
@@ -66,8 +64,7 @@ struct CholFactor {
     std::vector<int64_t> moff;       // offset of M_s in mval (column major m x k)
     std::vector<int> roff;           // offset of the row list in rows
     std::vector<int> rows;           // row lists (vertex ids; first k = pivots)
-    std::vector<float> mval;         // FP32 M_s blocks, column major (forward pass)
-    std::vector<float> mvalT;        // the same blocks, row major (backward pass)
+    std::vector<float> mval;         // FP32 M_s blocks, column major
     std::vector<int> level;          // level of each supernode (leaves = 0)
     int nlevels = 0;
     // GPU warp work items grouped by level (see kItemInts).

@@ -26,28 +26,42 @@ namespace pdgb {
 // shared-memory atomics; within a tile the sums are deterministic.
 template <bool kJacobiForm, int kRotation>
 __global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
+    // corner-major slots: corner c of local tet lt lives at c * kTileTets + lt
     __shared__ float4 slot[4 * kTileTets];
     if (a.done && *a.done) return;
     const int tile = blockIdx.x;
     const int vb = a.tile_vptr[tile];
     const int np = a.tile_vptr[tile + 1] - vb;
     const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
+    const int ntile = t1 - t0;
     const uint16_t* inc = a.inc_ent + 4 * (size_t)t0;
     const uint16_t* iend = a.inc_end + vb;
+    // Issue the per-tet geometry loads of this thread's tets first: they are
+    // in flight while the patch positions are gathered and scattered.
+    constexpr int kPer = kTileTets / kLocalThreads;
+    const int ntp = a.nt_pad;
+    float G[kPer][10];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        const int lt = threadIdx.x + j * kLocalThreads;
+        const int t = t0 + (lt < ntile ? lt : 0);
+#pragma unroll
+        for (int k = 0; k < 10; ++k) G[j][k] = __ldg(&a.geo[k * ntp + t]);
+    }
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
         const float4 p = __ldg(&a.sn[a.tile_verts[vb + k] & ~kPinnedBit]);
         const int e0 = k ? __ldg(&iend[k - 1]) : 0, e1 = __ldg(&iend[k]);
         for (int e = e0; e < e1; ++e) slot[__ldg(&inc[e])] = p;
     }
     __syncthreads();
-    const int ntp = a.nt_pad;
-    for (int lt = threadIdx.x; lt < t1 - t0; lt += kLocalThreads) {
-        const int t = t0 + lt;
-        float D[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) D[k] = __ldg(&a.geo[k * ntp + t]);
-        const float c = __ldg(&a.geo[9 * ntp + t]);
-        const float4 p0 = slot[4 * lt], p1 = slot[4 * lt + 1], p2 = slot[4 * lt + 2], p3 = slot[4 * lt + 3];
+    for (int j = 0; j < kPer; ++j) {
+        const int lt = threadIdx.x + j * kLocalThreads;
+        if (lt >= ntile) break;
+        const float* D = G[j];
+        const float c = G[j][9];
+        const float4 p0 = slot[lt], p1 = slot[kTileTets + lt], p2 = slot[2 * kTileTets + lt],
+                     p3 = slot[3 * kTileTets + lt];
         // Ds columns = edges; F = Ds * DmInv (row-major F[r][c])
         const float e[3][3] = {{p1.x - p0.x, p2.x - p0.x, p3.x - p0.x},
                                {p1.y - p0.y, p2.y - p0.y, p3.y - p0.y},
@@ -73,10 +87,10 @@ __global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) M[3 * r + cc] = fmaf(r0, D[3 * cc], fmaf(r1, D[3 * cc + 1], r2 * D[3 * cc + 2]));
         }
-        slot[4 * lt + 0] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
-        slot[4 * lt + 1] = make_float4(M[0], M[3], M[6], 0.f);
-        slot[4 * lt + 2] = make_float4(M[1], M[4], M[7], 0.f);
-        slot[4 * lt + 3] = make_float4(M[2], M[5], M[8], 0.f);
+        slot[lt] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
+        slot[kTileTets + lt] = make_float4(M[0], M[3], M[6], 0.f);
+        slot[2 * kTileTets + lt] = make_float4(M[1], M[4], M[7], 0.f);
+        slot[3 * kTileTets + lt] = make_float4(M[2], M[5], M[8], 0.f);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {

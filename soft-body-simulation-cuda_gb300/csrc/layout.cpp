@@ -191,7 +191,7 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
         for (int i = start; i < end; ++i)
             for (int c = 0; c < 4; ++c) {
                 const int k = loc[L.tets_int[4 * (size_t)i + c]];
-                L.inc_ent[4 * (size_t)start + cnt[k]++] = (uint16_t)(4 * (i - start) + c);
+                L.inc_ent[4 * (size_t)start + cnt[k]++] = (uint16_t)(c * kTileTets + (i - start));
             }
         for (int v : patch) {
             const int o = L.vperm[v];

@@ -192,8 +192,9 @@ __device__ __forceinline__ void closest_rotation_horn(const float F[9], float R[
     float f2 = 0.f;
 #pragma unroll
     for (int i = 0; i < 9; ++i) f2 = fmaf(F[i], F[i], f2);
-    const float c = 0.6f * sqrtf(f2);
-    const float sc = 1.0f / fmaxf(4.0f * c, 1e-30f);
+    f2 = fmaxf(f2, 1e-30f);
+    const float c = 0.6f * f2 * rsqrtf(f2);      // shift; precision irrelevant
+    const float sc = __fdividef(0.25f, c);       // eigenvalues of A / (4c) <= 1
     float a[10];
     a[0] = (F[0] + F[4] + F[8] + c) * sc;
     a[1] = (F[0] - F[4] - F[8] + c) * sc;
@@ -205,17 +206,26 @@ __device__ __forceinline__ void closest_rotation_horn(const float F[9], float R[
     a[7] = (F[1] + F[3]) * sc;
     a[8] = (F[2] + F[6]) * sc;
     a[9] = (F[5] + F[7]) * sc;
+    // A^16: the top eigenvalue of A/(4c) is >= 1/4, so no underflow yet.
     sym4_square(a);
     sym4_square(a);
     sym4_square(a);
-    for (int k = 0; k < kTail; ++k) {
-        const float it = 1.0f / (a[0] + a[1] + a[2] + a[3]);
+    const float t8 = a[0] + a[1] + a[2] + a[3];
+    sym4_square(a);
+    float t = a[0] + a[1] + a[2] + a[3];        // = trace(P8^2)
+    if (t < (1.0f - 4e-7f) * t8 * t8) {
+        // slow convergence (strongly stretched or inverted F): normalised
+        // squarings until P is rank one to float precision.
+        for (int k = 0; k < kTail; ++k) {
+            const float it = __fdividef(1.0f, t);
 #pragma unroll
-        for (int i = 0; i < 10; ++i) a[i] *= it;
-        const float off = a[4] * a[4] + a[5] * a[5] + a[6] * a[6] + a[7] * a[7] + a[8] * a[8] + a[9] * a[9];
-        const float t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3] + 2.0f * off;
-        sym4_square(a);
-        if (t2 >= 1.0f - 4e-7f) break;
+            for (int i = 0; i < 10; ++i) a[i] *= it;
+            sym4_square(a);
+            const float tn = a[0] + a[1] + a[2] + a[3];
+            const bool conv = tn >= 1.0f - 4e-7f;
+            t = tn;
+            if (conv) break;
+        }
     }
     // column with the largest diagonal entry
     float qw = a[0], qx = a[4], qy = a[5], qz = a[6], best = a[0];

@@ -56,50 +56,41 @@ __device__ __forceinline__ void fwd_warp_item(const CholArgs& a, const int* w, f
     else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
 }
 
-// Backward warp item {moff, roff, m, k, c0, c1}: lane = pivot column
-// c0 + lane; x[pivot c] = sum_{i >= c0} M_s[i, c] z_i with z = [y_pivots ;
-// -x_offdiag] (entries above the diagonal of the pivot block are stored
-// zeros).  The row-major copy makes each row's 32 columns one coalesced
-// load; z is staged 32 rows at a time.  No atomics, no reductions.
+// Backward warp item {moff, roff, m, k, c}: x[pivot c] = sum_{i >= c}
+// M_s[i, c] z_i with z = [y_pivots ; -x_offdiag]; lanes stride over rows
+// (a coalesced column of M_s, 4 independent loads in flight per lane),
+// then a warp reduction.  One column per warp keeps the large supernodes at
+// the top of the tree spread over many warps.  No atomics.
 __device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, float4* stage, int lane) {
+    (void)stage;
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
-    const int roff = h0.z, m = h0.w, k = h1.x, c0 = h1.y, c1 = h1.z;
+    const int roff = h0.z, m = h0.w, k = h1.x, c = h1.y;
     const int* rows = a.rows + roff;
-    const int c = c0 + lane;
-    const bool cvalid = c < c1;
-    const float* Tc = a.mvalT + moff + c;
+    const float* Mc = a.mval + moff + (size_t)c * m;
     float ax = 0.f, ay = 0.f, az = 0.f;
-    for (int i0 = c0; i0 < m; i0 += 32) {
-        const int n = min(32, m - i0);
-        __syncwarp();
-        if (lane < n) {
-            const int i = i0 + lane;
-            const int v = __ldg(&rows[i]);
-            if (i < k) stage[lane] = a.y[v];
-            else {
-                const float4 xv = a.x[v];
-                stage[lane] = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
-            }
+#pragma unroll 4
+    for (int i = c + lane; i < m; i += 32) {
+        const int vid = __ldg(&rows[i]);
+        const float mv = __ldg(Mc + i);
+        float4 z;
+        if (i < k) z = a.y[vid];
+        else {
+            const float4 xv = a.x[vid];
+            z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
         }
-        __syncwarp();
-        for (int j = 0; j < n; j += 8) {
-            float mv[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) mv[q] = (cvalid && j + q < n) ? __ldg(Tc + (size_t)(i0 + j + q) * k) : 0.f;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                if (j + q < n) {
-                    const float4 z = stage[j + q];
-                    ax = fmaf(mv[q], z.x, ax);
-                    ay = fmaf(mv[q], z.y, ay);
-                    az = fmaf(mv[q], z.z, az);
-                }
-            }
-        }
+        ax = fmaf(mv, z.x, ax);
+        ay = fmaf(mv, z.y, ay);
+        az = fmaf(mv, z.z, az);
     }
-    if (cvalid) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, off);
+        ay += __shfl_xor_sync(0xffffffffu, ay, off);
+        az += __shfl_xor_sync(0xffffffffu, az, off);
+    }
+    if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
 }
 
 // ---- one launch per level: each warp takes one item.

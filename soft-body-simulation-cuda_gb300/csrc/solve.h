@@ -17,8 +17,7 @@ struct CholArgs {
     const int* fwd_items;  // kItemInts per item
     const int* bwd_items;  // kItemInts per item
     const int* rows;
-    const float* mval;       // M_s column major (forward)
-    const float* mvalT;      // M_s row major (backward)
+    const float* mval;       // M_s column major
     const int4* levels;      // {fwd_begin, fwd_end, bwd_begin, bwd_end} per level, body-major
     const int* body_level;   // [nbodies + 1]: levels of body b (CTA solve)
     const int* body_order;   // CTA -> body (largest factor first)
