@@ -34,10 +34,12 @@ def test_batch_equals_bodies_alone(solver):
         assert e_alone < 1e-5, (b, e_alone)
         Xo, _, _ = O.simulate(body, params, 6, precision=64)
         assert rel_l2(Xb, Xo) < TOL, (b, rel_l2(Xb, Xo))
-        # displacement-relative diagnostic: stiff bodies move ~1e-4 m, where
-        # float rounding of ~1 m coordinates alone is ~1e-3 of the motion
+        # displacement diagnostic: stiff bodies placed ~1 m from the origin move
+        # ~1e-4 m, and float32 rounding of the coordinates alone is ~1e-3 of
+        # that motion, so the bound is relative or 1e-6 m rms, whichever is larger
+        d_err = float(np.linalg.norm(Xb - Xo) / np.sqrt(body.num_verts))
         disp = float(np.linalg.norm(Xo - body.X) / np.sqrt(body.num_verts))
-        assert rel_l2(Xb - body.X, Xo - body.X) < max(2e-3, 3e-7 / max(disp, 1e-12)), (b, disp)
+        assert d_err < max(2e-3 * disp, 1e-6), (b, d_err, disp)
 
 
 def test_batch_uneven_sizes_cholesky():
