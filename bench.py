@@ -56,6 +56,14 @@ WORKLOADS = {
                 "+ 1 vertex launch per iteration, CUDA graph per step",
         "nbodies": 512, "iterations": 10, "solver": "cholesky",
     },
+    "c5": {
+        "workload": "pd_serving_poisson200",
+        "desc": "request stream: Poisson arrivals 200 req/s over the arrival window, each a near-cubic hex-grid body "
+                "with tets log-uniform 1e3..3e5 (drawn from a seeded pool of 48 bodies), material as the batch "
+                "workload, K steps uniform 10..200, dt=1/120, 10 Jacobi+Chebyshev iterations; continuous batching, "
+                "admission by an 8 GiB HBM budget",
+        "rate": 200.0, "iterations": 10, "solver": "jacobi",
+    },
     "c3": {
         "workload": "pd_cholesky_hetero40",
         "desc": "40^3 hex grid x5 tets (68921 v / 320000 t), per-tet E log-uniform 1e4..1e7 (seed 3), nu U[0.3,0.45], "
@@ -265,6 +273,95 @@ def accuracy_vs_fp64(body, params, steps: int, refine_sweep: bool = False) -> di
     return out
 
 
+def run_serving(args):
+    """Serving workload: wall-clock request arrivals into the server."""
+    import math
+
+    from pdgb import PdServer, PdSolver, mesh
+    from pdgb.engine import SolverParams
+
+    rank, world, local = dist_info()
+    import torch
+
+    torch.cuda.set_device(local)
+    wl = dict(WORKLOADS["c5"])
+    rng = np.random.default_rng(5)
+    pool = [mesh.request_body(math.exp(rng.uniform(math.log(1e3), math.log(3e5))), rng) for _ in range(48)]
+    window = args.window
+    n_req = int(rng.poisson(wl["rate"] * window))
+    arrivals = np.sort(rng.uniform(0.0, window, size=n_req))
+    picks = rng.integers(0, len(pool), size=n_req)
+    ksteps = rng.integers(10, 201, size=n_req)
+    params = SolverParams(num_iterations=wl["iterations"], rho=0.9995, solver=0)
+    offered = float(sum(pool[p].num_tets * int(k) for p, k in zip(picks, ksteps)) * params.num_iterations / window)
+    srv = PdServer(params, hbm_budget_bytes=8 << 30)
+    # warm-up: a few requests through the server (graph capture, pool growth)
+    for p in range(4):
+        srv.submit(pool[p], 2)
+    while srv.stats()["completed"] < 4:
+        srv.tick()
+    base_completed = srv.stats()["completed"]
+    base_ti = srv.stats()["tet_iterations"]
+    ids = []
+    t0 = time.perf_counter()
+    nxt = 0
+    with ClockSampler(local) as clocks:
+        while True:
+            now = time.perf_counter() - t0
+            while nxt < n_req and arrivals[nxt] <= now:
+                ids.append((srv.submit(pool[picks[nxt]], int(ksteps[nxt])), int(picks[nxt]), int(ksteps[nxt])))
+                nxt += 1
+            st = srv.stats()
+            if nxt >= n_req and st["completed"] - base_completed >= n_req:
+                break
+            if st["active"] == 0 and st["waiting"] == 0:
+                time.sleep(0.0005)
+                continue
+            srv.tick()
+        wall = time.perf_counter() - t0
+    st = srv.stats()
+    lat = srv.latencies_ms()[base_completed:]
+    value = (st["tet_iterations"] - base_ti) / wall
+    # same alone vs in the mix, on a 1 % sample (the smallest sampled bodies first)
+    sample = sorted(range(len(ids)), key=lambda i: pool[ids[i][1]].num_tets)[: max(1, len(ids) // 100)]
+    worst_alone = 0.0
+    results = {}
+    for i in sample:
+        rid, p, k = ids[i]
+        results[i] = srv.result(rid)[0]
+    for i in sample:
+        rid, p, k = ids[i]
+        with PdSolver(pool[p], params) as e:
+            e.update(k)
+            Xa, _ = e.download_state()
+        worst_alone = max(worst_alone, float(np.linalg.norm(results[i] - Xa) / np.linalg.norm(Xa)))
+    acc = None
+    if not args.no_accuracy:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle as O
+
+        i = sample[0]
+        rid, p, k = ids[i]
+        Xo, _, _ = O.simulate(pool[p], params, k, precision=64, nthreads=os.cpu_count() or 1)
+        acc = {"request_tets": pool[p].num_tets, "steps": k,
+               "rel_err_x_vs_fp64": float(np.linalg.norm(results[i] - Xo) / np.linalg.norm(Xo))}
+    srv.close()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": int(ksteps.sum()),
+        "warmup": 4, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": dict(wl, window_s=window, requests=n_req, offered_tet_iter_per_s=offered),
+        "latency_ms": {"p50": float(np.percentile(lat, 50)) if len(lat) else None,
+                       "p99": float(np.percentile(lat, 99)) if len(lat) else None,
+                       "mean": float(np.mean(lat)) if len(lat) else None},
+        "wall_s": wall, "completed": int(st["completed"] - base_completed), "failed": int(st["failed"]),
+        "alone_vs_mix_max_rel_err": worst_alone, "alone_vs_mix_sample": len(sample),
+        "accuracy": acc, "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def launches_per_step(info, params) -> int:
     """Kernels of one step graph: prologue, per iteration local + global
     (Jacobi: 1 vertex kernel; Cholesky: 2 per solve level + 1 vertex kernel),
@@ -286,6 +383,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4, help="PD steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-oracle error report")
+    ap.add_argument("--window", type=float, default=20.0, help="arrival window of the serving workload, seconds")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "pdgb":
         args.warmup = 3
@@ -293,6 +391,9 @@ def main():
     from pdgb import mesh
     from pdgb.engine import SolverParams
 
+    if args.workload == "c5" and args.impl != "reference":
+        run_serving(args)
+        return
     global WORKLOAD
     WORKLOAD = dict(WORKLOADS[args.workload])
     WORKLOAD["l2"] = "flushed between timed steps (256 MB write)"

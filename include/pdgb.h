@@ -118,6 +118,58 @@ int pdgb_num_bodies(pdgb_engine* e);
 /* State of one body of a batch (caller layout, nv_b x 3 floats each). */
 int pdgb_download_body(pdgb_engine* e, int body, float* X, float* V, int memory);
 
+/* ---------------------------------------------------------------------
+ * Serving: a request loop with continuous batching (no counterpart in the
+ * reference, which advances one scene per frame).  Requests are soft bodies
+ * with a step count, submitted at any time.  Host threads prepare each
+ * request's layout; pdgb_server_tick admits ready requests in arrival order
+ * while their device memory fits hbm_budget_bytes (and max_active), runs ONE
+ * PD step (Jacobi + Chebyshev, the shared params) for every active request
+ * with one set of launches, and retires finished requests (state copied to
+ * host memory, device memory returned to the server's pool).  A request's
+ * arithmetic is that of a single engine, so its result does not depend on
+ * the other requests in the mix. */
+typedef struct pdgb_server_config {
+    pdgb_params params;       /* shared solver parameters (Jacobi path)       */
+    size_t hbm_budget_bytes;  /* device bytes of resident requests           */
+    int max_active;           /* slot limit, 0 = budget only                  */
+    int host_threads;         /* layout workers, 0 = half the host cores      */
+} pdgb_server_config;
+
+#define PDGB_REQ_QUEUED 0
+#define PDGB_REQ_PREPARING 1
+#define PDGB_REQ_READY 2
+#define PDGB_REQ_RUNNING 3
+#define PDGB_REQ_DONE 4
+#define PDGB_REQ_FAILED 5
+
+typedef struct pdgb_server_stats {
+    long long completed;
+    long long failed;
+    int active;               /* requests resident and stepping              */
+    int waiting;              /* submitted, not yet admitted                  */
+    size_t bytes_in_use;
+    double tet_iterations;    /* sum over steps run of tets x iterations      */
+    double busy_ms;           /* host time spent inside pdgb_server_tick      */
+} pdgb_server_stats;
+
+typedef struct pdgb_server pdgb_server;
+void pdgb_server_default_config(pdgb_server_config* cfg);
+int pdgb_server_create(const pdgb_server_config* cfg, void* stream, pdgb_server** out);
+/* Copies the host mesh; returns the request id. */
+int pdgb_server_submit(pdgb_server* s, const pdgb_mesh_desc* mesh, int nsteps, long long* request_id);
+/* Admission + one step of every active request + retirement (waits for the
+ * step).  active / completed (nullable): requests resident after the tick,
+ * requests finished by it. */
+int pdgb_server_tick(pdgb_server* s, int* active, int* completed);
+int pdgb_server_poll(pdgb_server* s, long long request_id, int* state, int* steps_done);
+/* Final state of a finished request (caller layout); releases the request. */
+int pdgb_server_result(pdgb_server* s, long long request_id, float* X, float* V);
+int pdgb_server_get_stats(pdgb_server* s, pdgb_server_stats* out);
+/* Submit-to-finish latencies of all completed requests, in ms. */
+int pdgb_server_latencies(pdgb_server* s, double* out_ms, int capacity, int* count);
+int pdgb_server_destroy(pdgb_server* s);
+
 /* Replaces PdSolver::SolverPrepare (pdSolver.cu:40-139): per-tet DmInv/V0,
  * system assembly, ordering and factorisation, step graph.  pdgb_step calls
  * it on first use, as PdSolver::Update does (pdSolver.cu:212-216). */

@@ -25,11 +25,7 @@ namespace pdgb {
 // (pinned vertices are skipped: their RHS is the pin term).  No
 // shared-memory atomics; within a tile the sums are deterministic.
 template <bool kJacobiForm, int kRotation>
-__global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
-    // corner-major slots: corner c of local tet lt lives at c * kTileTets + lt
-    __shared__ float4 slot[4 * kTileTets];
-    if (a.done && *a.done) return;
-    const int tile = blockIdx.x;
+__device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4* slot) {
     const int vb = a.tile_vptr[tile];
     const int np = a.tile_vptr[tile + 1] - vb;
     const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
@@ -108,6 +104,30 @@ __global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
     }
 }
 
+template <bool kJacobiForm, int kRotation>
+__global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
+    // corner-major slots: corner c of local tet lt lives at c * kTileTets + lt
+    __shared__ float4 slot[4 * kTileTets];
+    if (a.done && *a.done) return;
+    local_tile<kJacobiForm, kRotation>(a, blockIdx.x, slot);
+}
+
+// Multi-request form (serving): CTA i runs tile list[i] of request
+// descriptor req[list[i].x]; CTAs beyond *count exit.
+template <bool kJacobiForm>
+__global__ void __launch_bounds__(kLocalThreads) k_local_multi(const LocalArgs* __restrict__ req,
+                                                               const int2* __restrict__ list,
+                                                               const int* __restrict__ count) {
+    __shared__ float4 slot[4 * kTileTets];
+    if ((int)blockIdx.x >= *count) return;
+    const int2 w = list[blockIdx.x];
+    local_tile<kJacobiForm, PDGB_ROTATION_QUAT>(req[w.x], w.y, slot);
+}
+
+void launch_local_multi(const LocalArgs* req, const int2* list, const int* count, int grid, cudaStream_t s) {
+    if (grid > 0) k_local_multi<true><<<grid, kLocalThreads, 0, s>>>(req, list, count);
+}
+
 void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, int rotation, cudaStream_t s) {
     if (ntiles <= 0) return;
     if (rotation == PDGB_ROTATION_SVD) {
@@ -131,9 +151,7 @@ __device__ __forceinline__ float relax09(float nx, float s) {
 }
 
 template <int kMode>
-__global__ void __launch_bounds__(256) k_jacobi_vertex(VertexArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.nv) return;
+__device__ __forceinline__ void jacobi_vertex(const VertexArgs& a, int i, float omega) {
     const float4 s = a.sn[i];
     const float4 cf = __ldg(&a.coef[i]);
     const float cm = cf.x, md = cf.y;
@@ -146,9 +164,9 @@ __global__ void __launch_bounds__(256) k_jacobi_vertex(VertexArgs a) {
     nx.w = 0.f;
     if (kMode & kReadPrev) {
         const float4 p = a.prev[i];
-        nx.x = (nx.x - p.x) * a.omega + p.x;
-        nx.y = (nx.y - p.y) * a.omega + p.y;
-        nx.z = (nx.z - p.z) * a.omega + p.z;
+        nx.x = (nx.x - p.x) * omega + p.x;
+        nx.y = (nx.y - p.y) * omega + p.y;
+        nx.z = (nx.z - p.z) * omega + p.z;
     }
     if (kMode & kWritePrev) a.prev[i] = s;
     if (kMode & kFinal) {
@@ -158,6 +176,40 @@ __global__ void __launch_bounds__(256) k_jacobi_vertex(VertexArgs a) {
     } else {
         a.sn[i] = nx;
         a.b[i] = __ldg(&a.base[i]);
+    }
+}
+
+template <int kMode>
+__global__ void __launch_bounds__(256) k_jacobi_vertex(VertexArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.nv) jacobi_vertex<kMode>(a, i, a.omega);
+}
+
+// Multi-request form: CTA i updates 256 vertices of request list[i].x
+// starting at list[i].y.
+template <int kMode>
+__global__ void __launch_bounds__(256) k_jacobi_vertex_multi(const VertexArgs* __restrict__ req,
+                                                             const int2* __restrict__ list,
+                                                             const int* __restrict__ count, float omega) {
+    if ((int)blockIdx.x >= *count) return;
+    const int2 w = list[blockIdx.x];
+    const VertexArgs& a = req[w.x];
+    const int i = w.y + threadIdx.x;
+    if (i < a.nv) jacobi_vertex<kMode>(a, i, omega);
+}
+
+void launch_jacobi_vertex_multi(const VertexArgs* req, const int2* list, const int* count, int grid, int mode,
+                                float omega, cudaStream_t s) {
+    if (grid <= 0) return;
+    switch (mode & 7) {
+        case 0: k_jacobi_vertex_multi<0><<<grid, 256, 0, s>>>(req, list, count, omega); break;
+        case 1: k_jacobi_vertex_multi<1><<<grid, 256, 0, s>>>(req, list, count, omega); break;
+        case 2: k_jacobi_vertex_multi<2><<<grid, 256, 0, s>>>(req, list, count, omega); break;
+        case 3: k_jacobi_vertex_multi<3><<<grid, 256, 0, s>>>(req, list, count, omega); break;
+        case 4: k_jacobi_vertex_multi<4><<<grid, 256, 0, s>>>(req, list, count, omega); break;
+        case 5: k_jacobi_vertex_multi<5><<<grid, 256, 0, s>>>(req, list, count, omega); break;
+        case 6: k_jacobi_vertex_multi<6><<<grid, 256, 0, s>>>(req, list, count, omega); break;
+        default: k_jacobi_vertex_multi<7><<<grid, 256, 0, s>>>(req, list, count, omega); break;
     }
 }
 
@@ -178,13 +230,7 @@ void launch_jacobi_vertex(const VertexArgs& a, int mode, cudaStream_t s) {
 
 // Step prologue: f = (0, -g m, 0); s = x + h v + f / (M/h^2); base = (M/h^2) s;
 // b = base (pinned vertices: the pin RHS).
-__global__ void __launch_bounds__(256) k_begin(BeginArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
-        if (a.done) *a.done = 0;
-        if (a.iterations) *a.iterations = a.num_iterations;
-    }
-    if (i >= a.nv) return;
+__device__ __forceinline__ void begin_vertex(const BeginArgs& a, int i) {
     const float4 x = a.x[i], v = a.v[i], cf = __ldg(&a.coef[i]);
     const float dt2_m_1 = 1.0f / cf.x;
     const float fy = -a.gravity * cf.w;
@@ -215,6 +261,28 @@ __global__ void __launch_bounds__(256) k_begin(BeginArgs a) {
         }
         a.prev[i] = p;
     }
+}
+
+__global__ void __launch_bounds__(256) k_begin(BeginArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        if (a.done) *a.done = 0;
+        if (a.iterations) *a.iterations = a.num_iterations;
+    }
+    if (i < a.nv) begin_vertex(a, i);
+}
+
+__global__ void __launch_bounds__(256) k_begin_multi(const BeginArgs* __restrict__ req, const int2* __restrict__ list,
+                                                     const int* __restrict__ count) {
+    if ((int)blockIdx.x >= *count) return;
+    const int2 w = list[blockIdx.x];
+    const BeginArgs& a = req[w.x];
+    const int i = w.y + threadIdx.x;
+    if (i < a.nv) begin_vertex(a, i);
+}
+
+void launch_begin_multi(const BeginArgs* req, const int2* list, const int* count, int grid, cudaStream_t s) {
+    if (grid > 0) k_begin_multi<<<grid, 256, 0, s>>>(req, list, count);
 }
 
 void launch_begin(const BeginArgs& a, cudaStream_t s) {

@@ -1,0 +1,581 @@
+// Serving loop: continuous batching of PD simulation requests on one GPU.
+//
+// Requests (a soft body and a number of steps) are submitted at any time.
+// Host worker threads build each request's layout (the same Morton tiles and
+// coefficients as a single engine).  pdgb_server_tick then
+//   1. admits ready requests in arrival order while their device bytes fit
+//      the HBM budget (and the slot limit), giving each one block from a
+//      stream-ordered pool (cudaMallocAsync, no device-wide synchronisation);
+//   2. runs ONE PD step for every active request with one set of launches:
+//      prologue, num_iterations x (local step, Jacobi/Chebyshev vertex
+//      kernel), each covering the work lists of all active requests (tiles
+//      and 256-vertex chunks), captured once as a CUDA graph per capacity
+//      bucket and replayed every tick;
+//   3. retires the requests that reached their step count: state copied to
+//      host memory, block returned to the pool.
+// Requests join and leave between steps, their work shares every launch,
+// and a request's arithmetic is the single engine's (same kernels, own
+// arrays), so its result does not depend on the mix.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+#include "engine.h"
+
+using namespace pdgb;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+enum : int { kQueued = 0, kPreparing = 1, kReady = 2, kRunning = 3, kDone = 4, kFailed = 5 };
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct Request {
+    long long id = 0;
+    int state = kQueued;
+    int nsteps = 0, steps_done = 0;
+    int nv = 0, nt = 0;
+    std::vector<float> X, V, mass, mu, dbc;
+    std::vector<uint32_t> tets;
+    HostLayout L;
+    std::string error;
+    // device block and carved arrays
+    unsigned char* block = nullptr;
+    size_t bytes = 0;
+    LocalArgs la{};
+    VertexArgs va{};
+    BeginArgs ba{};
+    float* staging = nullptr;
+    int* vperm = nullptr;
+    std::vector<float> X_out, V_out;
+    Clock::time_point t_submit, t_admit, t_done;
+};
+
+template <class T> size_t bytes_of(const std::vector<T>& v) { return align256(v.size() * sizeof(T)); }
+
+// Device bytes of a prepared request (layout arrays + 8 float4 vectors +
+// staging for the state transfers).
+size_t request_bytes(const Request& r) {
+    const HostLayout& L = r.L;
+    size_t b = bytes_of(L.inc_ent) + bytes_of(L.inc_end) + bytes_of(L.geo) + bytes_of(L.tile_tet_ptr) +
+               bytes_of(L.tile_vptr) + bytes_of(L.tile_verts) + bytes_of(L.vperm) + bytes_of(L.coef) +
+               bytes_of(L.pin_rhs);
+    b += 6 * align256((size_t)r.nv * sizeof(float4));  // x, v, sn, prev, base, b
+    b += align256(6 * (size_t)r.nv * sizeof(float));   // staging
+    return b;
+}
+
+}  // namespace
+
+struct pdgb_server {
+    pdgb_server_config cfg{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaMemPool_t pool = nullptr;  // the server's own stream-ordered pool
+    std::mutex mu;
+    std::condition_variable cv;
+    std::vector<std::thread> workers;
+    bool stop = false;
+    long long next_id = 1;
+    std::unordered_map<long long, std::unique_ptr<Request>> reqs;
+    std::deque<long long> prep_queue, ready_queue;
+    std::vector<Request*> active;
+    size_t bytes_in_use = 0;
+    bool lists_dirty = true;
+    // work lists (device + pinned host mirrors)
+    int cap_req = 0, cap_tiles = 0, cap_chunks = 0;
+    LocalArgs* d_la = nullptr;
+    VertexArgs* d_va = nullptr;
+    BeginArgs* d_ba = nullptr;
+    int2 *d_tiles = nullptr, *d_chunks = nullptr;
+    int* d_counts = nullptr;  // {tiles, chunks}
+    LocalArgs* h_la = nullptr;
+    VertexArgs* h_va = nullptr;
+    BeginArgs* h_ba = nullptr;
+    int2 *h_tiles = nullptr, *h_chunks = nullptr;
+    int* h_counts = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    // stats
+    long long completed = 0, failed = 0;
+    double tet_iterations = 0.0;
+    std::vector<double> latencies_ms;
+    double busy_ms = 0.0;
+
+    ~pdgb_server() {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        for (auto& t : workers) t.join();
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto& kv : reqs)
+            if (kv.second->block) cudaFreeAsync(kv.second->block, stream);
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        cudaFree(d_la);
+        cudaFree(d_va);
+        cudaFree(d_ba);
+        cudaFree(d_tiles);
+        cudaFree(d_chunks);
+        cudaFree(d_counts);
+        cudaFreeHost(h_la);
+        cudaFreeHost(h_va);
+        cudaFreeHost(h_ba);
+        cudaFreeHost(h_tiles);
+        cudaFreeHost(h_chunks);
+        cudaFreeHost(h_counts);
+        if (stream) cudaStreamSynchronize(stream);
+        if (pool) cudaMemPoolDestroy(pool);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+template <class F> int guarded_s(F&& f) {
+    try {
+        f();
+        return PDGB_OK;
+    } catch (const Error& e) {
+        set_last_error(e.status, e.msg);
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        set_last_error(PDGB_ERR_OUT_OF_MEMORY, "host allocation failed");
+        return PDGB_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, e.what());
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+}
+
+void worker_loop(pdgb_server* S) {
+    for (;;) {
+        Request* r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv.wait(lk, [&] { return S->stop || !S->prep_queue.empty(); });
+            if (S->stop) return;
+            const long long id = S->prep_queue.front();
+            S->prep_queue.pop_front();
+            auto it = S->reqs.find(id);
+            if (it == S->reqs.end()) continue;
+            r = it->second.get();
+            r->state = kPreparing;
+        }
+        bool ok = true;
+        try {
+            build_layout(r->nv, r->nt, r->X.data(), r->tets.data(), r->mass.data(), r->mu.data(),
+                         r->dbc.empty() ? nullptr : r->dbc.data(), S->cfg.params, r->L);
+            r->bytes = request_bytes(*r);
+        } catch (const Error& e) {
+            ok = false;
+            r->error = e.msg;
+        } catch (const std::exception& e) {
+            ok = false;
+            r->error = e.what();
+        }
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (ok) {
+            r->state = kReady;
+            S->ready_queue.push_back(r->id);
+        } else {
+            r->state = kFailed;
+            S->failed++;
+        }
+    }
+}
+
+template <class T> T* carve(unsigned char*& p, size_t n) {
+    T* q = reinterpret_cast<T*>(p);
+    p += align256(n * sizeof(T));
+    return q;
+}
+
+template <class T> void put(cudaStream_t s, T* dst, const std::vector<T>& src) {
+    if (!src.empty()) PDGB_CUDA_TRY(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+// Uploads a prepared request into its device block.
+void admit(pdgb_server* S, Request* r) {
+    cudaStream_t s = S->stream;
+    PDGB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r->block), r->bytes, S->pool, s));
+    unsigned char* p = r->block;
+    const HostLayout& L = r->L;
+    const int nv = r->nv;
+    uint16_t* inc_ent = carve<uint16_t>(p, L.inc_ent.size());
+    uint16_t* inc_end = carve<uint16_t>(p, L.inc_end.size());
+    float* geo = carve<float>(p, L.geo.size());
+    int* ttp = carve<int>(p, L.tile_tet_ptr.size());
+    int* tvp = carve<int>(p, L.tile_vptr.size());
+    uint32_t* tv = carve<uint32_t>(p, L.tile_verts.size());
+    r->vperm = carve<int>(p, L.vperm.size());
+    float4* coef = carve<float4>(p, L.coef.size());
+    float4* pin = carve<float4>(p, L.pin_rhs.size());
+    float4* x = carve<float4>(p, nv);
+    float4* v = carve<float4>(p, nv);
+    float4* sn = carve<float4>(p, nv);
+    float4* prev = carve<float4>(p, nv);
+    float4* base = carve<float4>(p, nv);
+    float4* b = carve<float4>(p, nv);
+    r->staging = carve<float>(p, 6 * (size_t)nv);
+    put(s, inc_ent, L.inc_ent);
+    put(s, inc_end, L.inc_end);
+    put(s, geo, L.geo);
+    put(s, ttp, L.tile_tet_ptr);
+    put(s, tvp, L.tile_vptr);
+    put(s, tv, L.tile_verts);
+    put(s, r->vperm, L.vperm);
+    put(s, coef, L.coef);
+    put(s, pin, L.pin_rhs);
+    PDGB_CUDA_TRY(cudaMemcpyAsync(r->staging, r->X.data(), 3 * (size_t)nv * sizeof(float), cudaMemcpyHostToDevice, s));
+    const bool hasV = !r->V.empty();
+    if (hasV)
+        PDGB_CUDA_TRY(cudaMemcpyAsync(r->staging + 3 * (size_t)nv, r->V.data(), 3 * (size_t)nv * sizeof(float),
+                                      cudaMemcpyHostToDevice, s));
+    launch_gather_state(nv, r->vperm, r->staging, hasV ? r->staging + 3 * (size_t)nv : nullptr, x, v, s);
+    PDGB_CUDA_TRY(cudaGetLastError());
+    r->la = LocalArgs{sn, b, inc_ent, inc_end, geo, ttp, tvp, tv, L.nt_pad, nullptr};
+    r->va = VertexArgs{nv, sn, prev, b, base, coef, pin, x, v, 1.f, 1.0f / S->cfg.params.dt};
+    BeginArgs ba{};
+    ba.nv = nv;
+    ba.x = x;
+    ba.v = v;
+    ba.coef = coef;
+    ba.pin_rhs = pin;
+    ba.sn = sn;
+    ba.base = base;
+    ba.b = b;
+    ba.dt = S->cfg.params.dt;
+    ba.gravity = S->cfg.params.gravity;
+    ba.vperm = r->vperm;
+    ba.num_iterations = S->cfg.params.num_iterations;
+    r->ba = ba;
+    r->state = kRunning;
+    r->t_admit = Clock::now();
+    S->bytes_in_use += r->bytes;
+}
+
+void ensure_capacity(pdgb_server* S, int nreq, int ntiles, int nchunks) {
+    auto grow = [](int need, int cap) { return need <= cap ? cap : std::max(need, 2 * cap + 64); };
+    const int creq = grow(nreq, S->cap_req), ctile = grow(ntiles, S->cap_tiles), cchunk = grow(nchunks, S->cap_chunks);
+    if (creq == S->cap_req && ctile == S->cap_tiles && cchunk == S->cap_chunks && S->d_counts) return;
+    PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));
+    cudaFree(S->d_la);
+    cudaFree(S->d_va);
+    cudaFree(S->d_ba);
+    cudaFree(S->d_tiles);
+    cudaFree(S->d_chunks);
+    cudaFreeHost(S->h_la);
+    cudaFreeHost(S->h_va);
+    cudaFreeHost(S->h_ba);
+    cudaFreeHost(S->h_tiles);
+    cudaFreeHost(S->h_chunks);
+    PDGB_CUDA_TRY(cudaMalloc(&S->d_la, creq * sizeof(LocalArgs)));
+    PDGB_CUDA_TRY(cudaMalloc(&S->d_va, creq * sizeof(VertexArgs)));
+    PDGB_CUDA_TRY(cudaMalloc(&S->d_ba, creq * sizeof(BeginArgs)));
+    PDGB_CUDA_TRY(cudaMalloc(&S->d_tiles, ctile * sizeof(int2)));
+    PDGB_CUDA_TRY(cudaMalloc(&S->d_chunks, cchunk * sizeof(int2)));
+    PDGB_CUDA_TRY(cudaMallocHost(&S->h_la, creq * sizeof(LocalArgs)));
+    PDGB_CUDA_TRY(cudaMallocHost(&S->h_va, creq * sizeof(VertexArgs)));
+    PDGB_CUDA_TRY(cudaMallocHost(&S->h_ba, creq * sizeof(BeginArgs)));
+    PDGB_CUDA_TRY(cudaMallocHost(&S->h_tiles, ctile * sizeof(int2)));
+    PDGB_CUDA_TRY(cudaMallocHost(&S->h_chunks, cchunk * sizeof(int2)));
+    if (!S->d_counts) {
+        PDGB_CUDA_TRY(cudaMalloc(&S->d_counts, 2 * sizeof(int)));
+        PDGB_CUDA_TRY(cudaMallocHost(&S->h_counts, 2 * sizeof(int)));
+    }
+    S->cap_req = creq;
+    S->cap_tiles = ctile;
+    S->cap_chunks = cchunk;
+    // the step graph bakes the list pointers and grid sizes: re-capture
+    if (S->gexec) cudaGraphExecDestroy(S->gexec);
+    if (S->graph) cudaGraphDestroy(S->graph);
+    S->gexec = nullptr;
+    S->graph = nullptr;
+    cudaStream_t s = S->stream;
+    const int n = S->cfg.params.num_iterations;
+    const std::vector<float> omega = chebyshev_omegas(n, S->cfg.params.rho);
+    PDGB_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    launch_begin_multi(S->d_ba, S->d_chunks, S->d_counts + 1, S->cap_chunks, s);
+    for (int i = 0; i < n; ++i) {
+        launch_local_multi(S->d_la, S->d_tiles, S->d_counts, S->cap_tiles, s);
+        int mode = 0;
+        if (i >= 11) mode |= kReadPrev;
+        if (i >= 10 && i + 1 < n) mode |= kWritePrev;
+        if (i + 1 == n) mode |= kFinal;
+        launch_jacobi_vertex_multi(S->d_va, S->d_chunks, S->d_counts + 1, S->cap_chunks, mode, omega[i], s);
+    }
+    cudaError_t err = cudaStreamEndCapture(s, &S->graph);
+    if (err != cudaSuccess) throw Error{PDGB_ERR_CUDA, std::string("server graph capture: ") + cudaGetErrorString(err)};
+    PDGB_CUDA_TRY(cudaGraphInstantiate(&S->gexec, S->graph, 0));
+}
+
+void rebuild_lists(pdgb_server* S) {
+    int ntiles = 0, nchunks = 0;
+    for (Request* r : S->active) {
+        ntiles += r->L.ntiles;
+        nchunks += (r->nv + 255) / 256;
+    }
+    ensure_capacity(S, (int)S->active.size(), ntiles, nchunks);
+    PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));  // host mirrors may still be in flight
+    int t = 0, c = 0;
+    for (int q = 0; q < (int)S->active.size(); ++q) {
+        Request* r = S->active[q];
+        S->h_la[q] = r->la;
+        S->h_va[q] = r->va;
+        S->h_ba[q] = r->ba;
+        for (int k = 0; k < r->L.ntiles; ++k) S->h_tiles[t++] = make_int2(q, k);
+        for (int v0 = 0; v0 < r->nv; v0 += 256) S->h_chunks[c++] = make_int2(q, v0);
+    }
+    S->h_counts[0] = t;
+    S->h_counts[1] = c;
+    const size_t nq = S->active.size();
+    cudaStream_t s = S->stream;
+    if (nq) {
+        PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_la, S->h_la, nq * sizeof(LocalArgs), cudaMemcpyHostToDevice, s));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_va, S->h_va, nq * sizeof(VertexArgs), cudaMemcpyHostToDevice, s));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_ba, S->h_ba, nq * sizeof(BeginArgs), cudaMemcpyHostToDevice, s));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_tiles, S->h_tiles, t * sizeof(int2), cudaMemcpyHostToDevice, s));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_chunks, S->h_chunks, c * sizeof(int2), cudaMemcpyHostToDevice, s));
+    }
+    PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_counts, S->h_counts, 2 * sizeof(int), cudaMemcpyHostToDevice, s));
+    S->lists_dirty = false;
+}
+
+}  // namespace
+
+extern "C" {
+
+void pdgb_server_default_config(pdgb_server_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    pdgb_default_params(&c->params);
+    c->params.solver = PDGB_SOLVER_JACOBI;
+    c->hbm_budget_bytes = (size_t)8 << 30;
+    c->max_active = 0;
+    c->host_threads = 0;
+}
+
+int pdgb_server_create(const pdgb_server_config* cfg, void* stream, pdgb_server** out) {
+    if (!cfg || !out) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "null config or out");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    *out = nullptr;
+    pdgb_server* S = nullptr;
+    const int st = guarded_s([&] {
+        if (cfg->params.solver != PDGB_SOLVER_JACOBI)
+            throw Error{PDGB_ERR_UNSUPPORTED, "the server runs the Jacobi + Chebyshev global solve"};
+        if (!(cfg->params.dt > 0.f) || cfg->params.num_iterations < 1 || cfg->params.num_iterations > 4096)
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "bad solver parameters"};
+        if (cfg->hbm_budget_bytes == 0) throw Error{PDGB_ERR_INVALID_ARGUMENT, "zero HBM budget"};
+        S = new pdgb_server();
+        S->cfg = *cfg;
+        if (stream) S->stream = (cudaStream_t)stream;
+        else {
+            PDGB_CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+            S->own_stream = true;
+        }
+        int dev = 0;
+        PDGB_CUDA_TRY(cudaGetDevice(&dev));
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        PDGB_CUDA_TRY(cudaMemPoolCreate(&S->pool, &props));
+        uint64_t keep = UINT64_MAX;  // keep freed blocks for the next admissions
+        PDGB_CUDA_TRY(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        int nthr = cfg->host_threads > 0 ? cfg->host_threads : (int)std::max(1u, std::thread::hardware_concurrency() / 2);
+        for (int i = 0; i < nthr; ++i) S->workers.emplace_back(worker_loop, S);
+    });
+    if (st != PDGB_OK) {
+        delete S;
+        return st;
+    }
+    *out = S;
+    return PDGB_OK;
+}
+
+int pdgb_server_submit(pdgb_server* S, const pdgb_mesh_desc* mesh, int nsteps, long long* request_id) {
+    if (!S || !mesh || !request_id || nsteps < 1 || mesh->memory != PDGB_MEM_HOST || !mesh->X || !mesh->tets ||
+        !mesh->mass || !mesh->mu || mesh->num_verts <= 0 || mesh->num_tets <= 0) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad request (host mesh, nsteps >= 1 required)");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded_s([&] {
+        auto r = std::make_unique<Request>();
+        r->nsteps = nsteps;
+        r->nv = mesh->num_verts;
+        r->nt = mesh->num_tets;
+        r->X.assign(mesh->X, mesh->X + 3 * (size_t)r->nv);
+        if (mesh->V) r->V.assign(mesh->V, mesh->V + 3 * (size_t)r->nv);
+        r->tets.assign(mesh->tets, mesh->tets + 4 * (size_t)r->nt);
+        r->mass.assign(mesh->mass, mesh->mass + r->nv);
+        r->mu.assign(mesh->mu, mesh->mu + r->nt);
+        if (mesh->dbc) r->dbc.assign(mesh->dbc, mesh->dbc + r->nv);
+        r->t_submit = Clock::now();
+        std::lock_guard<std::mutex> lk(S->mu);
+        r->id = S->next_id++;
+        *request_id = r->id;
+        S->prep_queue.push_back(r->id);
+        S->reqs.emplace(r->id, std::move(r));
+        S->cv.notify_one();
+    });
+}
+
+int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
+    if (!S) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded_s([&] {
+        std::lock_guard<std::mutex> lk(S->mu);
+        const auto t0 = Clock::now();
+        // 1. admission in arrival order, by HBM budget and slot limit
+        while (!S->ready_queue.empty()) {
+            if (S->cfg.max_active > 0 && (int)S->active.size() >= S->cfg.max_active) break;
+            auto it = S->reqs.find(S->ready_queue.front());
+            if (it == S->reqs.end()) {
+                S->ready_queue.pop_front();
+                continue;
+            }
+            Request* r = it->second.get();
+            if (S->bytes_in_use + r->bytes > S->cfg.hbm_budget_bytes) {
+                if (S->active.empty() && r->bytes > S->cfg.hbm_budget_bytes) {  // can never fit
+                    r->state = kFailed;
+                    r->error = "request larger than the HBM budget";
+                    S->failed++;
+                    S->ready_queue.pop_front();
+                    continue;
+                }
+                break;
+            }
+            S->ready_queue.pop_front();
+            admit(S, r);
+            S->active.push_back(r);
+            S->lists_dirty = true;
+        }
+        int done_now = 0;
+        if (!S->active.empty()) {
+            if (S->lists_dirty) rebuild_lists(S);
+            // 2. one PD step for every active request
+            PDGB_CUDA_TRY(cudaGraphLaunch(S->gexec, S->stream));
+            // 3. retire finished requests
+            std::vector<Request*> keep;
+            for (Request* r : S->active) {
+                r->steps_done++;
+                S->tet_iterations += (double)r->nt * S->cfg.params.num_iterations;
+                if (r->steps_done >= r->nsteps) {
+                    const size_t n3 = 3 * (size_t)r->nv;
+                    r->X_out.resize(n3);
+                    r->V_out.resize(n3);
+                    launch_scatter_state(r->nv, r->vperm, r->va.x, r->va.v, r->staging, r->staging + n3, S->stream);
+                    PDGB_CUDA_TRY(cudaMemcpyAsync(r->X_out.data(), r->staging, n3 * sizeof(float),
+                                                  cudaMemcpyDeviceToHost, S->stream));
+                    PDGB_CUDA_TRY(cudaMemcpyAsync(r->V_out.data(), r->staging + n3, n3 * sizeof(float),
+                                                  cudaMemcpyDeviceToHost, S->stream));
+                    PDGB_CUDA_TRY(cudaFreeAsync(r->block, S->stream));
+                    r->block = nullptr;
+                    S->bytes_in_use -= r->bytes;
+                    r->state = kDone;
+                    S->lists_dirty = true;
+                    done_now++;
+                } else {
+                    keep.push_back(r);
+                }
+            }
+            S->active.swap(keep);
+            PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));
+            const auto now = Clock::now();
+            for (auto& kv : S->reqs) {
+                Request* r = kv.second.get();
+                if (r->state == kDone && r->t_done == Clock::time_point{}) {
+                    r->t_done = now;
+                    S->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
+                    S->completed++;
+                }
+            }
+            PDGB_CUDA_TRY(cudaGetLastError());
+        }
+        S->busy_ms += std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+        if (active) *active = (int)S->active.size();
+        if (completed) *completed = done_now;
+    });
+}
+
+int pdgb_server_poll(pdgb_server* S, long long id, int* state, int* steps_done) {
+    if (!S || !state) return PDGB_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end()) {
+        set_last_error(PDGB_ERR_NOT_FOUND, "unknown request id");
+        return PDGB_ERR_NOT_FOUND;
+    }
+    *state = it->second->state;
+    if (steps_done) *steps_done = it->second->steps_done;
+    return PDGB_OK;
+}
+
+int pdgb_server_result(pdgb_server* S, long long id, float* X, float* V) {
+    if (!S || (!X && !V)) return PDGB_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end()) {
+        set_last_error(PDGB_ERR_NOT_FOUND, "unknown request id");
+        return PDGB_ERR_NOT_FOUND;
+    }
+    Request* r = it->second.get();
+    if (r->state == kFailed) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "request failed: " + r->error);
+        const int st = PDGB_ERR_INVALID_ARGUMENT;
+        S->reqs.erase(it);
+        return st;
+    }
+    if (r->state != kDone) {
+        set_last_error(PDGB_ERR_BUSY, "request not finished");
+        return PDGB_ERR_BUSY;
+    }
+    if (X) std::memcpy(X, r->X_out.data(), r->X_out.size() * sizeof(float));
+    if (V) std::memcpy(V, r->V_out.data(), r->V_out.size() * sizeof(float));
+    S->reqs.erase(it);
+    return PDGB_OK;
+}
+
+int pdgb_server_get_stats(pdgb_server* S, pdgb_server_stats* out) {
+    if (!S || !out) return PDGB_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(S->mu);
+    std::memset(out, 0, sizeof(*out));
+    out->completed = S->completed;
+    out->failed = S->failed;
+    out->active = (int)S->active.size();
+    out->waiting = (int)(S->prep_queue.size() + S->ready_queue.size());
+    out->bytes_in_use = S->bytes_in_use;
+    out->tet_iterations = S->tet_iterations;
+    out->busy_ms = S->busy_ms;
+    return PDGB_OK;
+}
+
+int pdgb_server_latencies(pdgb_server* S, double* out_ms, int capacity, int* count) {
+    if (!S || !count) return PDGB_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(S->mu);
+    *count = (int)S->latencies_ms.size();
+    if (out_ms)
+        for (int i = 0; i < std::min(capacity, *count); ++i) out_ms[i] = S->latencies_ms[i];
+    return PDGB_OK;
+}
+
+int pdgb_server_destroy(pdgb_server* S) {
+    if (!S) return PDGB_ERR_INVALID_ARGUMENT;
+    delete S;
+    return PDGB_OK;
+}
+
+}  // extern "C"

@@ -7,5 +7,6 @@ provides the synthetic soft bodies used by tests and benchmarks.
 from . import mesh
 from ._native import PdgbError, library_path
 from .engine import PdSolver, SolverParams, SolverType
+from .server import PdServer
 
-__all__ = ["mesh", "PdSolver", "SolverParams", "SolverType", "PdgbError", "library_path"]
+__all__ = ["mesh", "PdSolver", "PdServer", "SolverParams", "SolverType", "PdgbError", "library_path"]

@@ -91,6 +91,30 @@ class pdgb_noalloc_mesh(C.Structure):
     ]
 
 
+class pdgb_server_config(C.Structure):
+    _fields_ = [
+        ("params", pdgb_params),
+        ("hbm_budget_bytes", C.c_size_t),
+        ("max_active", C.c_int),
+        ("host_threads", C.c_int),
+    ]
+
+
+class pdgb_server_stats(C.Structure):
+    _fields_ = [
+        ("completed", C.c_longlong),
+        ("failed", C.c_longlong),
+        ("active", C.c_int),
+        ("waiting", C.c_int),
+        ("bytes_in_use", C.c_size_t),
+        ("tet_iterations", C.c_double),
+        ("busy_ms", C.c_double),
+    ]
+
+
+PDGB_REQ_QUEUED, PDGB_REQ_PREPARING, PDGB_REQ_READY, PDGB_REQ_RUNNING, PDGB_REQ_DONE, PDGB_REQ_FAILED = range(6)
+
+
 class pdgb_factor_info(C.Structure):
     _fields_ = [
         ("nnz_L", C.c_longlong),
@@ -147,6 +171,15 @@ SIGNATURES = {
                                          C.c_void_p, C.POINTER(pdgb_factor_info)]),
     "pdgb_step_noalloc": (C.c_int, [C.POINTER(pdgb_noalloc_mesh), C.POINTER(pdgb_params), C.c_void_p, C.c_void_p,
                                     C.c_int, C.c_void_p]),
+    "pdgb_server_default_config": (None, [C.POINTER(pdgb_server_config)]),
+    "pdgb_server_create": (C.c_int, [C.POINTER(pdgb_server_config), C.c_void_p, C.POINTER(C.c_void_p)]),
+    "pdgb_server_submit": (C.c_int, [C.c_void_p, C.POINTER(pdgb_mesh_desc), C.c_int, C.POINTER(C.c_longlong)]),
+    "pdgb_server_tick": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "pdgb_server_poll": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "pdgb_server_result": (C.c_int, [C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]),
+    "pdgb_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(pdgb_server_stats)]),
+    "pdgb_server_latencies": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "pdgb_server_destroy": (C.c_int, [C.c_void_p]),
     "pdgb_inspect_layout": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_layout_info), C.c_void_p,
                                       C.c_void_p]),
 }

@@ -166,6 +166,24 @@ def batch_c4(nbodies: int = 512, seed: int = 4, lo: int = 4, hi: int = 24, cell:
     return bodies
 
 
+def request_body(target_tets: float, rng, cell: float = 1.0 / 16.0) -> SoftBody:
+    """A near-cubic hex-grid body with about target_tets tets (5 nx ny nz),
+    material drawn as in the batch workload."""
+    n = max(1.0, (target_tets / 5.0) ** (1.0 / 3.0))
+    base = int(n)
+    dims = [base, base, base]
+    k = 0
+    while 5 * dims[0] * dims[1] * dims[2] < target_tets and k < 3:
+        dims[k] += 1
+        k += 1
+    nx, ny, nz = (max(1, d) for d in dims)
+    E = float(np.exp(rng.uniform(math.log(1e4), math.log(1e7))))
+    nu = float(rng.uniform(0.3, 0.45))
+    rho = float(rng.uniform(800.0, 1200.0))
+    return make_grid_body(nx, ny, nz, size=(nx * cell, ny * cell, nz * cell), young=E, poisson=nu, density=rho,
+                          seed=int(rng.integers(1 << 30)))
+
+
 def concat(bodies: list) -> SoftBody:
     """One disconnected system holding all bodies (vertex ids offset per body):
     the reference's multi-body layout (dataLoader.cu:291-378)."""
