@@ -281,6 +281,63 @@ int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params
                            double* x, pdgb_factor_info* info);
 
 /* ---------------------------------------------------------------------
+ * Interactive drag (soft positional constraints).  The reference keeps a
+ * per-vertex weight moreDBC, an offset OffsetX and one mouse target in
+ * SolverData (def.h:16-18, 30-33) and applies them inside
+ * PdSolver::SolverStep (pdUtil.cu:56-95, 147-166, 180-205): a dragged vertex
+ * (weight w > 0) starts each step at target + offset, its mass term becomes
+ * (m + w)/h^2, it keeps that position through the Jacobi iterations, its
+ * RHS row becomes (target + offset) * w when the system has pinned vertices
+ * (the reference runs that overwrite only then), and its velocity is set to
+ * 0 at the end of the step.  The system matrix is not refactored.
+ *
+ * pdgb_set_drag: weights (float[nv]) and offsets (float[3 nv], nullable:
+ * keep the current ones), caller vertex order.  A weight > 0 on a pinned
+ * vertex is rejected (PDGB_ERR_INVALID_ARGUMENT): the reference's selection
+ * never sets one.
+ * pdgb_drag_select: the reference's selection (Control_Kernel,
+ * simulationContext.cu:201-231) on the current positions: every free vertex
+ * gets offset X_i - X_select, and weight control_mag if |offset|^2 <
+ * radius_sq (the reference uses 10 and 0.002); select_v = -1 clears the
+ * weights.  select_v is a caller vertex index.
+ * pdgb_set_drag_target: the mouse target (mouseSelection.target).
+ * pdgb_clear_drag: all weights 0 and the drag terms leave the step graph
+ * (ResetMoreDBC(true), simulationContext.cu:220-226; pdgb_reset does it
+ * too). */
+int pdgb_set_drag(pdgb_engine* e, const float* weights, const float* offsets, int memory);
+int pdgb_drag_select(pdgb_engine* e, int select_v, float control_mag, double radius_sq);
+int pdgb_set_drag_target(pdgb_engine* e, const float target[3]);
+int pdgb_clear_drag(pdgb_engine* e);
+
+/* ---------------------------------------------------------------------
+ * Fixed rigid bodies (FixedBodyData, fixedBodyData.cu:8-148).  After every
+ * step the engine projects XTilde out of each body and resolves the
+ * velocity with friction muT and restitution muN, spheres first, then
+ * planes, then cylinders, as FixedBodyData::HandleCollisions does, fused
+ * into the step's last kernel.  As in PdSolver::Update (pdSolver.cu:
+ * 218-232) X is copied from XTilde before the correction: X (what
+ * pdgb_download_state returns) holds the uncorrected positions and the next
+ * step starts from it, while the velocity update uses XTilde.
+ *
+ * A body is given as the reference's FixedBody fields: model is m_model
+ * (glm::mat4, column-major, 16 floats), radius is m_radius (sphere,
+ * cylinder), up is Plane::m_floorUp (plane only).  The cylinder axis is the
+ * normalised second column of model.  n = 0 removes all bodies.  The
+ * bodies and muT / muN apply from the next step. */
+#define PDGB_FIXED_SPHERE 0
+#define PDGB_FIXED_PLANE 1
+#define PDGB_FIXED_CYLINDER 2
+typedef struct pdgb_fixed_body {
+    int type;         /* PDGB_FIXED_*                                      */
+    float model[16];  /* column-major 4x4 model matrix                     */
+    float radius;
+    float up[3];
+} pdgb_fixed_body;
+int pdgb_set_fixed_bodies(pdgb_engine* e, const pdgb_fixed_body* bodies, int n, float mu_t, float mu_n);
+/* SolverData::XTilde after the last step (equals X without fixed bodies). */
+int pdgb_download_xtilde(pdgb_engine* e, float* XT, int memory);
+
+/* ---------------------------------------------------------------------
  * Allocation-free PD steps.  No counterpart in the reference: it exists for
  * callers that must not allocate device memory when they advance a body -- a
  * host application whose own allocator owns the GPU's memory, a frame loop

@@ -3,7 +3,8 @@
 # (src/simulation/solver/projective/pdUtil.cu, with the templates of
 # solverUtil.cuh and the vendored svd3_cuda/glm headers) compiled as C++
 # through refshim/shim.h, plus refshim/ref_harness.cpp which drives them in
-# the order PdSolver does.  Test infrastructure only; reads the reference
+# the order PdSolver does, and the scene unit (fixed rigid bodies and the
+# drag selection, see below).  Test infrastructure only; reads the reference
 # sources where they lie and writes nothing outside oracle/_ref/.
 #
 # usage: build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
@@ -19,5 +20,38 @@ INC=(-I"$HERE/refshim/include" -I"$R/src" -I"$R/src/simulation" -I"$R/src/simula
     -c "$R/src/simulation/solver/projective/pdUtil.cu" -o "$OUT/pdUtil.o"
 "${CXX[@]}" -include "$HERE/refshim/shim.h" "${INC[@]}" -c "$HERE/refshim/ref_harness.cpp" -o "$OUT/ref_harness.o"
 "${CXX[@]}" -fopenmp -c "$HERE/pd_oracle.cpp" -o "$OUT/pd_oracle.o"
-g++ -shared -fopenmp -o "$OUT/libref_pd.so.tmp" "$OUT/pdUtil.o" "$OUT/ref_harness.o" "$OUT/pd_oracle.o"
+
+# Scene unit: the reference's fixed-body kernels (fixedBodyData.cu), the
+# constructors and getType of Plane / Sphere / Cylinder (collision/rigid/),
+# FixedBody's constructors (rigid.cpp, compiled whole), the drag selection
+# kernel Control_Kernel with its radius (simulationContext.cu) and
+# utilityCore::modelMatrix (utilities.cpp).  Only the lines that hold them
+# are read from those files and piped to the compiler -- the rest of each
+# file launches kernels or draws with OpenGL -- so nothing is copied to disk.
+RR="$R/src/collision/rigid"
+SINC=("${INC[@]}" -I"$R/src/collision/rigid" -I"$HERE/refshim")
+kernel_text() {  # kernel_text FILE NAME TEMPLATE-HEAD: one __global__ function, head line included
+    awk -v name="$2" -v head="$3" '
+        $0 ~ ("__global__ void " name "[ (]") { p = 1; print head }
+        p { print }
+        p && /^}/ { p = 0 }' "$1"
+}
+{
+    echo '#include "fixed_prelude.h"'
+    for k in Plane Sphere Cylinder; do
+        f="$RR/$(echo "$k" | tr 'A-Z' 'a-z').cpp"
+        sed -n "/^$k::$k(const glm::mat4/,/^{}/p" "$f"
+        sed -n "/^BodyType $k::getType/,/^}/p" "$f"
+    done
+    for k in handleFloorCollision handleSphereCollision handleCylinderCollision; do
+        kernel_text "$R/src/simulation/fixedBodyData.cu" "$k" 'template<typename Scalar>'
+    done
+    sed -n '/^#define RADIUS_SQUARED/p' "$R/src/simulation/simulationContext.cu"
+    kernel_text "$R/src/simulation/simulationContext.cu" Control_Kernel 'template<class Scalar>'
+    sed -n '/^glm::mat4 utilityCore::modelMatrix/,/^}/p' "$R/src/utilities.cpp"
+    echo '#include "fixed_harness.inc"'
+} | "${CXX[@]}" -x c++ -include "$HERE/refshim/shim.h" "${SINC[@]}" -c - -o "$OUT/ref_scene.o"
+"${CXX[@]}" -include "$HERE/refshim/shim.h" "${SINC[@]}" -c "$RR/rigid.cpp" -o "$OUT/rigid.o"
+g++ -shared -fopenmp -o "$OUT/libref_pd.so.tmp" "$OUT/pdUtil.o" "$OUT/ref_harness.o" "$OUT/pd_oracle.o" \
+    "$OUT/ref_scene.o" "$OUT/rigid.o"
 mv "$OUT/libref_pd.so.tmp" "$OUT/libref_pd.so"

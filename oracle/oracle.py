@@ -23,6 +23,20 @@ class orc_params(C.Structure):
                 ("rho", C.c_float), ("positional_weight", C.c_float), ("solver", C.c_int), ("reserved", C.c_int)]
 
 
+class orc_fixed_body(C.Structure):
+    _fields_ = [("type", C.c_int), ("model", C.c_float * 16), ("radius", C.c_float), ("up", C.c_float * 3)]
+
+
+class orc_scene(C.Structure):
+    _fields_ = [("drag_w", C.c_void_p), ("drag_off", C.c_void_p), ("target", C.c_float * 3), ("nfixed", C.c_int),
+                ("fixed", C.POINTER(orc_fixed_body)), ("mu_t", C.c_float), ("mu_n", C.c_float),
+                ("XT", C.c_void_p)]
+
+
+class RefFixedSpec(C.Structure):
+    _fields_ = [("type", C.c_int), ("pos", C.c_float * 3), ("rot", C.c_float * 3), ("scale", C.c_float * 3)]
+
+
 _orc = None
 _ref = None
 
@@ -42,6 +56,10 @@ def _load_oracle():
         h.orc_simulate.restype = C.c_int
         h.orc_simulate.argtypes = [C.c_int, C.c_int, _F32, _F32, _F32, _U32, _F32, _F32, C.c_void_p,
                                    C.POINTER(orc_params), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        h.orc_simulate_scene.restype = C.c_int
+        h.orc_simulate_scene.argtypes = [C.c_int, C.c_int, _F32, _F32, _F32, _U32, _F32, _F32, C.c_void_p,
+                                         C.POINTER(orc_params), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                         C.POINTER(orc_scene)]
         h.orc_rotations.restype = None
         h.orc_rotations.argtypes = [C.c_int, _F64, _F64, C.c_int]
         h.orc_local_rhs.restype = C.c_int
@@ -70,6 +88,13 @@ def _load_ref():
         h.ref_simulate.restype = C.c_int
         h.ref_simulate.argtypes = [C.c_int, C.c_int, _F32, _F32, _F32, _U32, _F32, _F32, C.c_void_p, C.c_float,
                                    C.c_float, C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, C.c_void_p]
+        h.ref_simulate_scene.restype = C.c_int
+        h.ref_simulate_scene.argtypes = [C.c_int, C.c_int, _F32, _F32, _F32, _U32, _F32, _F32, C.c_void_p,
+                                         C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_int, C.c_int,
+                                         C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                         C.POINTER(RefFixedSpec), C.c_float, C.c_float, C.c_void_p]
+        h.ref_fixed_frame.restype = None
+        h.ref_fixed_frame.argtypes = [C.c_int, _F32, _F32, _F32, _F32, _F32]
         h.ref_rotation.restype = None
         h.ref_rotation.argtypes = [_F32, _F32]
         _ref = h
@@ -120,6 +145,111 @@ def reference_simulate(body, params, nsteps: int, X=None, V=None):
     if st != 0:
         raise RuntimeError(f"ref_simulate failed ({st})")
     return Xs.reshape(-1, 3), Vs.reshape(-1, 3), iters[:nsteps]
+
+
+def _params(params):
+    return orc_params(params.dt, params.gravity, params.num_iterations, params.tol, params.rho,
+                      params.positional_weight, int(params.solver), 0)
+
+
+def simulate_scene(body, params, nsteps: int, precision: int = 64, drag_w=None, drag_off=None,
+                   target=(0.0, 0.0, 0.0), fixed=(), mu_t: float = 0.5, mu_n: float = 0.5, X=None, V=None, XT=None,
+                   nthreads: int = 0):
+    """Oracle run with drag and fixed rigid bodies; returns (X, V, XTilde,
+    iterations per step).  fixed: objects with type, model (4x4, glm
+    column-major), radius and up."""
+    h = _load_oracle()
+    X0, tets, mass, mu, dbc = _arr(body)
+    Xs = np.array(X0 if X is None else np.asarray(X, np.float32).reshape(-1), dtype=np.float32)
+    Vs = np.zeros_like(Xs) if V is None else np.array(np.asarray(V, np.float32).reshape(-1), dtype=np.float32)
+    XTs = np.array(Xs if XT is None else np.asarray(XT, np.float32).reshape(-1), dtype=np.float32)
+    sc = orc_scene()
+    keep = []
+    if drag_w is not None:
+        w = np.ascontiguousarray(drag_w, dtype=np.float32).reshape(-1)
+        o = np.ascontiguousarray(drag_off, dtype=np.float32).reshape(-1)
+        keep += [w, o]
+        sc.drag_w, sc.drag_off = w.ctypes.data, o.ctypes.data
+    for d in range(3):
+        sc.target[d] = float(target[d])
+    fb = (orc_fixed_body * max(1, len(fixed)))()
+    for j, f in enumerate(fixed):
+        fb[j].type = int(f.type)
+        m = np.ascontiguousarray(f.model, dtype=np.float32).reshape(16)
+        for k in range(16):
+            fb[j].model[k] = float(m[k])
+        fb[j].radius = float(f.radius)
+        for k in range(3):
+            fb[j].up[k] = float(f.up[k])
+    sc.nfixed, sc.fixed = len(fixed), fb
+    sc.mu_t, sc.mu_n = mu_t, mu_n
+    sc.XT = XTs.ctypes.data
+    iters = np.zeros(max(nsteps, 1), dtype=np.int32)
+    p = _params(params)
+    st = h.orc_simulate_scene(len(mass), len(mu), X0, Xs, Vs, tets, mass, mu,
+                              None if dbc is None else dbc.ctypes.data, C.byref(p), precision, nsteps, nthreads,
+                              iters.ctypes.data, None, C.byref(sc))
+    if st != 0:
+        raise RuntimeError(f"orc_simulate_scene failed ({st})")
+    return Xs.reshape(-1, 3), Vs.reshape(-1, 3), XTs.reshape(-1, 3), iters[:nsteps]
+
+
+def drag_select(X, dbc, select_v: int, control_mag: float = 10.0, radius_sq: float = 0.002, offsets=None):
+    """The reference's drag selection (Control_Kernel, simulationContext.cu:
+    201-218) in float32: every free vertex gets its offset from the grabbed
+    vertex, and the weight control_mag when the squared distance is below
+    radius_sq (compared in double, as the macro is a double literal).
+    Returns (weights, offsets); pinned vertices keep `offsets`' rows."""
+    X = np.asarray(X, np.float32).reshape(-1, 3)
+    nv = X.shape[0]
+    off = np.zeros((nv, 3), np.float32) if offsets is None else np.array(offsets, np.float32).reshape(nv, 3)
+    w = np.zeros(nv, np.float32)
+    if select_v < 0:
+        return w, off
+    free = np.ones(nv, bool) if dbc is None else (np.asarray(dbc) == 0)
+    d = (X - X[select_v]).astype(np.float32)
+    off[free] = d[free]
+    dist2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]).astype(np.float32) + d[:, 2] * d[:, 2]
+    w[free & (dist2.astype(np.float64) < radius_sq)] = np.float32(control_mag)
+    return w, off
+
+
+def reference_simulate_scene(body, params, nsteps: int, select_v: int = -1, reselect: bool = False, target=None,
+                             fixed_specs=(), mu_t: float = 0.5, mu_n: float = 0.5, X=None, V=None):
+    """The reference's own PD, drag and fixed-body kernels on the CPU
+    (oracle/_ref).  fixed_specs: (type, pos, rot_deg, scale) as a scene file
+    gives them (sphere radius = scale[0]).  Returns (X, V, XTilde, iters)."""
+    h = _load_ref()
+    X0, tets, mass, mu, dbc = _arr(body)
+    Xs = np.array(X0 if X is None else np.asarray(X, np.float32).reshape(-1), dtype=np.float32)
+    Vs = np.zeros_like(Xs) if V is None else np.array(np.asarray(V, np.float32).reshape(-1), dtype=np.float32)
+    XTs = np.zeros_like(Xs)
+    specs = (RefFixedSpec * max(1, len(fixed_specs)))()
+    for j, (t, pos, rot, scale) in enumerate(fixed_specs):
+        specs[j].type = int(t)
+        for k in range(3):
+            specs[j].pos[k], specs[j].rot[k], specs[j].scale[k] = float(pos[k]), float(rot[k]), float(scale[k])
+    tgt = None if target is None else np.ascontiguousarray(target, dtype=np.float32)
+    iters = np.zeros(max(nsteps, 1), dtype=np.int32)
+    st = h.ref_simulate_scene(len(mass), len(mu), X0, Xs, Vs, tets, mass, mu,
+                              None if dbc is None else dbc.ctypes.data, params.dt, params.gravity,
+                              params.num_iterations, params.tol, params.rho, int(params.solver), nsteps,
+                              iters.ctypes.data, int(select_v), int(bool(reselect)),
+                              None if tgt is None else tgt.ctypes.data, len(fixed_specs), specs, mu_t, mu_n,
+                              XTs.ctypes.data)
+    if st != 0:
+        raise RuntimeError(f"ref_simulate_scene failed ({st})")
+    return Xs.reshape(-1, 3), Vs.reshape(-1, 3), XTs.reshape(-1, 3), iters[:nsteps]
+
+
+def reference_fixed_frame(type_: int, pos, rot, scale):
+    """The reference's model matrix (4x4, model[c][r]) and plane normal of one body."""
+    h = _load_ref()
+    model = np.zeros(16, np.float32)
+    up = np.zeros(3, np.float32)
+    h.ref_fixed_frame(int(type_), np.asarray(pos, np.float32), np.asarray(rot, np.float32),
+                      np.asarray(scale, np.float32), model, up)
+    return model.reshape(4, 4), up
 
 
 def rotations(F: np.ndarray, precision: int = 64) -> np.ndarray:

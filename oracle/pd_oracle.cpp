@@ -487,7 +487,7 @@ template <class T> struct Sim {
 };
 
 template <class T>
-void local_rhs(Sim<T>& S, const T* q, const T* s_old, bool jacobi_form, T* b) {
+void local_rhs(Sim<T>& S, const T* q, const T* s_old, bool jacobi_form, T* b, const T* mdt2) {
     const int nt = S.nt;
 #pragma omp parallel for schedule(static)
     for (int t = 0; t < nt; ++t) {
@@ -522,7 +522,7 @@ void local_rhs(Sim<T>& S, const T* q, const T* s_old, bool jacobi_form, T* b) {
     }
 #pragma omp parallel for schedule(static)
     for (int v = 0; v < S.nv; ++v) {
-        T acc[3] = {S.mdt2[v] * s_old[3 * v], S.mdt2[v] * s_old[3 * v + 1], S.mdt2[v] * s_old[3 * v + 2]};
+        T acc[3] = {mdt2[v] * s_old[3 * v], mdt2[v] * s_old[3 * v + 1], mdt2[v] * s_old[3 * v + 2]};
         for (int e = S.inc.ptr[v]; e < S.inc.ptr[v + 1]; ++e) {
             int ent = S.inc.ent[e];
             const T* o = &S.P[12 * (size_t)(ent >> 2) + 3 * (ent & 3)];
@@ -532,9 +532,81 @@ void local_rhs(Sim<T>& S, const T* q, const T* s_old, bool jacobi_form, T* b) {
     }
 }
 
+// ---- fixed rigid bodies (fixedBodyData.cu:66-148)
+template <class T> struct Fixed {
+    int type;
+    T p[3], n[3], r;
+};
+
+template <class T> std::vector<Fixed<T>> fixed_bodies(const orc_scene* sc) {
+    std::vector<Fixed<T>> out;
+    if (!sc) return out;
+    for (int kind = 0; kind < 3; ++kind)  // HandleCollisions: spheres, planes, cylinders
+        for (int j = 0; j < sc->nfixed; ++j) {
+            const orc_fixed_body& fb = sc->fixed[j];
+            if (fb.type != kind) continue;
+            Fixed<T> f{};
+            f.type = kind;
+            for (int d = 0; d < 3; ++d) f.p[d] = (T)fb.model[12 + d];
+            f.r = (T)fb.radius;
+            if (kind == 1) {
+                for (int d = 0; d < 3; ++d) f.n[d] = (T)fb.up[d];
+            } else if (kind == 2) {  // axis = normalize(vec3(model * (0,1,0,0)))
+                T a[3] = {(T)fb.model[4], (T)fb.model[5], (T)fb.model[6]};
+                T inv = (T)1 / std::sqrt(dot3(a, a));
+                for (int d = 0; d < 3; ++d) f.n[d] = a[d] * inv;
+            }
+            out.push_back(f);
+        }
+    return out;
+}
+
+template <class T> void contact_response(const T* nrm, T mu_t, T mu_n, T* V) {
+    T vn = dot3(V, nrm);
+    T vN[3], vT[3];
+    for (int d = 0; d < 3; ++d) {
+        vN[d] = vn * nrm[d];
+        vT[d] = V[d] - vN[d];
+    }
+    T mag_vT = std::sqrt(dot3(vT, vT));
+    T a = mag_vT == (T)0 ? (T)0 : std::max((T)1 - mu_t * ((T)1 + mu_n) * std::sqrt(dot3(vN, vN)) / mag_vT, (T)0);
+    for (int d = 0; d < 3; ++d) V[d] = -mu_n * vN[d] + a * vT[d];
+}
+
+template <class T> void collide(const std::vector<Fixed<T>>& fb, T mu_t, T mu_n, T* X, T* V) {
+    for (const Fixed<T>& f : fb) {
+        if (f.type == 1) {
+            T rel[3] = {X[0] - f.p[0], X[1] - f.p[1], X[2] - f.p[2]};
+            T sd = dot3(rel, f.n);
+            if (sd < (T)0 && dot3(V, f.n) < (T)0) {
+                for (int d = 0; d < 3; ++d) X[d] -= sd * f.n[d];
+                contact_response(f.n, mu_t, mu_n, V);
+            }
+            continue;
+        }
+        T dv[3] = {X[0] - f.p[0], X[1] - f.p[1], X[2] - f.p[2]};
+        if (f.type == 2) {  // (I - a a^T) d
+            T q[3] = {dv[0], dv[1], dv[2]};
+            for (int r = 0; r < 3; ++r) {
+                T acc = 0;
+                for (int c = 0; c < 3; ++c) acc += ((r == c ? (T)1 : (T)0) - f.n[r] * f.n[c]) * q[c];
+                dv[r] = acc;
+            }
+        }
+        T len = std::sqrt(dot3(dv, dv));
+        if (len < f.r) {
+            T inv = (T)1 / len;
+            T nrm[3] = {dv[0] * inv, dv[1] * inv, dv[2] * inv};
+            for (int d = 0; d < 3; ++d) X[d] += (f.r - len) * nrm[d];
+            contact_response(nrm, mu_t, mu_n, V);
+        }
+    }
+}
+
 template <class T>
 int simulate(int nv, int nt, const float* X0, float* Xio, float* Vio, const uint32_t* tets, const float* mass,
-             const float* mu, const float* dbc, const orc_params* p, int nsteps, int* iters_out, double* step_seconds) {
+             const float* mu, const float* dbc, const orc_params* p, int nsteps, int* iters_out, double* step_seconds,
+             const orc_scene* sc) {
     Sim<T> S;
     S.nv = nv; S.nt = nt; S.tets = tets;
     TetGeom g;
@@ -573,16 +645,37 @@ int simulate(int nv, int nt, const float* X0, float* Xio, float* Vio, const uint
         S.stiff_diag.assign(sd.begin(), sd.end());
     }
     std::vector<T> X((size_t)3 * nv), V((size_t)3 * nv), sn((size_t)3 * nv), sn_old((size_t)3 * nv),
-        b((size_t)3 * nv), next((size_t)3 * nv);
+        b((size_t)3 * nv), next((size_t)3 * nv), XT((size_t)3 * nv), mdt2s(nv), dragw(nv, (T)0),
+        dbcx((size_t)3 * nv, (T)0);
     S.prev.assign((size_t)3 * nv, (T)0);
-    for (size_t i = 0; i < (size_t)3 * nv; ++i) { X[i] = Xio[i]; V[i] = Vio[i]; }
+    for (size_t i = 0; i < (size_t)3 * nv; ++i) {
+        X[i] = Xio[i];
+        V[i] = Vio[i];
+        XT[i] = (sc && sc->XT) ? (T)sc->XT[i] : X[i];
+    }
+    int num_pinned = 0;
+    for (int v = 0; v < nv; ++v) num_pinned += S.dbc[v] > 0;
+    const bool drag = sc && sc->drag_w;
+    if (drag)
+        for (int v = 0; v < nv; ++v) dragw[v] = (T)sc->drag_w[v];
+    const std::vector<Fixed<T>> fixed = fixed_bodies<T>(sc);
+    const T mu_t = sc ? (T)sc->mu_t : (T)0, mu_n = sc ? (T)sc->mu_n : (T)0;
     const T g_acc = (T)p->gravity;
     const double t_start = now_seconds();
     for (int step = 0; step < nsteps; ++step) {
         // prologue: pdSolver.cu:154-163 (gravity, setMDt_2MoreDBC, computeSn)
         for (int v = 0; v < nv; ++v) {
+            T md = dragw[v];
+            mdt2s[v] = S.dbc[v] == (T)0 ? (md > (T)0 ? (S.mass[v] + md) / dt2 : S.mass[v] / dt2) : S.mdt2[v];
+            if (md > (T)0) {  // dragged: target + offset, also the DBC position
+                for (int d = 0; d < 3; ++d) {
+                    sn[3 * v + d] = (T)sc->target[d] + (T)sc->drag_off[3 * v + d];
+                    dbcx[3 * v + d] = sn[3 * v + d];
+                }
+                continue;
+            }
             T f1 = -g_acc * S.mass[v];
-            T dt2_m_1 = (T)1 / S.mdt2[v];
+            T dt2_m_1 = (T)1 / mdt2s[v];
             sn[3 * v + 0] = X[3 * v + 0] + dt * V[3 * v + 0] + dt2_m_1 * (T)0;
             sn[3 * v + 1] = X[3 * v + 1] + dt * V[3 * v + 1] + dt2_m_1 * f1;
             sn[3 * v + 2] = X[3 * v + 2] + dt * V[3 * v + 2] + dt2_m_1 * (T)0;
@@ -594,11 +687,16 @@ int simulate(int nv, int nt, const float* X0, float* Xio, float* Vio, const uint
         T omega = 1;
         int it = 0;
         for (int i = 0; i < p->num_iterations && std::sqrt(err) >= (T)p->tol; ++i, ++it) {
-            local_rhs<T>(S, sn.data(), sn_old.data(), !chol, b.data());
-            // pinned RHS overwrite (pdUtil.cu:147-166)
-            for (int v = 0; v < nv; ++v)
-                if (S.dbc[v] > 0)
-                    for (int d = 0; d < 3; ++d) b[3 * v + d] = S.x0[3 * v + d] * (pw * dt2Inv);
+            local_rhs<T>(S, sn.data(), sn_old.data(), !chol, b.data(), mdt2s.data());
+            // pinned / dragged RHS overwrite (pdUtil.cu:147-166), run only
+            // when the system has pinned vertices (pdSolver.cu:170)
+            if (num_pinned > 0)
+                for (int v = 0; v < nv; ++v) {
+                    if (S.dbc[v] > 0)
+                        for (int d = 0; d < 3; ++d) b[3 * v + d] = S.x0[3 * v + d] * (pw * dt2Inv);
+                    else if (dragw[v] > (T)0)
+                        for (int d = 0; d < 3; ++d) b[3 * v + d] = dbcx[3 * v + d] * dragw[v];
+                }
             if (chol) {
                 S.chol.template solve3<T>(b.data(), sn.data());
                 T acc = 0;
@@ -615,10 +713,11 @@ int simulate(int nv, int nt, const float* X0, float* Xio, float* Vio, const uint
                 else omega = (T)4 / ((T)4 - rho * rho * omega);
 #pragma omp parallel for schedule(static)
                 for (int v = 0; v < nv; ++v) {
-                    T c = S.mdt2[v], md = S.stiff_diag[v];
+                    T c = mdt2s[v], md = S.stiff_diag[v];
                     for (int d = 0; d < 3; ++d) {
                         size_t k = 3 * (size_t)v + d;
-                        T nx = (b[k] - c * sn[k]) / (c + md) + sn[k];
+                        // dragged vertices keep the iterate (getErrorKern, pdUtil.cu:200-205)
+                        T nx = dragw[v] > (T)0 ? sn[k] : (b[k] - c * sn[k]) / (c + md) + sn[k];
                         // 0.9 is a double literal in the reference (pdUtil.cu:221)
                         nx = (T)(0.9 * (double)(nx - sn[k]) + (double)sn[k]);
                         nx = (nx - S.prev[k]) * omega + S.prev[k];
@@ -629,14 +728,22 @@ int simulate(int nv, int nt, const float* X0, float* Xio, float* Vio, const uint
             }
         }
         if (iters_out) iters_out[step] = it;
-        // updateVelPos (pdUtil.cu:180-193), X <- XTilde (pdSolver.cu:227)
-        for (size_t k = 0; k < (size_t)3 * nv; ++k) {
-            V[k] = (sn[k] - X[k]) * dtInv;
-            X[k] = sn[k];
+        // updateVelPos (pdUtil.cu:180-193), X <- XTilde (pdSolver.cu:227),
+        // fixed-body correction of XTilde and V (pdSolver.cu:228-231)
+        for (int v = 0; v < nv; ++v) {
+            for (int d = 0; d < 3; ++d) {
+                size_t k = 3 * (size_t)v + d;
+                V[k] = dragw[v] > (T)0 ? (T)0 : (sn[k] - XT[k]) * dtInv;
+                XT[k] = sn[k];
+                X[k] = sn[k];
+            }
+            if (!fixed.empty()) collide<T>(fixed, mu_t, mu_n, &XT[3 * (size_t)v], &V[3 * (size_t)v]);
         }
     }
     if (step_seconds) *step_seconds = now_seconds() - t_start;
     for (size_t i = 0; i < (size_t)3 * nv; ++i) { Xio[i] = (float)X[i]; Vio[i] = (float)V[i]; }
+    if (sc && sc->XT)
+        for (size_t i = 0; i < (size_t)3 * nv; ++i) sc->XT[i] = (float)XT[i];
     return 0;
 }
 
@@ -653,8 +760,25 @@ int orc_simulate(int nv, int nt, const float* X0, float* X, float* V, const uint
 #else
     (void)nthreads;
 #endif
-    if (precision == 64) return simulate<double>(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nsteps, iters_out, step_seconds);
-    return simulate<float>(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nsteps, iters_out, step_seconds);
+    if (precision == 64)
+        return simulate<double>(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nsteps, iters_out, step_seconds, nullptr);
+    return simulate<float>(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nsteps, iters_out, step_seconds, nullptr);
+}
+
+int orc_simulate_scene(int nv, int nt, const float* X0, float* X, float* V, const uint32_t* tets, const float* mass,
+                       const float* mu, const float* dbc, const orc_params* p, int precision, int nsteps,
+                       int nthreads, int* iters_out, double* step_seconds, const orc_scene* scene) {
+    if (nv <= 0 || nt <= 0 || !X0 || !X || !V || !tets || !mass || !mu || !p) return -1;
+    if (scene && ((scene->drag_w && !scene->drag_off) || (scene->nfixed > 0 && !scene->fixed) || scene->nfixed < 0))
+        return -1;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    if (precision == 64)
+        return simulate<double>(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nsteps, iters_out, step_seconds, scene);
+    return simulate<float>(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nsteps, iters_out, step_seconds, scene);
 }
 
 void orc_rotations(int n, const double* F, double* R, int precision) {
@@ -687,7 +811,7 @@ int orc_local_rhs(int nv, int nt, const float* X0, const uint32_t* tets, const f
     S.mdt2.resize(nv);
     double dt2 = (double)dt * (double)dt;
     for (int v = 0; v < nv; ++v) S.mdt2[v] = ((double)mass[v] + (dbc ? (double)dbc[v] : 0.0) * positional_weight) / dt2;
-    local_rhs<double>(S, q, s_old, jacobi_form != 0, b);
+    local_rhs<double>(S, q, s_old, jacobi_form != 0, b, S.mdt2.data());
     return 0;
 }
 

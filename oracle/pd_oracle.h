@@ -58,6 +58,36 @@ int orc_simulate(int nv, int nt, const float* X0, float* X, float* V,
                  const float* dbc, const orc_params* p, int precision,
                  int nsteps, int nthreads, int* iters_out, double* step_seconds);
 
+/* Scene terms of a step: interactive drag (SolverData moreDBC / OffsetX /
+ * mouseSelection.target, def.h:16-33; applied in pdUtil.cu:56-95, 147-205)
+ * and fixed rigid bodies (fixedBodyData.cu:66-148, applied after each step
+ * to XTilde and V, pdSolver.cu:218-232).  Body fields are the reference's
+ * FixedBody members: model = m_model (glm column-major), radius = m_radius,
+ * up = Plane::m_floorUp.  type: 0 sphere, 1 plane, 2 cylinder. */
+typedef struct orc_fixed_body {
+    int type;
+    float model[16];
+    float radius;
+    float up[3];
+} orc_fixed_body;
+
+typedef struct orc_scene {
+    const float* drag_w;    /* [nv] drag weights (moreDBC) or NULL         */
+    const float* drag_off;  /* [3 nv] offsets (OffsetX), with drag_w       */
+    float target[3];        /* mouse target                                */
+    int nfixed;
+    const orc_fixed_body* fixed;
+    float mu_t, mu_n;
+    float* XT;              /* [3 nv] XTilde in/out, or NULL (XTilde = X)  */
+} orc_scene;
+
+/* orc_simulate with scene terms (scene may be NULL). */
+int orc_simulate_scene(int nv, int nt, const float* X0, float* X, float* V,
+                       const uint32_t* tets, const float* mass, const float* mu,
+                       const float* dbc, const orc_params* p, int precision,
+                       int nsteps, int nthreads, int* iters_out, double* step_seconds,
+                       const orc_scene* scene);
+
 /* Closest proper rotation of each 3x3 matrix F (row-major, 9 per item).
  * precision 64: exact; 32: the float McAdams-style SVD.  R row-major. */
 void orc_rotations(int n, const double* F, double* R, int precision);

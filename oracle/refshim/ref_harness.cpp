@@ -7,7 +7,7 @@
 //   FEMSolver ctor      femSolver.cu:7-17  (computeInvDmV0)
 //   SolverPrepare       pdSolver.cu:40-139 (computeSiTSi, setMDt_2, DBCX = X0)
 //   SolverStep          pdSolver.cu:141-208
-//   Update (no collision, no fixed bodies)  pdSolver.cu:210-232
+//   Update (no CCD collision; fixed bodies)  pdSolver.cu:210-232
 // The only piece that is not the reference's code is the Cholesky global
 // solve: the reference calls cuSOLVER's sparse Cholesky (a GPU library);
 // here the same 3n x 3n system (the COO the kernels emit, duplicates summed
@@ -22,12 +22,21 @@
 #include <vector>
 
 #include "../pd_oracle.h"
+#include "ref_scene.h"
 
 thread_local refshim_dim3 blockIdx, threadIdx, blockDim, gridDim;
 
-extern "C" int ref_simulate(int nv, int nt, const float* X0in, float* Xio, float* Vio, const uint32_t* tetsin,
-                            const float* massin, const float* muin, const float* dbcin, float dt, float gravity,
-                            int numIterations, float tol, float rho, int solver, int nsteps, int* iters_out) {
+// Scene terms (nullable): select_v >= 0 runs the drag selection (the
+// reference's ResetMoreDBC while dragging) before the first step, or before
+// every step with reselect != 0 (as a mouse-move callback does); target is
+// the mouse target; the fixed bodies are built from their scene-file
+// description and applied after every step as PdSolver::Update does;
+// XTout (nullable) receives XTilde.
+extern "C" int ref_simulate_scene(int nv, int nt, const float* X0in, float* Xio, float* Vio, const uint32_t* tetsin,
+                                  const float* massin, const float* muin, const float* dbcin, float dt, float gravity,
+                                  int numIterations, float tol, float rho, int solver, int nsteps, int* iters_out,
+                                  int select_v, int reselect, const float* target_in, int nfixed,
+                                  const RefFixedSpec* fixed_specs, float muT, float muN, float* XTout) {
     const int tpb = 128;  // context.json "threads per block"
     const float positional_weight = 1e6f;
     const int vertBlocks = (nv + tpb - 1) / tpb;
@@ -103,8 +112,13 @@ extern "C" int ref_simulate(int nv, int nt, const float* X0in, float* Xio, float
     float omega = 1.f;
     const float dtInv = 1.0f / dt;
     const float dt2Inv = dtInv * dtInv;
-    const glm::vec3 target(0.f);
+    const glm::vec3 target = target_in ? glm::vec3(target_in[0], target_in[1], target_in[2]) : glm::vec3(0.f);
+    if (select_v >= nv) return -1;
+    void* fixed = nfixed > 0 ? ref_make_fixed(nfixed, fixed_specs) : nullptr;
+    if (select_v >= 0) ref_control(X.data(), DBC.data(), moreDBC.data(), OffsetX.data(), nv, select_v);
     for (int step = 0; step < nsteps; ++step) {
+        if (select_v >= 0 && reselect && step > 0)
+            ref_control(X.data(), DBC.data(), moreDBC.data(), OffsetX.data(), nv, select_v);
         // ---- SolverStep (pdSolver.cu:141-208)
         for (int v = 0; v < nv; ++v) ExtForce[v] = glm::vec3(0.0f, -gravity * mass[v], 0.0f);
         refshim_launch(vertBlocks, tpb, [&] {
@@ -155,13 +169,25 @@ extern "C" int ref_simulate(int nv, int nt, const float* X0in, float* Xio, float
             PdUtil::updateVelPos(sn.data(), dtInv, XTilde.data(), V.data(), nv, moreDBC.data());
         });
         X = XTilde;  // Update tail without collision handling (pdSolver.cu:227)
+        if (fixed) ref_handle_collisions(fixed, XTilde.data(), V.data(), nv, muT, muN);  // pdSolver.cu:228-231
     }
     if (factor) orc_free_factor(factor);
+    if (fixed) ref_free_fixed(fixed);
     for (int v = 0; v < nv; ++v) {
         Xio[3 * v] = X[v].x; Xio[3 * v + 1] = X[v].y; Xio[3 * v + 2] = X[v].z;
         Vio[3 * v] = V[v].x; Vio[3 * v + 1] = V[v].y; Vio[3 * v + 2] = V[v].z;
+        if (XTout) {
+            XTout[3 * v] = XTilde[v].x; XTout[3 * v + 1] = XTilde[v].y; XTout[3 * v + 2] = XTilde[v].z;
+        }
     }
     return 0;
+}
+
+extern "C" int ref_simulate(int nv, int nt, const float* X0in, float* Xio, float* Vio, const uint32_t* tetsin,
+                            const float* massin, const float* muin, const float* dbcin, float dt, float gravity,
+                            int numIterations, float tol, float rho, int solver, int nsteps, int* iters_out) {
+    return ref_simulate_scene(nv, nt, X0in, Xio, Vio, tetsin, massin, muin, dbcin, dt, gravity, numIterations, tol,
+                              rho, solver, nsteps, iters_out, -1, 0, nullptr, 0, nullptr, 0.5f, 0.5f, nullptr);
 }
 
 // The reference's rotation for one deformation gradient: svdGLM + R = U V^T

@@ -64,6 +64,15 @@ struct pdgb_engine {
     DBuf<float4> bsave, dx;
     bool cta_solve = false;  // whole solve in one CTA (small systems)
     double factor_ms = 0.0;
+    // scene terms: drag and fixed rigid bodies
+    bool drag_on = false;
+    DBuf<float> drag_w;
+    DBuf<float4> drag_off, drag_target;
+    DBuf<float4> xt;                  // XTilde, allocated when fixed bodies are first set
+    DBuf<FixedBodyDev> fixed;
+    int nfixed = 0;
+    float mu_t = 0.5f, mu_n = 0.5f;
+    int num_pinned = 0;
     // step graph
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -148,6 +157,23 @@ LocalArgs local_args(pdgb_engine* e, const int* done) {
     return a;
 }
 
+SceneArgs scene_args(pdgb_engine* e) {
+    SceneArgs sc{};
+    if (e->drag_on) {
+        sc.drag_w = e->drag_w.p;
+        sc.drag_off = e->drag_off.p;
+        sc.target = e->drag_target.p;
+        sc.drag_rhs = e->num_pinned > 0;
+    }
+    sc.dt2 = e->prm.dt * e->prm.dt;
+    sc.xt = e->xt.p;
+    sc.fixed = e->fixed.p;
+    sc.nfixed = e->nfixed;
+    sc.mu_t = e->mu_t;
+    sc.mu_n = e->mu_n;
+    return sc;
+}
+
 BeginArgs begin_args(pdgb_engine* e) {
     BeginArgs ba{};
     ba.nv = e->nv;
@@ -162,6 +188,7 @@ BeginArgs begin_args(pdgb_engine* e) {
     ba.gravity = e->prm.gravity;
     ba.vperm = e->vperm.p;
     ba.num_iterations = e->prm.num_iterations;
+    ba.sc = scene_args(e);
     return ba;
 }
 
@@ -181,6 +208,7 @@ void record_jacobi_step(pdgb_engine* e) {
     const LocalArgs la = local_args(e, nullptr);
     VertexArgs va{e->nv, e->sn.p, e->prev.p, e->b.p, e->base.p, e->coef.p, e->pin_rhs.p, e->x.p, e->v.p, 1.f,
                   1.0f / e->prm.dt};
+    va.sc = scene_args(e);
     for (int i = 0; i < n; ++i) {
         record_local(e, la, true, i);
         int mode = 0;
@@ -220,6 +248,8 @@ void record_chol_step(pdgb_engine* e) {
     cv.x = e->x.p;
     cv.v = e->v.p;
     cv.dt_inv = 1.0f / e->prm.dt;
+    cv.sc = scene_args(e);
+    const bool drag_rhs = cv.sc.drag_w && cv.sc.drag_rhs;
     const int refine = e->nbodies == 1 ? e->prm.refine_steps : 0;
     CholArgs cd = ca;  // refinement solves write the correction into dx
     cd.x = e->dx.p;
@@ -231,6 +261,7 @@ void record_chol_step(pdgb_engine* e) {
     };
     for (int i = 0; i < n; ++i) {
         record_local(e, la, false, i);
+        if (drag_rhs) launch_drag_rhs(e->nv, cv.sc, e->base.p, e->b.p, &st->done, s);
         if (refine > 0) launch_copy_rhs(e->nv, e->b.p, e->bsave.p, &st->done, s);
         solve(ca);
         for (int r = 0; r < refine; ++r) {
@@ -287,8 +318,8 @@ void upload_mesh(pdgb_engine* e) {
     e->base.alloc(nv);
     e->b.alloc(nv);
     e->y.alloc(nv);
-    e->coef.alloc(nv);
-    e->pin_rhs.alloc(nv);
+    e->coef.upload(L.coef, s);  // valid before the first prepare (pin flags)
+    e->pin_rhs.upload(L.pin_rhs, s);
     e->staging.alloc(6 * nv);
     e->st.alloc(1);
     PDGB_CUDA_TRY(cudaMemsetAsync(e->prev.p, 0, nv * sizeof(float4), s));
@@ -422,6 +453,8 @@ int create_impl(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* str
         copy_in(e->mu, mesh->mu, (size_t)e->nt, mesh->memory);
         e->has_dbc = mesh->dbc != nullptr;
         if (e->has_dbc) copy_in(e->dbc, mesh->dbc, (size_t)e->nv, mesh->memory);
+        if (e->has_dbc)
+            for (float d : e->dbc) e->num_pinned += d > 0.f;
         if (body_vstart) {
             e->nbodies = (int)body_vstart->size() - 1;
             e->body_vstart = *body_vstart;
@@ -638,6 +671,7 @@ int pdgb_upload_state(pdgb_engine* e, const float* X, const float* V, int memory
         } else {
             throw Error{PDGB_ERR_INVALID_ARGUMENT, "bad memory kind"};
         }
+        if (e->xt.p) launch_copy_state(e->nv, e->x.p, e->xt.p, e->stream);  // XTilde = X
         PDGB_CUDA_TRY(cudaGetLastError());
     });
 }
@@ -667,11 +701,162 @@ int pdgb_reset(pdgb_engine* e) {
     if (!e) return PDGB_ERR_INVALID_ARGUMENT;
     return guarded([&] {
         launch_copy_x0(e->nv, e->x0.p, e->x.p, e->v.p, e->stream);
+        if (e->xt.p) launch_copy_state(e->nv, e->x0.p, e->xt.p, e->stream);
+        if (e->drag_w.p) PDGB_CUDA_TRY(cudaMemsetAsync(e->drag_w.p, 0, (size_t)e->nv * sizeof(float), e->stream));
+        e->drag_on = false;
         PDGB_CUDA_TRY(cudaMemsetAsync(e->prev.p, 0, (size_t)e->nv * sizeof(float4), e->stream));
         PDGB_CUDA_TRY(cudaGetLastError());
         e->prepared = false;
         e->steps_run = 0;
         e->iters_run = 0;
+    });
+}
+
+// ---- drag
+namespace {
+void ensure_drag(pdgb_engine* e) {
+    if (e->drag_w.p) return;
+    e->drag_w.alloc(e->nv);
+    e->drag_off.alloc(e->nv);
+    e->drag_target.alloc(1);
+    PDGB_CUDA_TRY(cudaMemsetAsync(e->drag_w.p, 0, (size_t)e->nv * sizeof(float), e->stream));
+    PDGB_CUDA_TRY(cudaMemsetAsync(e->drag_off.p, 0, (size_t)e->nv * sizeof(float4), e->stream));
+    PDGB_CUDA_TRY(cudaMemsetAsync(e->drag_target.p, 0, sizeof(float4), e->stream));
+}
+
+void enable_drag(pdgb_engine* e) {
+    if (!e->drag_on) {
+        e->drag_on = true;
+        e->prepared = false;  // the step graph gains the drag terms
+    }
+}
+}  // namespace
+
+int pdgb_set_drag(pdgb_engine* e, const float* weights, const float* offsets, int memory) {
+    if (!e || !weights || (memory != PDGB_MEM_HOST && memory != PDGB_MEM_DEVICE)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine, weights or memory kind");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        const size_t nv = (size_t)e->nv;
+        std::vector<float> w, off;
+        copy_in(w, weights, nv, memory);
+        if (offsets) copy_in(off, offsets, 3 * nv, memory);
+        for (size_t i = 0; i < nv; ++i) {
+            if (!std::isfinite(w[i])) throw Error{PDGB_ERR_NONFINITE, "drag weight is not finite"};
+            if (w[i] > 0.f && e->has_dbc && e->dbc[i] > 0.f)
+                throw Error{PDGB_ERR_INVALID_ARGUMENT, "drag weight on pinned vertex " + std::to_string(i)};
+        }
+        ensure_drag(e);
+        // host copies are staged through the engine's transfer buffer
+        PDGB_CUDA_TRY(cudaMemcpyAsync(e->staging.p, w.data(), nv * sizeof(float), cudaMemcpyHostToDevice, e->stream));
+        if (offsets)
+            PDGB_CUDA_TRY(cudaMemcpyAsync(e->staging.p + nv, off.data(), 3 * nv * sizeof(float), cudaMemcpyHostToDevice,
+                                          e->stream));
+        launch_gather_drag(e->nv, e->vperm.p, e->staging.p, offsets ? e->staging.p + nv : nullptr, e->drag_w.p,
+                           e->drag_off.p, e->stream);
+        PDGB_CUDA_TRY(cudaGetLastError());
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));  // w / off leave scope
+        enable_drag(e);
+    });
+}
+
+int pdgb_drag_select(pdgb_engine* e, int select_v, float control_mag, double radius_sq) {
+    if (!e || select_v < -1 || select_v >= (e ? e->nv : 0) || !(control_mag >= 0.f)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine, vertex or control magnitude");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        ensure_drag(e);
+        const int sel = select_v < 0 ? -1 : e->L.viperm[select_v];
+        launch_drag_select(e->nv, e->x.p, e->coef.p, sel, control_mag, radius_sq, e->drag_w.p, e->drag_off.p,
+                           e->stream);
+        PDGB_CUDA_TRY(cudaGetLastError());
+        enable_drag(e);
+    });
+}
+
+int pdgb_set_drag_target(pdgb_engine* e, const float target[3]) {
+    if (!e || !target) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        ensure_drag(e);
+        const float4 t = make_float4(target[0], target[1], target[2], 0.f);
+        // pageable source: the call returns once the 16 bytes are staged
+        PDGB_CUDA_TRY(cudaMemcpyAsync(e->drag_target.p, &t, sizeof(t), cudaMemcpyHostToDevice, e->stream));
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    });
+}
+
+int pdgb_clear_drag(pdgb_engine* e) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (e->drag_w.p) PDGB_CUDA_TRY(cudaMemsetAsync(e->drag_w.p, 0, (size_t)e->nv * sizeof(float), e->stream));
+        if (e->drag_on) {
+            e->drag_on = false;
+            e->prepared = false;
+        }
+    });
+}
+
+// ---- fixed rigid bodies
+int pdgb_set_fixed_bodies(pdgb_engine* e, const pdgb_fixed_body* bodies, int n, float mu_t, float mu_n) {
+    if (!e || n < 0 || (n > 0 && !bodies) || n > 4096 || !std::isfinite(mu_t) || !std::isfinite(mu_n)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine, body list or friction coefficients");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        std::vector<FixedBodyDev> dev;
+        for (int kind : {PDGB_FIXED_SPHERE, PDGB_FIXED_PLANE, PDGB_FIXED_CYLINDER})
+            for (int j = 0; j < n; ++j) {
+                const pdgb_fixed_body& fb = bodies[j];
+                if (fb.type < PDGB_FIXED_SPHERE || fb.type > PDGB_FIXED_CYLINDER)
+                    throw Error{PDGB_ERR_INVALID_ARGUMENT, "unknown fixed body type"};
+                for (float m : fb.model)
+                    if (!std::isfinite(m)) throw Error{PDGB_ERR_NONFINITE, "fixed body model is not finite"};
+                if (fb.type != kind) continue;
+                FixedBodyDev d{};
+                d.p = make_float4(fb.model[12], fb.model[13], fb.model[14], fb.radius);
+                if (kind == PDGB_FIXED_PLANE) {
+                    d.n = make_float4(fb.up[0], fb.up[1], fb.up[2], (float)kFixedPlane);
+                } else if (kind == PDGB_FIXED_CYLINDER) {
+                    // normalize(vec3(model * vec4(0, 1, 0, 0))), fixedBodyData.cu:116
+                    const float ax = fb.model[4], ay = fb.model[5], az = fb.model[6];
+                    const float inv = 1.0f / std::sqrt(ax * ax + ay * ay + az * az);
+                    d.n = make_float4(ax * inv, ay * inv, az * inv, (float)kFixedCylinder);
+                } else {
+                    d.n = make_float4(0.f, 0.f, 0.f, (float)kFixedSphere);
+                }
+                dev.push_back(d);
+            }
+        if (n > 0 && !e->xt.p) {  // XTilde starts as X
+            e->xt.alloc(e->nv);
+            launch_copy_state(e->nv, e->x.p, e->xt.p, e->stream);
+            PDGB_CUDA_TRY(cudaGetLastError());
+        }
+        if (!dev.empty()) e->fixed.upload(dev, e->stream);
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        e->nfixed = (int)dev.size();
+        e->mu_t = mu_t;
+        e->mu_n = mu_n;
+        e->prepared = false;  // body count and friction are graph parameters
+    });
+}
+
+int pdgb_download_xtilde(pdgb_engine* e, float* XT, int memory) {
+    if (!e || !XT) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        const float4* src = e->xt.p ? e->xt.p : e->x.p;
+        const size_t n3 = 3 * (size_t)e->nv;
+        if (memory == PDGB_MEM_HOST) {
+            launch_scatter_state(e->nv, e->vperm.p, src, nullptr, e->staging.p, nullptr, e->stream);
+            PDGB_CUDA_TRY(cudaMemcpyAsync(XT, e->staging.p, n3 * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+            PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        } else if (memory == PDGB_MEM_DEVICE) {
+            launch_scatter_state(e->nv, e->vperm.p, src, nullptr, XT, nullptr, e->stream);
+        } else {
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "bad memory kind"};
+        }
+        PDGB_CUDA_TRY(cudaGetLastError());
     });
 }
 

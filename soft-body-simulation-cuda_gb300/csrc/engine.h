@@ -134,6 +134,30 @@ enum : int {
     kFinal = 4,       // last iteration: velocity/position update, no b reset
 };
 
+// ---- interactive drag and fixed rigid bodies (optional per engine)
+enum : int { kFixedSphere = 0, kFixedPlane = 1, kFixedCylinder = 2 };
+
+// One fixed rigid body: p.xyz = sphere/cylinder centre or a point of the
+// plane, p.w = radius; n.xyz = plane normal or cylinder axis (unit),
+// n.w = type.  Bodies are stored spheres first, then planes, then cylinders
+// (the order FixedBodyData::HandleCollisions applies them).
+struct FixedBodyDev {
+    float4 p;
+    float4 n;
+};
+
+struct SceneArgs {
+    const float* drag_w;      // per-vertex drag weight (moreDBC); null: no drag
+    const float4* drag_off;   // per-vertex offset from the grabbed vertex
+    const float4* target;     // drag target, one float4 in device memory
+    int drag_rhs;             // the system has pinned vertices, so dragged rows of b are overwritten
+    float dt2;                // dt * dt
+    float4* xt;               // XTilde (position after collision handling); null: X serves as XTilde
+    const FixedBodyDev* fixed;
+    int nfixed;
+    float mu_t, mu_n;
+};
+
 struct VertexArgs {
     int nv;
     float4* sn;
@@ -146,6 +170,7 @@ struct VertexArgs {
     float4* v;
     float omega;
     float dt_inv;
+    SceneArgs sc;
 };
 
 struct BeginArgs {
@@ -167,6 +192,7 @@ struct BeginArgs {
     int* done;          // reset to 0 at step start (may be null)
     int* iterations;    // reset to the full count (may be null)
     int num_iterations;
+    SceneArgs sc;
 };
 
 void launch_begin(const BeginArgs& a, cudaStream_t s);
@@ -183,5 +209,15 @@ void launch_gather_state(int nv, const int* vperm, const float* X, const float* 
 void launch_scatter_state(int nv, const int* vperm, const float4* x, const float4* v, float* X, float* V,
                           cudaStream_t s);
 void launch_copy_x0(int nv, const float4* x0, float4* x, float4* v, cudaStream_t s);
+
+// Drag: per-vertex weights and offsets from caller order (gather); the
+// selection kernel of the reference's mouse drag; the Cholesky-path RHS
+// overwrite of dragged rows after the local step.
+void launch_gather_drag(int nv, const int* vperm, const float* w, const float* off, float* drag_w, float4* drag_off,
+                        cudaStream_t s);
+void launch_drag_select(int nv, const float4* x, const float4* coef, int select_v, float control_mag,
+                        double radius_sq, float* drag_w, float4* drag_off, cudaStream_t s);
+void launch_drag_rhs(int nv, const SceneArgs& sc, const float4* base, float4* b, const int* done, cudaStream_t s);
+void launch_copy_state(int nv, const float4* src, float4* dst, cudaStream_t s);
 
 }  // namespace pdgb

@@ -9,6 +9,7 @@
 //   k_begin        step prologue: gravity, s_n, M/h^2 s_n (reference:
 //                  pdSolver.cu:154-163, computeSn pdUtil.cu:73-95)
 #include "engine.h"
+#include "scene.cuh"
 #include "rotation.cuh"
 
 namespace pdgb {
@@ -158,9 +159,16 @@ __device__ __forceinline__ void jacobi_vertex(const VertexArgs& a, int i, float 
     const float4 bb = (cf.z != 0.f) ? __ldg(&a.pin_rhs[i]) : a.b[i];
     const float den = cm + md;
     float4 nx;
-    nx.x = relax09((bb.x - cm * s.x) / den + s.x, s.x);
-    nx.y = relax09((bb.y - cm * s.y) / den + s.y, s.y);
-    nx.z = relax09((bb.z - cm * s.z) / den + s.z, s.z);
+    if (drag_weight(a.sc, i) > 0.f) {
+        nx = s;  // dragged vertices keep the current iterate (getErrorKern, pdUtil.cu:200-205)
+    } else {
+        nx.x = (bb.x - cm * s.x) / den + s.x;
+        nx.y = (bb.y - cm * s.y) / den + s.y;
+        nx.z = (bb.z - cm * s.z) / den + s.z;
+    }
+    nx.x = relax09(nx.x, s.x);
+    nx.y = relax09(nx.y, s.y);
+    nx.z = relax09(nx.z, s.z);
     nx.w = 0.f;
     if (kMode & kReadPrev) {
         const float4 p = a.prev[i];
@@ -170,9 +178,7 @@ __device__ __forceinline__ void jacobi_vertex(const VertexArgs& a, int i, float 
     }
     if (kMode & kWritePrev) a.prev[i] = s;
     if (kMode & kFinal) {
-        const float4 xo = a.x[i];
-        a.v[i] = make_float4((nx.x - xo.x) * a.dt_inv, (nx.y - xo.y) * a.dt_inv, (nx.z - xo.z) * a.dt_inv, 0.f);
-        a.x[i] = nx;
+        finish_vertex(a.sc, i, nx, a.dt_inv, a.x, a.v);
     } else {
         a.sn[i] = nx;
         a.b[i] = __ldg(&a.base[i]);
@@ -229,18 +235,29 @@ void launch_jacobi_vertex(const VertexArgs& a, int mode, cudaStream_t s) {
 }
 
 // Step prologue: f = (0, -g m, 0); s = x + h v + f / (M/h^2); base = (M/h^2) s;
-// b = base (pinned vertices: the pin RHS).
+// b = base (pinned vertices: the pin RHS).  A dragged vertex (weight w > 0)
+// starts at its drag target, its M/h^2 becomes (m + w)/h^2
+// (setMDt_2MoreDBC, pdUtil.cu:56-69), and when the system has pinned
+// vertices its RHS row is target * w (computeDBCLocal, pdUtil.cu:159-164).
 __device__ __forceinline__ void begin_vertex(const BeginArgs& a, int i) {
     const float4 x = a.x[i], v = a.v[i], cf = __ldg(&a.coef[i]);
-    const float dt2_m_1 = 1.0f / cf.x;
-    const float fy = -a.gravity * cf.w;
+    const float w = drag_weight(a.sc, i);
     float4 s;
-    s.x = x.x + a.dt * v.x + dt2_m_1 * 0.0f;
-    s.y = x.y + a.dt * v.y + dt2_m_1 * fy;
-    s.z = x.z + a.dt * v.z + dt2_m_1 * 0.0f;
-    s.w = 0.f;
+    float mdt2 = cf.x;
+    if (w > 0.f) {
+        s = drag_target(a.sc, i);
+        if (cf.z == 0.f) mdt2 = (cf.w + w) / a.sc.dt2;
+    } else {
+        const float dt2_m_1 = 1.0f / cf.x;
+        const float fy = -a.gravity * cf.w;
+        s.x = x.x + a.dt * v.x + dt2_m_1 * 0.0f;
+        s.y = x.y + a.dt * v.y + dt2_m_1 * fy;
+        s.z = x.z + a.dt * v.z + dt2_m_1 * 0.0f;
+        s.w = 0.f;
+    }
     a.sn[i] = s;
-    const float4 bs = make_float4(cf.x * s.x, cf.x * s.y, cf.x * s.z, 0.f);
+    float4 bs = make_float4(mdt2 * s.x, mdt2 * s.y, mdt2 * s.z, 0.f);
+    if (w > 0.f && a.sc.drag_rhs && cf.z == 0.f) bs = make_float4(s.x * w, s.y * w, s.z * w, 0.f);
     a.base[i] = bs;
     a.b[i] = cf.z != 0.f ? __ldg(&a.pin_rhs[i]) : bs;
     if (a.prev) {

@@ -9,6 +9,7 @@
 // hold engine vertex ids, so no permutation pass is needed.
 #include "engine.h"
 #include "solve.h"
+#include "scene.cuh"
 
 namespace pdgb {
 
@@ -206,14 +207,12 @@ __global__ void __launch_bounds__(256) k_chol_vertex(CholVertexArgs a) {
 }
 
 // After the iterations: velocity / position update (updateVelPos,
-// pdUtil.cu:180-193) and X <- XTilde (pdSolver.cu:227).
+// pdUtil.cu:180-193), X <- XTilde (pdSolver.cu:227) and the fixed-body
+// correction of XTilde and V (pdSolver.cu:228-231).
 __global__ void __launch_bounds__(256) k_chol_finish(CholVertexArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.nv) return;
-    const float4 s = a.sn[i];
-    const float4 xo = a.x[i];
-    a.v[i] = make_float4((s.x - xo.x) * a.dt_inv, (s.y - xo.y) * a.dt_inv, (s.z - xo.z) * a.dt_inv, 0.f);
-    a.x[i] = s;
+    finish_vertex(a.sc, i, a.sn[i], a.dt_inv, a.x, a.v);
     a.y[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 

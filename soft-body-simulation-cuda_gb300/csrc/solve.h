@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "cholesky.h"
+#include "engine.h"
 
 namespace pdgb {
 
@@ -50,6 +51,7 @@ struct CholVertexArgs {
     float4* x;
     float4* v;
     float dt_inv;
+    SceneArgs sc;
 };
 
 // One launch per level and direction (large systems).

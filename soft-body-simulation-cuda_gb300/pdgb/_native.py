@@ -30,6 +30,9 @@ PDGB_ROTATION_QUAT = 0
 PDGB_ROTATION_SVD = 1
 PDGB_ORDER_AMD = 0
 PDGB_ORDER_ND = 1
+PDGB_FIXED_SPHERE = 0
+PDGB_FIXED_PLANE = 1
+PDGB_FIXED_CYLINDER = 2
 
 
 class pdgb_params(C.Structure):
@@ -138,6 +141,15 @@ class pdgb_layout_info(C.Structure):
     ]
 
 
+class pdgb_fixed_body(C.Structure):
+    _fields_ = [
+        ("type", C.c_int),
+        ("model", C.c_float * 16),
+        ("radius", C.c_float),
+        ("up", C.c_float * 3),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/pdgb.h declares.
 SIGNATURES = {
     "pdgb_default_params": (None, [C.POINTER(pdgb_params)]),
@@ -182,6 +194,12 @@ SIGNATURES = {
     "pdgb_server_destroy": (C.c_int, [C.c_void_p]),
     "pdgb_inspect_layout": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_layout_info), C.c_void_p,
                                       C.c_void_p]),
+    "pdgb_set_drag": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "pdgb_drag_select": (C.c_int, [C.c_void_p, C.c_int, C.c_float, C.c_double]),
+    "pdgb_set_drag_target": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "pdgb_clear_drag": (C.c_int, [C.c_void_p]),
+    "pdgb_set_fixed_bodies": (C.c_int, [C.c_void_p, C.POINTER(pdgb_fixed_body), C.c_int, C.c_float, C.c_float]),
+    "pdgb_download_xtilde": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
 }
 
 _lib = None

@@ -128,6 +128,36 @@ class PdSolver:
         N.check(self._lib.pdgb_download_state(self._h, _ptr(X), _ptr(V), N.PDGB_MEM_HOST), "pdgb_download_state")
         return X, V
 
+    def download_xtilde(self) -> np.ndarray:
+        """XTilde: positions after the fixed-body correction (= X without bodies)."""
+        XT = np.empty((self.num_verts, 3), dtype=np.float32)
+        N.check(self._lib.pdgb_download_xtilde(self._h, _ptr(XT), N.PDGB_MEM_HOST), "pdgb_download_xtilde")
+        return XT
+
+    # -- interactive drag (moreDBC / OffsetX / mouse target of SolverData)
+    def set_drag(self, weights: np.ndarray, offsets: np.ndarray | None = None) -> None:
+        w = np.ascontiguousarray(weights, dtype=np.float32).reshape(self.num_verts)
+        o = None if offsets is None else np.ascontiguousarray(offsets, dtype=np.float32).reshape(self.num_verts, 3)
+        N.check(self._lib.pdgb_set_drag(self._h, _ptr(w), _ptr(o), N.PDGB_MEM_HOST), "pdgb_set_drag")
+
+    def drag_select(self, select_v: int, control_mag: float = 10.0, radius_sq: float = 0.002) -> None:
+        """The reference's mouse selection (Control_Kernel) around vertex select_v."""
+        N.check(self._lib.pdgb_drag_select(self._h, int(select_v), float(control_mag), float(radius_sq)),
+                "pdgb_drag_select")
+
+    def set_drag_target(self, target) -> None:
+        t = (C.c_float * 3)(*[float(v) for v in target])
+        N.check(self._lib.pdgb_set_drag_target(self._h, t), "pdgb_set_drag_target")
+
+    def clear_drag(self) -> None:
+        N.check(self._lib.pdgb_clear_drag(self._h), "pdgb_clear_drag")
+
+    # -- fixed rigid bodies
+    def set_fixed_bodies(self, bodies: list, mu_t: float = 0.5, mu_n: float = 0.5) -> None:
+        arr = (N.pdgb_fixed_body * max(1, len(bodies)))(*[b.to_c() for b in bodies])
+        N.check(self._lib.pdgb_set_fixed_bodies(self._h, arr, len(bodies), float(mu_t), float(mu_n)),
+                "pdgb_set_fixed_bodies")
+
     def download_body(self, b: int) -> tuple[np.ndarray, np.ndarray]:
         n = int(self.body_verts[b + 1] - self.body_verts[b])
         X = np.empty((n, 3), dtype=np.float32)

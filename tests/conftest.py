@@ -44,3 +44,34 @@ def load_golden(name: str):
 
 GOLDEN_CASES = ["tet1_jacobi", "grid3_jacobi", "grid3_chol", "grid3_chol_tol", "grid435_soft_jacobi", "c1_chol",
                 "c1_jacobi"]
+
+
+# Cases with the reference's interactive drag and fixed rigid bodies
+# (tests/golden/make_golden.py, make_scene_case).
+SCENE_CASES = ["drag_jacobi", "drag_chol", "drag_chol_nopin", "fixed_jacobi", "fixed_chol"]
+
+
+def load_scene_golden(name: str):
+    """(body, params, steps, X, V, scene) with scene = select_v, reselect,
+    target, fixed (rows type, pos, rot, scale), mu_t, mu_n, XT."""
+    body, params, steps, X, V, _ = load_golden(name)
+    z = np.load(GOLDEN / f"{name}.npz")
+    sc = {"select_v": int(z["select_v"]), "reselect": bool(z["reselect"]), "target": z["target"],
+          "fixed": z["fixed"], "mu_t": float(z["mu_t"]), "mu_n": float(z["mu_n"]), "XT": z["XT"]}
+    return body, params, steps, X, V, sc
+
+
+def scene_fixed_bodies(rows):
+    """Fixed bodies of a case, built as a scene file would (pdgb.scene)."""
+    from pdgb import scene
+
+    out = []
+    for r in np.asarray(rows, np.float32).reshape(-1, 10):
+        t, pos, rot, sc = int(r[0]), r[1:4], r[4:7], r[7:10]
+        if t == 0:
+            out.append(scene.sphere(pos, float(sc[0]), rot))
+        elif t == 1:
+            out.append(scene.plane(pos, rot, sc))
+        else:
+            out.append(scene.cylinder(pos, rot, sc))
+    return out

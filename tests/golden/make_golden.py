@@ -10,6 +10,9 @@ synthetic body, and stores inputs and outputs:
   X, V                           state after `steps` steps
   iters                          local/global iterations run per step
 
+Scene cases (drag_*, fixed_*) add the reference's interactive drag and
+fixed rigid bodies (see make_scene_case).
+
 Also `rotations.npz`: random deformation gradients (including inverted and
 nearly flat ones) with the reference's rotation R = U V^T (svd.cuh:7-14 +
 pdUtil.cu:113-122).
@@ -54,6 +57,60 @@ CASES = {
 }
 
 
+def _small_body(pin):
+    # 6^3 cells of 2 cm: the reference's drag radius (sqrt(0.002) m) covers
+    # a few dozen vertices
+    return mesh.make_grid_body(6, 6, 6, size=(0.12, 0.12, 0.12), young=2e4, poisson=0.4, jitter=0.1, seed=21,
+                               pin=pin)
+
+
+def _falling_body():
+    return mesh.make_grid_body(5, 5, 5, size=(0.5, 0.5, 0.5), origin=(0.0, 0.05, 0.0), young=1e5, poisson=0.4,
+                               jitter=0.1, seed=4, pin=None)
+
+
+# (type, pos, rot_deg, scale) as a scene file gives them; sphere radius = scale[0]
+_FIXED = [(0, (0.25, -0.1, 0.25), (0.0, 0.0, 0.0), (0.12, 0.12, 0.12)),
+          (1, (0.0, 0.0, 0.0), (5.0, 0.0, 3.0), (4.0, 4.0, 4.0)),
+          (2, (0.25, 0.05, 0.25), (0.0, 0.0, 90.0), (0.05, 2.0, 0.05))]
+
+SCENE_CASES = {
+    # name: (body factory, params, steps, select_v, reselect, target offset from X[select_v], fixed, mu_t, mu_n)
+    "drag_jacobi": (lambda: _small_body("top"), SolverParams(num_iterations=20, rho=0.9995, solver=0), 30,
+                    0, True, (0.05, -0.04, 0.03), [], 0.5, 0.5),
+    "drag_chol": (lambda: _small_body("top"), SolverParams(num_iterations=10, solver=1), 30,
+                  0, True, (0.05, -0.04, 0.03), [], 0.5, 0.5),
+    "drag_chol_nopin": (lambda: _small_body(None), SolverParams(num_iterations=10, solver=1), 20,
+                        0, False, (0.02, 0.03, -0.01), [], 0.5, 0.5),
+    "fixed_jacobi": (_falling_body, SolverParams(num_iterations=20, rho=0.9995, solver=0), 60,
+                     -1, False, (0.0, 0.0, 0.0), _FIXED, 0.5, 0.3),
+    "fixed_chol": (_falling_body, SolverParams(num_iterations=10, solver=1), 60,
+                   -1, False, (0.0, 0.0, 0.0), _FIXED, 0.5, 0.3),
+}
+
+
+def make_scene_case(name: str) -> Path:
+    """Drag (the reference's Control_Kernel selection, re-run before every
+    step when `reselect`, as its mouse-move callback does) and fixed rigid
+    bodies (FixedBodyData kernels after every step).  Adds to the case file:
+    select_v, reselect, target, fixed (rows type, pos, rot, scale), mu_t,
+    mu_n and XT (XTilde after the last step)."""
+    factory, params, steps, sel, reselect, toff, fixed, mu_t, mu_n = SCENE_CASES[name]
+    body = factory()
+    target = (np.zeros(3, np.float32) if sel < 0 else body.X[sel] + np.asarray(toff, np.float32)).astype(np.float32)
+    X, V, XT, iters = O.reference_simulate_scene(body, params, steps, select_v=sel, reselect=reselect,
+                                                 target=target, fixed_specs=fixed, mu_t=mu_t, mu_n=mu_n)
+    rows = np.array([[t, *pos, *rot, *sc] for (t, pos, rot, sc) in fixed], dtype=np.float32).reshape(-1, 10)
+    out = HERE / f"{name}.npz"
+    np.savez_compressed(
+        out, X0=body.X, tets=body.tets, mass=body.mass, mu=body.mu, dbc=body.dbc,
+        dt=np.float32(params.dt), gravity=np.float32(params.gravity), num_iterations=np.int32(params.num_iterations),
+        tol=np.float32(params.tol), rho=np.float32(params.rho), solver=np.int32(params.solver),
+        steps=np.int32(steps), X=X, V=V, iters=iters, XT=XT, select_v=np.int32(sel),
+        reselect=np.int32(reselect), target=target, fixed=rows, mu_t=np.float32(mu_t), mu_n=np.float32(mu_n))
+    return out
+
+
 def make_case(name: str) -> Path:
     factory, params, steps = CASES[name]
     body = factory()
@@ -96,6 +153,9 @@ def main() -> None:
         raise SystemExit("oracle/_ref/libref_pd.so is missing: build it with oracle/build_ref.sh")
     for name in CASES:
         p = make_case(name)
+        print("wrote", p.relative_to(ROOT), p.stat().st_size, "bytes")
+    for name in SCENE_CASES:
+        p = make_scene_case(name)
         print("wrote", p.relative_to(ROOT), p.stat().st_size, "bytes")
     p = make_rotations()
     print("wrote", p.relative_to(ROOT), p.stat().st_size, "bytes")

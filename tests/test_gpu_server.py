@@ -3,6 +3,8 @@
 Every request's result must equal the same body simulated alone by a single
 engine (same kernels; only the float summation order of atomics across tiles
 may differ) and match the FP64 oracle within the parity bar."""
+import time
+
 import numpy as np
 import pytest
 
@@ -96,11 +98,17 @@ def test_slot_limit_and_bad_request():
     with PdServer(PARAMS, max_active=2) as srv:
         ids = [srv.submit(b, s) for b, s in reqs[:4]]
         bad_id = srv.submit(bad, 3)
-        for _ in range(300):
+        # the bad request fails in a layout worker, possibly after the good
+        # ones have finished: tick until both are settled (bounded in time)
+        deadline = time.monotonic() + 60.0
+        while time.monotonic() < deadline:
             a, _ = srv.tick()
             assert a <= 2
-            if all(srv.poll(i)[0] == N.PDGB_REQ_DONE for i in ids):
+            if (all(srv.poll(i)[0] == N.PDGB_REQ_DONE for i in ids)
+                    and srv.poll(bad_id)[0] == N.PDGB_REQ_FAILED):
                 break
+            if a == 0:
+                time.sleep(0.01)
         assert srv.poll(bad_id)[0] == N.PDGB_REQ_FAILED
         with pytest.raises(Exception):
             srv.result(bad_id)
