@@ -338,6 +338,65 @@ int pdgb_set_fixed_bodies(pdgb_engine* e, const pdgb_fixed_body* bodies, int n, 
 int pdgb_download_xtilde(pdgb_engine* e, float* XT, int memory);
 
 /* ---------------------------------------------------------------------
+ * Tet-mesh files (host only, no GPU needed).  Replaces the reference's
+ * DataLoader::CollectData for one soft body (src/simulation/dataLoader.cu:
+ * 38-290; Gmsh reader src/simulation/MshLoader.cpp):
+ *   - TetGen: node_file + ele_file (+ optional face_file).  The .node's
+ *     first line holds the vertex count, each following "id x y z ..." line
+ *     the next vertex; .ele / .face lines "id a b c [d] ..." hold corner ids
+ *     minus start_index (the scene file's "start index"; -1 = the first
+ *     .node id).  centralize subtracts the centroid and swaps y and z.
+ *     Without faces the surface is extracted from the tets (faces used by
+ *     exactly one tet, ascending by sorted corners, oriented as the tet
+ *     lists them).  '#' comments and blank lines are skipped.
+ *   - Gmsh 2.0-2.2, ASCII or binary: msh_file (used when node_file is NULL
+ *     or empty); its tetrahedra (type 4, corner nodes of type 11); no
+ *     centring and no surface, as in the reference.
+ *   - placement: X <- translate(pos) * scale(scale) * rotX * rotY * rotZ * X,
+ *     angles in degrees (dataLoader.cu:209-217).
+ * The result owns its arrays (malloc); free it with pdgb_free_tet_mesh.
+ * Edges are the distinct surface-triangle edges, ascending. */
+typedef struct pdgb_body_file {
+    const char* node_file;
+    const char* ele_file;
+    const char* face_file;
+    const char* msh_file;
+    float pos[3];
+    float scale[3];
+    float rot[3];
+    int centralize;
+    int start_index;
+} pdgb_body_file;
+
+typedef struct pdgb_tet_mesh {
+    int num_verts;
+    int num_tets;
+    int num_tris;
+    int num_edges;
+    float* X;          /* [3 num_verts], placed                          */
+    uint32_t* tets;    /* [4 num_tets]                                   */
+    uint32_t* tris;    /* [3 num_tris] surface triangles                 */
+    uint32_t* edges;   /* [2 num_edges]                                  */
+} pdgb_tet_mesh;
+int pdgb_load_body_file(const pdgb_body_file* file, pdgb_tet_mesh** out);
+void pdgb_free_tet_mesh(pdgb_tet_mesh* mesh);
+/* Surface triangles of a tet list (the extraction above); capacity in
+ * triangles.  num_tris receives the count even when capacity is short
+ * (then PDGB_ERR_INVALID_ARGUMENT). */
+int pdgb_surface_triangles(int num_tets, const uint32_t* tets, uint32_t* tris, long long capacity, int* num_tris);
+
+/* Render-side positions and normals of a triangle surface, written to
+ * device buffers in place of the reference's OpenGL vertex buffers
+ * (PopulateTriPos + RecalculateNormals, utilities.cu:93-107, 147-183, run
+ * by SimulationCUDAContext::PrepareRenderData, simulationContext.cu:
+ * 245-257).  tris (device, uint32[3 n], caller vertex ids) index the
+ * engine's current X.  tri_pos (device, float[9 n]) receives per triangle
+ * X[t0], X[t2], X[t1]; tri_nor (device, float[12 n]) the face normal
+ * cross(p1 - p0, p2 - p0), normalised when its squared length exceeds
+ * 1e-12, w = 0, once per corner.  Stream-ordered, no synchronisation. */
+int pdgb_render_surface(pdgb_engine* e, const uint32_t* tris, int num_tris, float* tri_pos, float* tri_nor);
+
+/* ---------------------------------------------------------------------
  * Allocation-free PD steps.  No counterpart in the reference: it exists for
  * callers that must not allocate device memory when they advance a body -- a
  * host application whose own allocator owns the GPU's memory, a frame loop

@@ -46,6 +46,7 @@ struct pdgb_engine {
     DBuf<uint16_t> inc_ent, inc_end;
     DBuf<float> geo;
     DBuf<int> tile_tet_ptr, tile_vptr, vperm;
+    DBuf<int> viperm;  // caller -> internal vertex, uploaded on first render
     DBuf<uint32_t> tile_verts;
     DBuf<float4> coef, pin_rhs, x0;
     // device: state + scratch
@@ -856,6 +857,18 @@ int pdgb_download_xtilde(pdgb_engine* e, float* XT, int memory) {
         } else {
             throw Error{PDGB_ERR_INVALID_ARGUMENT, "bad memory kind"};
         }
+        PDGB_CUDA_TRY(cudaGetLastError());
+    });
+}
+
+int pdgb_render_surface(pdgb_engine* e, const uint32_t* tris, int num_tris, float* tri_pos, float* tri_nor) {
+    if (!e || num_tris < 0 || (num_tris > 0 && (!tris || !tri_pos || !tri_nor))) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine, triangles or output buffers");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        if (!e->viperm.p) e->viperm.upload(e->L.viperm, e->stream);
+        launch_render_surface(num_tris, tris, e->viperm.p, e->nv, e->x.p, tri_pos, tri_nor, e->stream);
         PDGB_CUDA_TRY(cudaGetLastError());
     });
 }

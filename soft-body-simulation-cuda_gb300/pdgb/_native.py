@@ -150,6 +150,33 @@ class pdgb_fixed_body(C.Structure):
     ]
 
 
+class pdgb_body_file(C.Structure):
+    _fields_ = [
+        ("node_file", C.c_char_p),
+        ("ele_file", C.c_char_p),
+        ("face_file", C.c_char_p),
+        ("msh_file", C.c_char_p),
+        ("pos", C.c_float * 3),
+        ("scale", C.c_float * 3),
+        ("rot", C.c_float * 3),
+        ("centralize", C.c_int),
+        ("start_index", C.c_int),
+    ]
+
+
+class pdgb_tet_mesh(C.Structure):
+    _fields_ = [
+        ("num_verts", C.c_int),
+        ("num_tets", C.c_int),
+        ("num_tris", C.c_int),
+        ("num_edges", C.c_int),
+        ("X", C.POINTER(C.c_float)),
+        ("tets", C.POINTER(C.c_uint32)),
+        ("tris", C.POINTER(C.c_uint32)),
+        ("edges", C.POINTER(C.c_uint32)),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/pdgb.h declares.
 SIGNATURES = {
     "pdgb_default_params": (None, [C.POINTER(pdgb_params)]),
@@ -200,6 +227,10 @@ SIGNATURES = {
     "pdgb_clear_drag": (C.c_int, [C.c_void_p]),
     "pdgb_set_fixed_bodies": (C.c_int, [C.c_void_p, C.POINTER(pdgb_fixed_body), C.c_int, C.c_float, C.c_float]),
     "pdgb_download_xtilde": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "pdgb_load_body_file": (C.c_int, [C.POINTER(pdgb_body_file), C.POINTER(C.POINTER(pdgb_tet_mesh))]),
+    "pdgb_free_tet_mesh": (None, [C.POINTER(pdgb_tet_mesh)]),
+    "pdgb_surface_triangles": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_int)]),
+    "pdgb_render_surface": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

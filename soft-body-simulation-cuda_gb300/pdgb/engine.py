@@ -134,6 +134,13 @@ class PdSolver:
         N.check(self._lib.pdgb_download_xtilde(self._h, _ptr(XT), N.PDGB_MEM_HOST), "pdgb_download_xtilde")
         return XT
 
+    def render_surface(self, tris_ptr: int, num_tris: int, pos_ptr: int, nor_ptr: int) -> None:
+        """Per-triangle corner positions (float[9 n]) and normals (float[12 n])
+        of the current state into device buffers; tris_ptr: device uint32[3 n]
+        caller vertex ids.  Stream-ordered on the engine's stream."""
+        N.check(self._lib.pdgb_render_surface(self._h, C.c_void_p(tris_ptr), int(num_tris), C.c_void_p(pos_ptr),
+                                              C.c_void_p(nor_ptr)), "pdgb_render_surface")
+
     # -- interactive drag (moreDBC / OffsetX / mouse target of SolverData)
     def set_drag(self, weights: np.ndarray, offsets: np.ndarray | None = None) -> None:
         w = np.ascontiguousarray(weights, dtype=np.float32).reshape(self.num_verts)
