@@ -200,9 +200,9 @@ def cpu_baseline(body, params, steps: int):
     import oracle as O
 
     cores = os.cpu_count() or 1
-    tm = {}
-    O.simulate(body, params, steps, precision=32, nthreads=cores, timing=tm)
-    secs = tm["step_seconds"]
+    r = O.Runner(body, params, precision=32, nthreads=cores)
+    secs = r.run(steps)
+    r.close()
     return {"value": body.num_tets * params.num_iterations * steps / secs, "unit": UNIT, "cores": cores,
             "kind": "port", "seconds": secs,
             "sample": f"{steps} PD step(s) of the full workload ({steps * params.num_iterations} iterations x "
@@ -217,32 +217,44 @@ def run_reference_arm(args, body, params, scale=1.0):
     import oracle as O
 
     cores = os.cpu_count() or 1
-    use_ref = O.reference_available()
+    use_ref = O.reference_available() and not args.port
     kind = "reference" if use_ref else "port"
-    # warm-up steps then timed steps, one PD step per bench step, state carried.
-    X, V = body.X.copy(), np.zeros_like(body.X)
-    t_total = 0.0
-    for k in range(args.warmup + args.steps):
-        if use_ref:
+    # Each bench step is one PD step of the workload; when K full steps would
+    # take longer than the time budget, each bench step runs fewer iterations
+    # (same per-iteration work: every tet, every vertex), so that the whole
+    # run stays within a few minutes.
+    budget_s = 120.0
+    if use_ref:
+        # the reference kernels compiled for the CPU (serial), one call per
+        # step, set-up outside the timed region excluded by timing only the
+        # step call of a one-step run is not possible: time the whole call
+        X, V = body.X.copy(), np.zeros_like(body.X)
+        its = params.num_iterations
+        t_total = 0.0
+        for k in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             X, V, _ = O.reference_simulate(body, params, 1, X=X, V=V)
             dt = time.perf_counter() - t0
-        else:
-            tm = {}
-            X, V, _ = O.simulate(body, params, 1, precision=32, nthreads=cores, X=X, V=V, timing=tm)
-            dt = tm["step_seconds"]
-        if k >= args.warmup:
-            t_total += dt
-    value = body.num_tets * params.num_iterations * args.steps / t_total
-    sample = (f"one PD step ({params.num_iterations} iterations x {body.num_tets} tets) per bench step, "
-              f"{'reference kernels compiled for the CPU (serial)' if use_ref else 'float CPU restatement, OpenMP'}")
+            if k >= args.warmup:
+                t_total += dt
+    else:
+        r = O.Runner(body, params, precision=32, nthreads=cores)
+        t_it = r.run(1, 1)  # one iteration: the per-iteration cost
+        its = max(1, min(params.num_iterations, int(budget_s / max(args.steps * t_it, 1e-9))))
+        r.run(args.warmup, its)
+        t_total = r.run(args.steps, its)
+        r.close()
+    value = body.num_tets * its * args.steps / t_total
+    sample = (f"one PD step of {its} iteration(s) x {body.num_tets} tets per bench step (workload: "
+              f"{params.num_iterations} iterations per step), "
+              f"{'reference kernels compiled for the CPU (serial)' if use_ref else f'float CPU restatement, OpenMP over {cores} threads'}")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": WORKLOAD,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1 if use_ref else cores, "kind": kind,
-                         "sample": sample},
+                         "sample": sample, "seconds": t_total},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -371,10 +383,16 @@ def launches_per_step(info, params) -> int:
     return 2 + params.num_iterations * (2 + 2 * info["levels"])
 
 
+# Default timed steps per workload: about 1.5 s of device time, so that the
+# clock sampler (200 ms period) sees the GPU under load.
+DEFAULT_STEPS = {"c1": 1200, "c2": 1200, "c3": 300, "c4": 60}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=0,
+                    help="timed steps (default: about 1.5 s of device time for the workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pdgb", choices=["pdgb", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
@@ -382,11 +400,15 @@ def main():
     ap.add_argument("--bodies", type=int, default=0, help="override the number of bodies of the batch workload")
     ap.add_argument("--cpu-steps", type=int, default=4, help="PD steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--port", action="store_true", help="reference arm: time the oracle port even where the "
+                    "reference harness is built")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-oracle error report")
     ap.add_argument("--window", type=float, default=20.0, help="arrival window of the serving workload, seconds")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "pdgb":
         args.warmup = 3
+    if args.steps <= 0:
+        args.steps = DEFAULT_STEPS.get(args.workload, 20) if args.impl == "pdgb" else 2
 
     from pdgb import mesh
     from pdgb.engine import SolverParams
@@ -430,6 +452,8 @@ def main():
     dist = init_dist(world)
     from pdgb import PdSolver
 
+    from pdgb import _native as N
+
     eng = PdSolver(body if bodies is None else bodies, params)
     stream = torch.cuda.ExternalStream(eng._lib.pdgb_stream(eng.handle))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
@@ -439,7 +463,8 @@ def main():
             flush.add_(1.0)
 
     eng.prepare()
-    eng.enable_kernel_timing(True)
+    eng.enable_kernel_timing(N.PDGB_TIMING_STEPS)
+    eng.prepare()
     for _ in range(args.warmup):
         eng.update(1)
         flush_l2()
@@ -447,9 +472,9 @@ def main():
     eng.read_timing()  # clear the accumulators
     barrier(dist)
     torch.cuda.synchronize()
-    # Timed region: every step graph is bracketed by CUDA events on the
-    # engine's stream (and each local-step launch inside it); the L2 flush
-    # runs between steps, outside the events.
+    # Timed region: every step graph is bracketed by a pair of CUDA events on
+    # the engine's stream (no host wait between steps); the L2 flush runs
+    # between steps, outside the events.
     with ClockSampler(local) as clocks:
         for k in range(args.steps):
             eng.update(1)
@@ -458,18 +483,26 @@ def main():
     barrier(dist)
     tm = eng.read_timing()
     assert tm["steps"] == args.steps
-    local_ms, local_launches = tm["local_ms"], tm["local_launches"]
     t_local = tm["step_ms"] / 1e3
+    # Kernel pass (not part of the value): the same steps with every
+    # local-step launch bracketed by events inside the graph, for the
+    # roofline of the dominant kernel.
+    eng.enable_kernel_timing(N.PDGB_TIMING_KERNELS)
+    eng.prepare()
+    eng.update(1)
+    eng.read_timing()
+    for k in range(args.steps):
+        eng.update(1)
+        flush_l2()
+    eng.synchronize()
+    tk = eng.read_timing()
+    local_ms, local_launches = tk["local_ms"], tk["local_launches"]
     t_max = reduce_max(dist, t_local)
     tet_iters = reduce_sum(dist, float(body.num_tets * params.num_iterations * args.steps))
     value = tet_iters / t_max
 
     # ---- e2e through the C ABI with pinned host buffers
-    import ctypes as C
-
-    from pdgb import _native as N
-
-    eng.enable_kernel_timing(False)
+    eng.enable_kernel_timing(N.PDGB_TIMING_OFF)
     eng.prepare()
     nv = body.num_verts
     Xh = torch.from_numpy(body.X.copy()).pin_memory()
@@ -529,7 +562,8 @@ def main():
         "data": "synthetic",
         "config": dict(WORKLOAD, parallelism=f"replicas{world}" if world > 1 else "single"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_local<true>",
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "k_local<jacobi_form=%d>" % (1 if params.solver == 0 else 0),
                      "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_local_s * 1e6,
                      "launches": local_launches},
         "cpu_baseline": cpu,

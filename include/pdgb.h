@@ -104,8 +104,8 @@ typedef struct pdgb_perf {
  * stream the engine creates. */
 int pdgb_create(const pdgb_mesh_desc* mesh, const pdgb_params* params, void* stream, pdgb_engine** out);
 
-/* Batch of independent soft bodies advanced together (SURVEY "batching";
- * the reference's own multi-body mode concatenates bodies into one system,
+/* Batch of independent soft bodies advanced together (the reference's own
+ * multi-body mode concatenates bodies into one system,
  * dataLoader.cu:291-378).  Vertices of body b are caller ids
  * sum_{i<b} nv_i .. + nv_b in pdgb_upload_state / pdgb_download_state.  Per
  * step: one local-step launch over the tiles of all bodies and, on the
@@ -205,18 +205,25 @@ int pdgb_last_step_iterations(pdgb_engine* e, int* iterations);
 /* Waits for the engine's stream. */
 int pdgb_synchronize(pdgb_engine* e);
 
-/* Device timing for benchmarks.  When enabled, pdgb_step brackets every
- * step-graph launch and every local-step kernel inside it with CUDA events
- * on the engine's stream, waits for each step and accumulates the elapsed
- * times; pdgb_read_timing returns the sums since the last read and clears
- * them.  Disabled (the default), pdgb_step never waits. */
+/* Device timing for benchmarks (mode, default OFF):
+ *   PDGB_TIMING_STEPS: pdgb_step brackets every step-graph launch with a
+ *     pair of CUDA events on the engine's stream and does not wait;
+ *     pdgb_read_timing waits for the stream and sums the pairs.
+ *   PDGB_TIMING_KERNELS: additionally brackets every local-step kernel
+ *     inside the graph (event nodes, which add a little time to the step)
+ *     and waits for each step.
+ * pdgb_read_timing returns the sums since the last read and clears them.
+ * With timing off pdgb_step never waits. */
+#define PDGB_TIMING_OFF 0
+#define PDGB_TIMING_STEPS 1
+#define PDGB_TIMING_KERNELS 2
 typedef struct pdgb_timing {
     double step_ms;          /* summed device time of the step graphs          */
     long long steps;         /* steps timed                                     */
     double local_ms;         /* summed device time of the local-step launches   */
     long long local_launches;
 } pdgb_timing;
-int pdgb_enable_kernel_timing(pdgb_engine* e, int enable);
+int pdgb_enable_kernel_timing(pdgb_engine* e, int mode);
 int pdgb_read_timing(pdgb_engine* e, pdgb_timing* out);
 
 /* Algorithmic bytes of one local-step launch (inputs read once, outputs

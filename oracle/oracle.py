@@ -60,6 +60,15 @@ def _load_oracle():
         h.orc_simulate_scene.argtypes = [C.c_int, C.c_int, _F32, _F32, _F32, _U32, _F32, _F32, C.c_void_p,
                                          C.POINTER(orc_params), C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                          C.POINTER(orc_scene)]
+        h.orc_runner_create.restype = C.c_void_p
+        h.orc_runner_create.argtypes = [C.c_int, C.c_int, _F32, _F32, _F32, _U32, _F32, _F32, C.c_void_p,
+                                        C.POINTER(orc_params), C.c_int, C.c_int]
+        h.orc_runner_run.restype = C.c_int
+        h.orc_runner_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        h.orc_runner_state.restype = C.c_int
+        h.orc_runner_state.argtypes = [C.c_void_p, _F32, _F32]
+        h.orc_runner_destroy.restype = None
+        h.orc_runner_destroy.argtypes = [C.c_void_p]
         h.orc_rotations.restype = None
         h.orc_rotations.argtypes = [C.c_int, _F64, _F64, C.c_int]
         h.orc_local_rhs.restype = C.c_int
@@ -145,6 +154,45 @@ def reference_simulate(body, params, nsteps: int, X=None, V=None):
     if st != 0:
         raise RuntimeError(f"ref_simulate failed ({st})")
     return Xs.reshape(-1, 3), Vs.reshape(-1, 3), iters[:nsteps]
+
+
+class Runner:
+    """A persistent oracle simulation (set-up once, then timed steps)."""
+
+    def __init__(self, body, params, precision: int = 32, nthreads: int = 0, X=None, V=None):
+        self._h = _load_oracle()
+        X0, tets, mass, mu, dbc = _arr(body)
+        self._keep = (X0, tets, mass, mu, dbc)
+        self.nv, self.nt = len(mass), len(mu)
+        Xs = np.array(X0 if X is None else np.asarray(X, np.float32).reshape(-1), dtype=np.float32)
+        Vs = np.zeros_like(Xs) if V is None else np.array(np.asarray(V, np.float32).reshape(-1), dtype=np.float32)
+        p = _params(params)
+        self._r = self._h.orc_runner_create(self.nv, self.nt, X0, Xs, Vs, tets, mass, mu,
+                                            None if dbc is None else dbc.ctypes.data, C.byref(p), precision,
+                                            nthreads)
+        if not self._r:
+            raise RuntimeError("orc_runner_create failed")
+
+    def run(self, nsteps: int, num_iterations: int = 0) -> float:
+        """Runs nsteps steps; returns their wall time in seconds."""
+        secs = C.c_double(0.0)
+        if self._h.orc_runner_run(self._r, nsteps, num_iterations, None, C.addressof(secs)) != 0:
+            raise RuntimeError("orc_runner_run failed")
+        return secs.value
+
+    def state(self):
+        X = np.empty(3 * self.nv, np.float32)
+        V = np.empty(3 * self.nv, np.float32)
+        self._h.orc_runner_state(self._r, X, V)
+        return X.reshape(-1, 3), V.reshape(-1, 3)
+
+    def close(self):
+        if self._r:
+            self._h.orc_runner_destroy(self._r)
+            self._r = None
+
+    def __del__(self):
+        self.close()
 
 
 def _params(params):

@@ -603,147 +603,196 @@ template <class T> void collide(const std::vector<Fixed<T>>& fb, T mu_t, T mu_n,
     }
 }
 
+// One simulation: set-up (geometry, system, factor) once, then steps.  The
+// state X, V, XTilde and the Cholesky path's prev vector persist across
+// calls of run().
+struct RunnerBase {
+    virtual ~RunnerBase() {}
+    virtual void run(int nsteps, int iters, int* iters_out, double* step_seconds) = 0;
+    virtual void state(float* X, float* V, float* XT) const = 0;
+};
+
+template <class T> struct Runner : RunnerBase {
+    int nv = 0, nt = 0;
+    Sim<T> S;
+    orc_params prm{};
+    bool chol = false;
+    T dt = 0, dt2 = 0, dtInv = 0, dt2Inv = 0, pw = 0;
+    int num_pinned = 0;
+    std::vector<T> X, V, XT, sn, sn_old, b, mdt2s, dragw, dbcx, drag_off;
+    T target[3] = {0, 0, 0};
+    std::vector<Fixed<T>> fixed;
+    T mu_t = 0, mu_n = 0;
+
+    // Returns 0, or -1 (bad mesh) / -2 (factor failed).
+    int setup(int nv_, int nt_, const float* X0, const float* Xin, const float* Vin, const uint32_t* tets,
+              const float* mass, const float* mu, const float* dbc, const orc_params* p, const orc_scene* sc) {
+        nv = nv_;
+        nt = nt_;
+        prm = *p;
+        S.nv = nv; S.nt = nt; S.tets = tets;
+        TetGeom g;
+        if (!tet_geometry(nv, nt, X0, tets, mu, g)) return -1;
+        S.dminv.assign(g.dminv.begin(), g.dminv.end());
+        S.coef.assign(g.coef.begin(), g.coef.end());
+        S.inc = build_incidence(nv, nt, tets);
+        S.P.resize((size_t)nt * 12);
+        dt = (T)p->dt;
+        dt2 = dt * dt;
+        dtInv = (T)1 / dt;
+        dt2Inv = dtInv * dtInv;
+        pw = (T)p->positional_weight;
+        S.mass.resize(nv); S.mdt2.resize(nv); S.dbc.resize(nv); S.x0.resize((size_t)3 * nv);
+        std::vector<double> mdt2d(nv);
+        for (int v = 0; v < nv; ++v) {
+            S.mass[v] = mass[v];
+            S.dbc[v] = dbc ? (T)dbc[v] : (T)0;
+            S.mdt2[v] = (S.mass[v] + S.dbc[v] * pw) / dt2;  // setMDt_2, pdUtil.cu:48
+            mdt2d[v] = (double)S.mdt2[v];
+            for (int d = 0; d < 3; ++d) S.x0[3 * v + d] = X0[3 * v + d];
+        }
+        chol = p->solver == 1;
+        if (chol) {
+            CSR K = assemble_K(nv, nt, tets, g, mdt2d, nullptr);
+            if (!S.chol.factor(K, X0)) return -2;
+        } else {
+            // Jacobi needs only diag(sum_t c_t B_t^T B_t) (pdUtil.cu:21-24)
+            std::vector<double> sd(nv, 0.0);
+            for (int t = 0; t < nt; ++t) {
+                double B[3][4];
+                make_B(&g.dminv[9 * (size_t)t], B);
+                for (int a = 0; a < 4; ++a)
+                    sd[tets[4 * (size_t)t + a]] +=
+                        g.coef[t] * (B[0][a] * B[0][a] + B[1][a] * B[1][a] + B[2][a] * B[2][a]);
+            }
+            S.stiff_diag.assign(sd.begin(), sd.end());
+        }
+        const size_t n3 = (size_t)3 * nv;
+        X.resize(n3); V.resize(n3); XT.resize(n3); sn.resize(n3); sn_old.resize(n3); b.resize(n3);
+        mdt2s.resize(nv); dragw.assign(nv, (T)0); dbcx.assign(n3, (T)0); drag_off.assign(n3, (T)0);
+        S.prev.assign(n3, (T)0);
+        for (size_t i = 0; i < n3; ++i) {
+            X[i] = Xin[i];
+            V[i] = Vin[i];
+            XT[i] = (sc && sc->XT) ? (T)sc->XT[i] : X[i];
+        }
+        for (int v = 0; v < nv; ++v) num_pinned += S.dbc[v] > 0;
+        if (sc && sc->drag_w) {
+            for (int v = 0; v < nv; ++v) dragw[v] = (T)sc->drag_w[v];
+            for (size_t i = 0; i < n3; ++i) drag_off[i] = (T)sc->drag_off[i];
+        }
+        if (sc)
+            for (int d = 0; d < 3; ++d) target[d] = (T)sc->target[d];
+        fixed = fixed_bodies<T>(sc);
+        mu_t = sc ? (T)sc->mu_t : (T)0;
+        mu_n = sc ? (T)sc->mu_n : (T)0;
+        return 0;
+    }
+
+    // nsteps PD steps of `iters` iterations (0: the parameters' count).
+    void run(int nsteps, int iters, int* iters_out, double* step_seconds) override {
+        const int n_it = iters > 0 ? iters : prm.num_iterations;
+        const T g_acc = (T)prm.gravity;
+        const double t_start = now_seconds();
+        for (int step = 0; step < nsteps; ++step) {
+            // prologue: pdSolver.cu:154-163 (gravity, setMDt_2MoreDBC, computeSn)
+            for (int v = 0; v < nv; ++v) {
+                T md = dragw[v];
+                mdt2s[v] = S.dbc[v] == (T)0 ? (md > (T)0 ? (S.mass[v] + md) / dt2 : S.mass[v] / dt2) : S.mdt2[v];
+                if (md > (T)0) {  // dragged: target + offset, also the DBC position
+                    for (int d = 0; d < 3; ++d) {
+                        sn[3 * v + d] = target[d] + drag_off[3 * v + d];
+                        dbcx[3 * v + d] = sn[3 * v + d];
+                    }
+                    continue;
+                }
+                T f1 = -g_acc * S.mass[v];
+                T dt2_m_1 = (T)1 / mdt2s[v];
+                sn[3 * v + 0] = X[3 * v + 0] + dt * V[3 * v + 0] + dt2_m_1 * (T)0;
+                sn[3 * v + 1] = X[3 * v + 1] + dt * V[3 * v + 1] + dt2_m_1 * f1;
+                sn[3 * v + 2] = X[3 * v + 2] + dt * V[3 * v + 2] + dt2_m_1 * (T)0;
+            }
+            sn_old = sn;
+            if (!chol) S.prev = sn;
+            else std::memset(S.prev.data(), 0, std::min((size_t)3 * nv, S.prev.size() * sizeof(T)));  // bytes (pdSolver.cu:162)
+            T err = 1;
+            T omega = 1;
+            int it = 0;
+            for (int i = 0; i < n_it && std::sqrt(err) >= (T)prm.tol; ++i, ++it) {
+                local_rhs<T>(S, sn.data(), sn_old.data(), !chol, b.data(), mdt2s.data());
+                // pinned / dragged RHS overwrite (pdUtil.cu:147-166), run only
+                // when the system has pinned vertices (pdSolver.cu:170)
+                if (num_pinned > 0)
+                    for (int v = 0; v < nv; ++v) {
+                        if (S.dbc[v] > 0)
+                            for (int d = 0; d < 3; ++d) b[3 * v + d] = S.x0[3 * v + d] * (pw * dt2Inv);
+                        else if (dragw[v] > (T)0)
+                            for (int d = 0; d < 3; ++d) b[3 * v + d] = dbcx[3 * v + d] * dragw[v];
+                    }
+                if (chol) {
+                    S.chol.template solve3<T>(b.data(), sn.data());
+                    T acc = 0;
+                    for (size_t k = 0; k < (size_t)3 * nv; ++k) {
+                        T dlt = S.prev[k] - sn[k];
+                        acc += dlt * dlt;
+                    }
+                    err = acc / (T)(3 * nv);
+                    S.prev = sn;
+                } else {
+                    const T rho = (T)prm.rho;
+                    if (i <= 10) omega = 1;
+                    else if (i == 11) omega = (T)2 / ((T)2 - rho * rho);
+                    else omega = (T)4 / ((T)4 - rho * rho * omega);
+#pragma omp parallel for schedule(static)
+                    for (int v = 0; v < nv; ++v) {
+                        T c = mdt2s[v], md = S.stiff_diag[v];
+                        for (int d = 0; d < 3; ++d) {
+                            size_t k = 3 * (size_t)v + d;
+                            // dragged vertices keep the iterate (getErrorKern, pdUtil.cu:200-205)
+                            T nx = dragw[v] > (T)0 ? sn[k] : (b[k] - c * sn[k]) / (c + md) + sn[k];
+                            // 0.9 is a double literal in the reference (pdUtil.cu:221)
+                            nx = (T)(0.9 * (double)(nx - sn[k]) + (double)sn[k]);
+                            nx = (nx - S.prev[k]) * omega + S.prev[k];
+                            S.prev[k] = sn[k];
+                            sn[k] = nx;
+                        }
+                    }
+                }
+            }
+            if (iters_out) iters_out[step] = it;
+            // updateVelPos (pdUtil.cu:180-193), X <- XTilde (pdSolver.cu:227),
+            // fixed-body correction of XTilde and V (pdSolver.cu:228-231)
+            for (int v = 0; v < nv; ++v) {
+                for (int d = 0; d < 3; ++d) {
+                    size_t k = 3 * (size_t)v + d;
+                    V[k] = dragw[v] > (T)0 ? (T)0 : (sn[k] - XT[k]) * dtInv;
+                    XT[k] = sn[k];
+                    X[k] = sn[k];
+                }
+                if (!fixed.empty()) collide<T>(fixed, mu_t, mu_n, &XT[3 * (size_t)v], &V[3 * (size_t)v]);
+            }
+        }
+        if (step_seconds) *step_seconds = now_seconds() - t_start;
+    }
+
+    void state(float* Xo, float* Vo, float* XTo) const override {
+        for (size_t i = 0; i < (size_t)3 * nv; ++i) {
+            if (Xo) Xo[i] = (float)X[i];
+            if (Vo) Vo[i] = (float)V[i];
+            if (XTo) XTo[i] = (float)XT[i];
+        }
+    }
+};
+
 template <class T>
 int simulate(int nv, int nt, const float* X0, float* Xio, float* Vio, const uint32_t* tets, const float* mass,
              const float* mu, const float* dbc, const orc_params* p, int nsteps, int* iters_out, double* step_seconds,
              const orc_scene* sc) {
-    Sim<T> S;
-    S.nv = nv; S.nt = nt; S.tets = tets;
-    TetGeom g;
-    if (!tet_geometry(nv, nt, X0, tets, mu, g)) return -1;
-    S.dminv.assign(g.dminv.begin(), g.dminv.end());
-    S.coef.assign(g.coef.begin(), g.coef.end());
-    S.inc = build_incidence(nv, nt, tets);
-    S.P.resize((size_t)nt * 12);
-    const T dt = (T)p->dt;
-    const T dt2 = dt * dt;
-    const T dtInv = (T)1 / dt;
-    const T dt2Inv = dtInv * dtInv;
-    const T pw = (T)p->positional_weight;
-    S.mass.resize(nv); S.mdt2.resize(nv); S.dbc.resize(nv); S.x0.resize((size_t)3 * nv);
-    std::vector<double> mdt2d(nv);
-    for (int v = 0; v < nv; ++v) {
-        S.mass[v] = mass[v];
-        S.dbc[v] = dbc ? (T)dbc[v] : (T)0;
-        S.mdt2[v] = (S.mass[v] + S.dbc[v] * pw) / dt2;  // setMDt_2, pdUtil.cu:48
-        mdt2d[v] = (double)S.mdt2[v];
-        for (int d = 0; d < 3; ++d) S.x0[3 * v + d] = X0[3 * v + d];
-    }
-    const bool chol = p->solver == 1;
-    if (chol) {
-        CSR K = assemble_K(nv, nt, tets, g, mdt2d, nullptr);
-        if (!S.chol.factor(K, X0)) return -2;
-    } else {
-        // Jacobi needs only diag(sum_t c_t B_t^T B_t) (pdUtil.cu:21-24)
-        std::vector<double> sd(nv, 0.0);
-        for (int t = 0; t < nt; ++t) {
-            double B[3][4];
-            make_B(&g.dminv[9 * (size_t)t], B);
-            for (int a = 0; a < 4; ++a)
-                sd[tets[4 * (size_t)t + a]] += g.coef[t] * (B[0][a] * B[0][a] + B[1][a] * B[1][a] + B[2][a] * B[2][a]);
-        }
-        S.stiff_diag.assign(sd.begin(), sd.end());
-    }
-    std::vector<T> X((size_t)3 * nv), V((size_t)3 * nv), sn((size_t)3 * nv), sn_old((size_t)3 * nv),
-        b((size_t)3 * nv), next((size_t)3 * nv), XT((size_t)3 * nv), mdt2s(nv), dragw(nv, (T)0),
-        dbcx((size_t)3 * nv, (T)0);
-    S.prev.assign((size_t)3 * nv, (T)0);
-    for (size_t i = 0; i < (size_t)3 * nv; ++i) {
-        X[i] = Xio[i];
-        V[i] = Vio[i];
-        XT[i] = (sc && sc->XT) ? (T)sc->XT[i] : X[i];
-    }
-    int num_pinned = 0;
-    for (int v = 0; v < nv; ++v) num_pinned += S.dbc[v] > 0;
-    const bool drag = sc && sc->drag_w;
-    if (drag)
-        for (int v = 0; v < nv; ++v) dragw[v] = (T)sc->drag_w[v];
-    const std::vector<Fixed<T>> fixed = fixed_bodies<T>(sc);
-    const T mu_t = sc ? (T)sc->mu_t : (T)0, mu_n = sc ? (T)sc->mu_n : (T)0;
-    const T g_acc = (T)p->gravity;
-    const double t_start = now_seconds();
-    for (int step = 0; step < nsteps; ++step) {
-        // prologue: pdSolver.cu:154-163 (gravity, setMDt_2MoreDBC, computeSn)
-        for (int v = 0; v < nv; ++v) {
-            T md = dragw[v];
-            mdt2s[v] = S.dbc[v] == (T)0 ? (md > (T)0 ? (S.mass[v] + md) / dt2 : S.mass[v] / dt2) : S.mdt2[v];
-            if (md > (T)0) {  // dragged: target + offset, also the DBC position
-                for (int d = 0; d < 3; ++d) {
-                    sn[3 * v + d] = (T)sc->target[d] + (T)sc->drag_off[3 * v + d];
-                    dbcx[3 * v + d] = sn[3 * v + d];
-                }
-                continue;
-            }
-            T f1 = -g_acc * S.mass[v];
-            T dt2_m_1 = (T)1 / mdt2s[v];
-            sn[3 * v + 0] = X[3 * v + 0] + dt * V[3 * v + 0] + dt2_m_1 * (T)0;
-            sn[3 * v + 1] = X[3 * v + 1] + dt * V[3 * v + 1] + dt2_m_1 * f1;
-            sn[3 * v + 2] = X[3 * v + 2] + dt * V[3 * v + 2] + dt2_m_1 * (T)0;
-        }
-        sn_old = sn;
-        if (!chol) S.prev = sn;
-        else std::memset(S.prev.data(), 0, std::min((size_t)3 * nv, S.prev.size() * sizeof(T)));  // bytes (pdSolver.cu:162)
-        T err = 1;
-        T omega = 1;
-        int it = 0;
-        for (int i = 0; i < p->num_iterations && std::sqrt(err) >= (T)p->tol; ++i, ++it) {
-            local_rhs<T>(S, sn.data(), sn_old.data(), !chol, b.data(), mdt2s.data());
-            // pinned / dragged RHS overwrite (pdUtil.cu:147-166), run only
-            // when the system has pinned vertices (pdSolver.cu:170)
-            if (num_pinned > 0)
-                for (int v = 0; v < nv; ++v) {
-                    if (S.dbc[v] > 0)
-                        for (int d = 0; d < 3; ++d) b[3 * v + d] = S.x0[3 * v + d] * (pw * dt2Inv);
-                    else if (dragw[v] > (T)0)
-                        for (int d = 0; d < 3; ++d) b[3 * v + d] = dbcx[3 * v + d] * dragw[v];
-                }
-            if (chol) {
-                S.chol.template solve3<T>(b.data(), sn.data());
-                T acc = 0;
-                for (size_t k = 0; k < (size_t)3 * nv; ++k) {
-                    T dlt = S.prev[k] - sn[k];
-                    acc += dlt * dlt;
-                }
-                err = acc / (T)(3 * nv);
-                S.prev = sn;
-            } else {
-                const T rho = (T)p->rho;
-                if (i <= 10) omega = 1;
-                else if (i == 11) omega = (T)2 / ((T)2 - rho * rho);
-                else omega = (T)4 / ((T)4 - rho * rho * omega);
-#pragma omp parallel for schedule(static)
-                for (int v = 0; v < nv; ++v) {
-                    T c = mdt2s[v], md = S.stiff_diag[v];
-                    for (int d = 0; d < 3; ++d) {
-                        size_t k = 3 * (size_t)v + d;
-                        // dragged vertices keep the iterate (getErrorKern, pdUtil.cu:200-205)
-                        T nx = dragw[v] > (T)0 ? sn[k] : (b[k] - c * sn[k]) / (c + md) + sn[k];
-                        // 0.9 is a double literal in the reference (pdUtil.cu:221)
-                        nx = (T)(0.9 * (double)(nx - sn[k]) + (double)sn[k]);
-                        nx = (nx - S.prev[k]) * omega + S.prev[k];
-                        S.prev[k] = sn[k];
-                        sn[k] = nx;
-                    }
-                }
-            }
-        }
-        if (iters_out) iters_out[step] = it;
-        // updateVelPos (pdUtil.cu:180-193), X <- XTilde (pdSolver.cu:227),
-        // fixed-body correction of XTilde and V (pdSolver.cu:228-231)
-        for (int v = 0; v < nv; ++v) {
-            for (int d = 0; d < 3; ++d) {
-                size_t k = 3 * (size_t)v + d;
-                V[k] = dragw[v] > (T)0 ? (T)0 : (sn[k] - XT[k]) * dtInv;
-                XT[k] = sn[k];
-                X[k] = sn[k];
-            }
-            if (!fixed.empty()) collide<T>(fixed, mu_t, mu_n, &XT[3 * (size_t)v], &V[3 * (size_t)v]);
-        }
-    }
-    if (step_seconds) *step_seconds = now_seconds() - t_start;
-    for (size_t i = 0; i < (size_t)3 * nv; ++i) { Xio[i] = (float)X[i]; Vio[i] = (float)V[i]; }
-    if (sc && sc->XT)
-        for (size_t i = 0; i < (size_t)3 * nv; ++i) sc->XT[i] = (float)XT[i];
+    Runner<T> r;
+    const int st = r.setup(nv, nt, X0, Xio, Vio, tets, mass, mu, dbc, p, sc);
+    if (st != 0) return st;
+    r.run(nsteps, 0, iters_out, step_seconds);
+    r.state(Xio, Vio, (sc && sc->XT) ? sc->XT : nullptr);
     return 0;
 }
 
@@ -780,6 +829,47 @@ int orc_simulate_scene(int nv, int nt, const float* X0, float* X, float* V, cons
         return simulate<double>(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nsteps, iters_out, step_seconds, scene);
     return simulate<float>(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nsteps, iters_out, step_seconds, scene);
 }
+
+orc_runner* orc_runner_create(int nv, int nt, const float* X0, const float* X, const float* V, const uint32_t* tets,
+                              const float* mass, const float* mu, const float* dbc, const orc_params* p,
+                              int precision, int nthreads) {
+    if (nv <= 0 || nt <= 0 || !X0 || !X || !V || !tets || !mass || !mu || !p) return nullptr;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    RunnerBase* r = nullptr;
+    int st = 0;
+    if (precision == 64) {
+        auto* q = new Runner<double>();
+        st = q->setup(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nullptr);
+        r = q;
+    } else {
+        auto* q = new Runner<float>();
+        st = q->setup(nv, nt, X0, X, V, tets, mass, mu, dbc, p, nullptr);
+        r = q;
+    }
+    if (st != 0) {
+        delete r;
+        return nullptr;
+    }
+    return reinterpret_cast<orc_runner*>(r);
+}
+
+int orc_runner_run(orc_runner* r, int nsteps, int num_iterations, int* iters_out, double* step_seconds) {
+    if (!r || nsteps < 0) return -1;
+    reinterpret_cast<RunnerBase*>(r)->run(nsteps, num_iterations, iters_out, step_seconds);
+    return 0;
+}
+
+int orc_runner_state(const orc_runner* r, float* X, float* V) {
+    if (!r) return -1;
+    reinterpret_cast<const RunnerBase*>(r)->state(X, V, nullptr);
+    return 0;
+}
+
+void orc_runner_destroy(orc_runner* r) { delete reinterpret_cast<RunnerBase*>(r); }
 
 void orc_rotations(int n, const double* F, double* R, int precision) {
     for (int k = 0; k < n; ++k) {

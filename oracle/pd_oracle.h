@@ -88,6 +88,17 @@ int orc_simulate_scene(int nv, int nt, const float* X0, float* X, float* V,
                        int nsteps, int nthreads, int* iters_out, double* step_seconds,
                        const orc_scene* scene);
 
+/* A persistent simulation for timing: set-up (geometry, system, factor)
+ * once, then steps on demand; the state carries over between runs.
+ * num_iterations > 0 overrides the parameters' count for that run. */
+typedef struct orc_runner orc_runner;
+orc_runner* orc_runner_create(int nv, int nt, const float* X0, const float* X, const float* V,
+                              const uint32_t* tets, const float* mass, const float* mu,
+                              const float* dbc, const orc_params* p, int precision, int nthreads);
+int orc_runner_run(orc_runner* r, int nsteps, int num_iterations, int* iters_out, double* step_seconds);
+int orc_runner_state(const orc_runner* r, float* X, float* V);
+void orc_runner_destroy(orc_runner* r);
+
 /* Closest proper rotation of each 3x3 matrix F (row-major, 9 per item).
  * precision 64: exact; 32: the float McAdams-style SVD.  R row-major. */
 void orc_rotations(int n, const double* F, double* R, int precision);

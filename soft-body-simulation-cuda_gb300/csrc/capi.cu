@@ -77,9 +77,15 @@ struct pdgb_engine {
     // step graph
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    bool timing = false;
+    // timing: PDGB_TIMING_STEPS records a pair of events around every step
+    // graph launch; PDGB_TIMING_KERNELS also brackets every local-step launch
+    // inside the graph and waits for each step
+    int timing_mode = PDGB_TIMING_OFF;
+    bool timing = false;              // graph carries the per-local events
     std::vector<cudaEvent_t> events;  // 2 per local launch
     cudaEvent_t step_ev[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> step_pairs;  // 2 per step, PDGB_TIMING_STEPS
+    size_t step_pairs_used = 0;
     double local_ms_acc = 0.0, step_ms_acc = 0.0;
     long long local_launches = 0, steps_timed = 0;
     // perf
@@ -92,6 +98,7 @@ struct pdgb_engine {
         for (auto ev : events) cudaEventDestroy(ev);
         for (auto ev : step_ev)
             if (ev) cudaEventDestroy(ev);
+        for (auto ev : step_pairs) cudaEventDestroy(ev);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
@@ -591,6 +598,19 @@ int pdgb_step(pdgb_engine* e, int nsteps) {
             PDGB_CUDA_TRY(cudaEventCreate(&e->step_ev[1]));
         }
         for (int k = 0; k < nsteps; ++k) {
+            if (e->timing_mode == PDGB_TIMING_STEPS) {
+                // events only, no wait: pdgb_read_timing sums the pairs
+                while (e->step_pairs.size() < 2 * (e->step_pairs_used + 1)) {
+                    cudaEvent_t ev;
+                    PDGB_CUDA_TRY(cudaEventCreate(&ev));
+                    e->step_pairs.push_back(ev);
+                }
+                cudaEvent_t* pr = &e->step_pairs[2 * e->step_pairs_used++];
+                PDGB_CUDA_TRY(cudaEventRecord(pr[0], e->stream));
+                PDGB_CUDA_TRY(cudaGraphLaunch(e->gexec, e->stream));
+                PDGB_CUDA_TRY(cudaEventRecord(pr[1], e->stream));
+                continue;
+            }
             if (e->timing) PDGB_CUDA_TRY(cudaEventRecord(e->step_ev[0], e->stream));
             PDGB_CUDA_TRY(cudaGraphLaunch(e->gexec, e->stream));
             if (e->timing) {
@@ -903,19 +923,38 @@ int pdgb_synchronize(pdgb_engine* e) {
     return guarded([&] { PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream)); });
 }
 
-int pdgb_enable_kernel_timing(pdgb_engine* e, int enable) {
-    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
-    if ((enable != 0) != e->timing) {
-        e->timing = enable != 0;
-        e->prepared = false;
+int pdgb_enable_kernel_timing(pdgb_engine* e, int mode) {
+    if (!e || mode < PDGB_TIMING_OFF || mode > PDGB_TIMING_KERNELS) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or timing mode");
+        return PDGB_ERR_INVALID_ARGUMENT;
     }
+    const bool kernels = mode == PDGB_TIMING_KERNELS;
+    if (kernels != e->timing) {
+        e->timing = kernels;
+        e->prepared = false;  // the graph gains or loses the per-local events
+    }
+    e->timing_mode = mode;
     e->local_ms_acc = e->step_ms_acc = 0.0;
     e->local_launches = e->steps_timed = 0;
+    e->step_pairs_used = 0;
     return PDGB_OK;
 }
 
 int pdgb_read_timing(pdgb_engine* e, pdgb_timing* out) {
     if (!e || !out) return PDGB_ERR_INVALID_ARGUMENT;
+    if (e->step_pairs_used) {
+        int st = guarded([&] {
+            PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+            for (size_t k = 0; k < e->step_pairs_used; ++k) {
+                float ms = 0.f;
+                PDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e->step_pairs[2 * k], e->step_pairs[2 * k + 1]));
+                e->step_ms_acc += ms;
+            }
+            e->steps_timed += (long long)e->step_pairs_used;
+        });
+        e->step_pairs_used = 0;
+        if (st != PDGB_OK) return st;
+    }
     out->step_ms = e->step_ms_acc;
     out->steps = e->steps_timed;
     out->local_ms = e->local_ms_acc;

@@ -30,6 +30,9 @@ PDGB_ROTATION_QUAT = 0
 PDGB_ROTATION_SVD = 1
 PDGB_ORDER_AMD = 0
 PDGB_ORDER_ND = 1
+PDGB_TIMING_OFF = 0
+PDGB_TIMING_STEPS = 1
+PDGB_TIMING_KERNELS = 2
 PDGB_FIXED_SPHERE = 0
 PDGB_FIXED_PLANE = 1
 PDGB_FIXED_CYLINDER = 2

@@ -195,8 +195,10 @@ class PdSolver:
         return it.value
 
     # -- measurement hooks
-    def enable_kernel_timing(self, on: bool = True) -> None:
-        N.check(self._lib.pdgb_enable_kernel_timing(self._h, int(bool(on))), "pdgb_enable_kernel_timing")
+    def enable_kernel_timing(self, on=True) -> None:
+        """on: False/0 off, 1 step events only, True/2 step and local-kernel events."""
+        mode = 2 if on is True else int(on)
+        N.check(self._lib.pdgb_enable_kernel_timing(self._h, mode), "pdgb_enable_kernel_timing")
 
     def read_timing(self) -> dict:
         t = N.pdgb_timing()

@@ -181,3 +181,12 @@ def test_kernel_timing_hook_counts_launches():
         assert t["local_launches"] == 21 and t["steps"] == 3
         assert 0 < t["local_ms"] < t["step_ms"]
         assert e.local_step_bytes() == 56.0 * body.num_tets + 36.0 * body.num_verts
+        # step events only: no per-local records, no wait inside pdgb_step
+        e.enable_kernel_timing(1)
+        e.update(4)
+        t = e.read_timing()
+        assert t["steps"] == 4 and t["local_launches"] == 0 and t["step_ms"] > 0
+        assert e.read_timing()["steps"] == 0
+        X, _ = e.download_state()
+    Xo, _, _ = O.simulate(body, params, 7, 64)
+    assert rel_l2(X, Xo) < TOL
