@@ -105,8 +105,13 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
     }
 }
 
+// Resident CTAs per SM the register allocation of the local step aims for.
+#ifndef PDGB_LOCAL_MIN_BLOCKS
+#define PDGB_LOCAL_MIN_BLOCKS 1
+#endif
+
 template <bool kJacobiForm, int kRotation>
-__global__ void __launch_bounds__(kLocalThreads) k_local(LocalArgs a) {
+__global__ void __launch_bounds__(kLocalThreads, PDGB_LOCAL_MIN_BLOCKS) k_local(LocalArgs a) {
     // corner-major slots: corner c of local tet lt lives at c * kTileTets + lt
     __shared__ float4 slot[4 * kTileTets];
     if (a.done && *a.done) return;
@@ -129,8 +134,22 @@ void launch_local_multi(const LocalArgs* req, const int2* list, const int* count
     if (grid > 0) k_local_multi<true><<<grid, kLocalThreads, 0, s>>>(req, list, count);
 }
 
+// The local step is limited by registers and shared memory per SM: ask for
+// the largest shared-memory carveout once per kernel.
+template <class K> void max_smem_carveout(K kernel) {
+    static bool done = false;
+    if (!done) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        done = true;
+    }
+}
+
 void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, int rotation, cudaStream_t s) {
     if (ntiles <= 0) return;
+    max_smem_carveout(k_local<true, PDGB_ROTATION_QUAT>);
+    max_smem_carveout(k_local<false, PDGB_ROTATION_QUAT>);
+    max_smem_carveout(k_local<true, PDGB_ROTATION_SVD>);
+    max_smem_carveout(k_local<false, PDGB_ROTATION_SVD>);
     if (rotation == PDGB_ROTATION_SVD) {
         if (jacobi_form) k_local<true, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, 0, s>>>(a);
         else k_local<false, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, 0, s>>>(a);

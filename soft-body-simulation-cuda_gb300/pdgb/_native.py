@@ -6,9 +6,11 @@ fallback: if the library is missing or cannot load, every entry point raises.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libpdgb.so"
+# PDGB_LIBRARY may name another build of the same library (e.g. a tuning variant).
+_LIB_PATH = Path(os.environ.get("PDGB_LIBRARY") or (Path(__file__).resolve().parent / "_lib" / "libpdgb.so"))
 
 PDGB_OK = 0
 PDGB_ERR_INVALID_ARGUMENT = 1
