@@ -497,6 +497,8 @@ def main():
     eng.synchronize()
     tk = eng.read_timing()
     local_ms, local_launches = tk["local_ms"], tk["local_launches"]
+    solve_ms, solves = tk["solve_ms"], tk["solves"]
+    step_ms_kernel_pass = tk["step_ms"]
     t_max = reduce_max(dist, t_local)
     tet_iters = reduce_sum(dist, float(body.num_tets * params.num_iterations * args.steps))
     value = tet_iters / t_max
@@ -526,6 +528,7 @@ def main():
     finite = bool(torch.isfinite(Xh).all().item())
     eng_info = eng.get_performance_data()
     eng_info["levels"] = eng.solve_levels() if params.solver == 1 else 0
+    solve_bytes = eng.solve_bytes()
     eng.close()
 
     if rank != 0:
@@ -535,6 +538,26 @@ def main():
     avg_local_s = (local_ms / 1e3) / max(local_launches, 1)
     achieved = bytes_per_launch / avg_local_s / 1e9
     traffic = ncu_traffic_per_launch(WORKLOAD["workload"])
+    local_roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                  "traffic": traffic, "peak_kind": peak_kind,
+                  "kernel": "k_local<jacobi_form=%d>" % (1 if params.solver == 0 else 0),
+                  "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_local_s * 1e6,
+                  "launches": local_launches,
+                  "share_of_step": (local_ms / step_ms_kernel_pass) if step_ms_kernel_pass > 0 else None}
+    roofline, kernels = local_roof, {"local": local_roof}
+    if params.solver == 1 and solves > 0 and solve_bytes > 0:
+        avg_solve_s = (solve_ms / 1e3) / solves
+        s_ach = solve_bytes / avg_solve_s / 1e9
+        solve_roof = {"bound": "hbm", "achieved": s_ach, "peak": peak, "unit": "GB/s", "frac": s_ach / peak,
+                      "traffic": None, "peak_kind": peak_kind,
+                      "kernel": "cholesky solve (k_chol_solve_cta, or k_chol_fwd_level/k_chol_bwd_level)",
+                      "bytes_per_launch": solve_bytes, "avg_launch_us": avg_solve_s * 1e6, "launches": solves,
+                      "share_of_step": solve_ms / step_ms_kernel_pass if step_ms_kernel_pass > 0 else None,
+                      "note": "one solve = forward + backward over the supernodal tree; bytes per the scalar "
+                              "factor (8 B per nonzero) plus column pointers and right-hand sides"}
+        kernels["solve"] = solve_roof
+        if solve_ms > local_ms:
+            roofline = solve_roof  # the dominant kernel of the Cholesky step
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(cpu_body, params, args.cpu_steps)
@@ -561,18 +584,14 @@ def main():
         "dtype": "f32",
         "data": "synthetic",
         "config": dict(WORKLOAD, parallelism=f"replicas{world}" if world > 1 else "single"),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "k_local<jacobi_form=%d>" % (1 if params.solver == 0 else 0),
-                     "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_local_s * 1e6,
-                     "launches": local_launches},
+        "roofline": roofline,
+        "kernels": kernels,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
                 "d2h_bytes_per_step": 2 * 3 * 4 * nv},
         "gpu_launches": args.steps * launches_per_step(eng_info, params),
         "clocks": clk,
         "finite": finite,
-        "local_step_share": (local_ms / 1e3) / t_local if t_local > 0 else None,
         "accuracy": acc,
     }
     print(json.dumps(line), flush=True)

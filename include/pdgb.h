@@ -222,6 +222,8 @@ typedef struct pdgb_timing {
     long long steps;         /* steps timed                                     */
     double local_ms;         /* summed device time of the local-step launches   */
     long long local_launches;
+    double solve_ms;         /* Cholesky path: summed device time of the solves */
+    long long solves;
 } pdgb_timing;
 int pdgb_enable_kernel_timing(pdgb_engine* e, int mode);
 int pdgb_read_timing(pdgb_engine* e, pdgb_timing* out);
@@ -229,6 +231,11 @@ int pdgb_read_timing(pdgb_engine* e, pdgb_timing* out);
 /* Algorithmic bytes of one local-step launch (inputs read once, outputs
  * written once; see the roofline section of the design notes). */
 int pdgb_local_step_bytes(pdgb_engine* e, double* bytes);
+/* Algorithmic bytes of one Cholesky solve (forward + backward): factor
+ * values and row indices of the scalar L (8 B per nonzero), column pointers,
+ * and the 3-column right-hand sides; 0 on the Jacobi path or before the
+ * first prepare. */
+int pdgb_solve_bytes(pdgb_engine* e, double* bytes);
 
 int pdgb_destroy(pdgb_engine* e);
 

@@ -86,8 +86,9 @@ struct pdgb_engine {
     cudaEvent_t step_ev[2] = {nullptr, nullptr};
     std::vector<cudaEvent_t> step_pairs;  // 2 per step, PDGB_TIMING_STEPS
     size_t step_pairs_used = 0;
-    double local_ms_acc = 0.0, step_ms_acc = 0.0;
-    long long local_launches = 0, steps_timed = 0;
+    std::vector<cudaEvent_t> solve_events;  // 2 per global solve (Cholesky path)
+    double local_ms_acc = 0.0, step_ms_acc = 0.0, solve_ms_acc = 0.0;
+    long long local_launches = 0, steps_timed = 0, solves = 0;
     // perf
     double prepare_ms = 0.0;
     double steps_run = 0, iters_run = 0;
@@ -99,6 +100,7 @@ struct pdgb_engine {
         for (auto ev : step_ev)
             if (ev) cudaEventDestroy(ev);
         for (auto ev : step_pairs) cudaEventDestroy(ev);
+        for (auto ev : solve_events) cudaEventDestroy(ev);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
@@ -271,7 +273,9 @@ void record_chol_step(pdgb_engine* e) {
         record_local(e, la, false, i);
         if (drag_rhs) launch_drag_rhs(e->nv, cv.sc, e->base.p, e->b.p, &st->done, s);
         if (refine > 0) launch_copy_rhs(e->nv, e->b.p, e->bsave.p, &st->done, s);
+        if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->solve_events[2 * i], s, cudaEventRecordExternal));
         solve(ca);
+        if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->solve_events[2 * i + 1], s, cudaEventRecordExternal));
         for (int r = 0; r < refine; ++r) {
             launch_refine_residual(ra, s);
             solve(cd);
@@ -287,11 +291,12 @@ void build_graph(pdgb_engine* e) {
     destroy_graph(e);
     if (e->timing) {
         const size_t need = 2 * (size_t)e->prm.num_iterations;
-        while (e->events.size() < need) {
-            cudaEvent_t ev;
-            PDGB_CUDA_TRY(cudaEventCreate(&ev));
-            e->events.push_back(ev);
-        }
+        for (auto* vec : {&e->events, &e->solve_events})
+            while (vec->size() < need) {
+                cudaEvent_t ev;
+                PDGB_CUDA_TRY(cudaEventCreate(&ev));
+                vec->push_back(ev);
+            }
     }
     PDGB_CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
     try {
@@ -624,6 +629,11 @@ int pdgb_step(pdgb_engine* e, int nsteps) {
                     PDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e->events[2 * i], e->events[2 * i + 1]));
                     e->local_ms_acc += ms;
                     e->local_launches++;
+                    if (e->prm.solver == PDGB_SOLVER_CHOLESKY) {
+                        PDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e->solve_events[2 * i], e->solve_events[2 * i + 1]));
+                        e->solve_ms_acc += ms;
+                        e->solves++;
+                    }
                 }
             }
         }
@@ -934,8 +944,8 @@ int pdgb_enable_kernel_timing(pdgb_engine* e, int mode) {
         e->prepared = false;  // the graph gains or loses the per-local events
     }
     e->timing_mode = mode;
-    e->local_ms_acc = e->step_ms_acc = 0.0;
-    e->local_launches = e->steps_timed = 0;
+    e->local_ms_acc = e->step_ms_acc = e->solve_ms_acc = 0.0;
+    e->local_launches = e->steps_timed = e->solves = 0;
     e->step_pairs_used = 0;
     return PDGB_OK;
 }
@@ -959,8 +969,10 @@ int pdgb_read_timing(pdgb_engine* e, pdgb_timing* out) {
     out->steps = e->steps_timed;
     out->local_ms = e->local_ms_acc;
     out->local_launches = e->local_launches;
-    e->local_ms_acc = e->step_ms_acc = 0.0;
-    e->local_launches = e->steps_timed = 0;
+    out->solve_ms = e->solve_ms_acc;
+    out->solves = e->solves;
+    e->local_ms_acc = e->step_ms_acc = e->solve_ms_acc = 0.0;
+    e->local_launches = e->steps_timed = e->solves = 0;
     return PDGB_OK;
 }
 
@@ -969,6 +981,18 @@ int pdgb_local_step_bytes(pdgb_engine* e, double* bytes) {
     // per tet: 4 x u32 corner ids + 9 x f32 DmInv + 1 x f32 V0*w = 56 B;
     // per vertex: read q (12 B), read (M/h^2) s (12 B), write b (12 B) = 36 B.
     *bytes = 56.0 * e->nt + 36.0 * e->nv;
+    return PDGB_OK;
+}
+
+int pdgb_solve_bytes(pdgb_engine* e, double* bytes) {
+    if (!e || !bytes) return PDGB_ERR_INVALID_ARGUMENT;
+    *bytes = 0.0;
+    if (e->prm.solver != PDGB_SOLVER_CHOLESKY || e->chol.n != e->nv) return PDGB_OK;
+    // forward + backward: factor values and row indices (4 B + 4 B per
+    // nonzero of the scalar L) and column pointers, plus the 3-column
+    // right-hand sides: read b 12 n, write and read y 24 n, write x 12 n
+    const double n = (double)e->nv, nnz = (double)e->chol.nnz_L;
+    *bytes = 2.0 * (8.0 * nnz + 4.0 * (n + 1.0)) + 48.0 * n;
     return PDGB_OK;
 }
 

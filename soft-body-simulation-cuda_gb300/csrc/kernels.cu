@@ -134,22 +134,8 @@ void launch_local_multi(const LocalArgs* req, const int2* list, const int* count
     if (grid > 0) k_local_multi<true><<<grid, kLocalThreads, 0, s>>>(req, list, count);
 }
 
-// The local step is limited by registers and shared memory per SM: ask for
-// the largest shared-memory carveout once per kernel.
-template <class K> void max_smem_carveout(K kernel) {
-    static bool done = false;
-    if (!done) {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-        done = true;
-    }
-}
-
 void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, int rotation, cudaStream_t s) {
     if (ntiles <= 0) return;
-    max_smem_carveout(k_local<true, PDGB_ROTATION_QUAT>);
-    max_smem_carveout(k_local<false, PDGB_ROTATION_QUAT>);
-    max_smem_carveout(k_local<true, PDGB_ROTATION_SVD>);
-    max_smem_carveout(k_local<false, PDGB_ROTATION_SVD>);
     if (rotation == PDGB_ROTATION_SVD) {
         if (jacobi_form) k_local<true, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, 0, s>>>(a);
         else k_local<false, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, 0, s>>>(a);

@@ -84,6 +84,8 @@ class pdgb_timing(C.Structure):
         ("steps", C.c_longlong),
         ("local_ms", C.c_double),
         ("local_launches", C.c_longlong),
+        ("solve_ms", C.c_double),
+        ("solves", C.c_longlong),
     ]
 
 
@@ -203,6 +205,7 @@ SIGNATURES = {
     "pdgb_enable_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_read_timing": (C.c_int, [C.c_void_p, C.POINTER(pdgb_timing)]),
     "pdgb_local_step_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "pdgb_solve_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "pdgb_destroy": (C.c_int, [C.c_void_p]),
     "pdgb_stream": (C.c_void_p, [C.c_void_p]),
     "pdgb_status_string": (C.c_char_p, [C.c_int]),

@@ -203,11 +203,18 @@ class PdSolver:
     def read_timing(self) -> dict:
         t = N.pdgb_timing()
         N.check(self._lib.pdgb_read_timing(self._h, C.byref(t)), "pdgb_read_timing")
-        return {"step_ms": t.step_ms, "steps": t.steps, "local_ms": t.local_ms, "local_launches": t.local_launches}
+        return {"step_ms": t.step_ms, "steps": t.steps, "local_ms": t.local_ms, "local_launches": t.local_launches,
+                "solve_ms": t.solve_ms, "solves": t.solves}
 
     def local_step_bytes(self) -> float:
         b = C.c_double()
         N.check(self._lib.pdgb_local_step_bytes(self._h, C.byref(b)), "pdgb_local_step_bytes")
+        return b.value
+
+    def solve_bytes(self) -> float:
+        """Algorithmic bytes of one Cholesky solve (0 on the Jacobi path)."""
+        b = C.c_double()
+        N.check(self._lib.pdgb_solve_bytes(self._h, C.byref(b)), "pdgb_solve_bytes")
         return b.value
 
     @property

@@ -107,3 +107,23 @@ def test_fp64_residual_refinement_tightens_the_solve():
         assert rel_l2(X, Xo) < TOL
     assert errs[1] <= errs[0] * 1.05 + 1e-9, errs
     assert max(errs[1:]) <= errs[0] * 1.05 + 1e-9, errs
+
+
+def test_solve_timing_and_bytes():
+    """Kernel timing brackets every global solve of the Cholesky path; the
+    solve's algorithmic bytes follow the factor size."""
+    body = mesh.make_grid_body(6, 6, 6, jitter=0.1, seed=3)
+    params = SolverParams(num_iterations=5, solver=1)
+    with PdSolver(body, params) as e:
+        e.enable_kernel_timing(True)
+        e.update(3)
+        t = e.read_timing()
+        info = e.factor_info()
+        nbytes = e.solve_bytes()
+        X, _ = e.download_state()
+    assert t["solves"] == 15 and t["local_launches"] == 15
+    assert 0 < t["solve_ms"] < t["step_ms"]
+    n = body.num_verts
+    assert nbytes == 2 * (8.0 * info["nnz_L"] + 4.0 * (n + 1)) + 48.0 * n
+    Xo, _, _ = O.simulate(body, params, 3, precision=64)
+    assert rel_l2(X, Xo) < TOL
