@@ -380,7 +380,8 @@ def launches_per_step(info, params) -> int:
     Cholesky epilogue."""
     if params.solver == 0:
         return 1 + 2 * params.num_iterations
-    return 2 + params.num_iterations * (2 + 2 * info["levels"])
+    per_solve = 2 * info["levels"] if info.get("solve_mode") == 3 else 1  # PDGB_SOLVE_LEVELS: per level
+    return 2 + params.num_iterations * (2 + per_solve)
 
 
 # Default timed steps per workload: about 1.5 s of device time, so that the
@@ -400,6 +401,9 @@ def main():
     ap.add_argument("--bodies", type=int, default=0, help="override the number of bodies of the batch workload")
     ap.add_argument("--cpu-steps", type=int, default=4, help="PD steps in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--solve-mode", type=int, default=0, help="Cholesky solve schedule (PDGB_SOLVE_*), 0 = auto")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the engine's autotuner (tile size, solve "
+                    "schedule), which runs before the timed region")
     ap.add_argument("--port", action="store_true", help="reference arm: time the oracle port even where the "
                     "reference harness is built")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-oracle error report")
@@ -455,6 +459,8 @@ def main():
     from pdgb import _native as N
 
     eng = PdSolver(body if bodies is None else bodies, params)
+    if args.solve_mode:
+        eng.set_solve_mode(args.solve_mode)
     stream = torch.cuda.ExternalStream(eng._lib.pdgb_stream(eng.handle))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
@@ -463,6 +469,9 @@ def main():
             flush.add_(1.0)
 
     eng.prepare()
+    tune = None
+    if not args.no_autotune:
+        tune = eng.autotune(steps=3)  # set-up, outside the timed region; the state is restored
     eng.enable_kernel_timing(N.PDGB_TIMING_STEPS)
     eng.prepare()
     for _ in range(args.warmup):
@@ -528,6 +537,7 @@ def main():
     finite = bool(torch.isfinite(Xh).all().item())
     eng_info = eng.get_performance_data()
     eng_info["levels"] = eng.solve_levels() if params.solver == 1 else 0
+    eng_info["solve_mode"] = eng.solve_mode() if params.solver == 1 else 0
     solve_bytes = eng.solve_bytes()
     eng.close()
 
@@ -550,7 +560,8 @@ def main():
         s_ach = solve_bytes / avg_solve_s / 1e9
         solve_roof = {"bound": "hbm", "achieved": s_ach, "peak": peak, "unit": "GB/s", "frac": s_ach / peak,
                       "traffic": None, "peak_kind": peak_kind,
-                      "kernel": "cholesky solve (k_chol_solve_cta, or k_chol_fwd_level/k_chol_bwd_level)",
+                      "kernel": {1: "k_chol_solve_cta", 2: "k_chol_solve_cluster",
+                                 3: "k_chol_fwd_level + k_chol_bwd_level"}.get(eng_info.get("solve_mode"), "solve"),
                       "bytes_per_launch": solve_bytes, "avg_launch_us": avg_solve_s * 1e6, "launches": solves,
                       "share_of_step": solve_ms / step_ms_kernel_pass if step_ms_kernel_pass > 0 else None,
                       "note": "one solve = forward + backward over the supernodal tree; bytes per the scalar "
@@ -586,6 +597,7 @@ def main():
         "config": dict(WORKLOAD, parallelism=f"replicas{world}" if world > 1 else "single"),
         "roofline": roofline,
         "kernels": kernels,
+        "autotune": tune,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
                 "d2h_bytes_per_step": 2 * 3 * 4 * nv},

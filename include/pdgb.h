@@ -273,6 +273,43 @@ int pdgb_set_ordering(pdgb_engine* e, int ordering);
 #define PDGB_ROTATION_SVD 1
 int pdgb_set_rotation(pdgb_engine* e, int rotation);
 
+/* Schedule of the Cholesky solve.  CTA: one CTA per body walks the body's
+ * whole elimination tree (levels separated by block barriers); CLUSTER: one
+ * cluster of 8 CTAs per body (cluster barriers); LEVELS: one launch per
+ * level and direction over the whole GPU (large single systems).  AUTO
+ * picks by size: a batch uses CTA, a single system CLUSTER up to 2^20
+ * stored factor entries and LEVELS above.  LEVELS is not used for batches
+ * (CLUSTER instead).  Takes effect at the next prepare; pdgb_get_solve_mode
+ * returns the schedule in use (AUTO before the first prepare or on the
+ * Jacobi path). */
+#define PDGB_SOLVE_AUTO 0
+#define PDGB_SOLVE_CTA 1
+#define PDGB_SOLVE_CLUSTER 2
+#define PDGB_SOLVE_LEVELS 3
+int pdgb_set_solve_mode(pdgb_engine* e, int mode);
+int pdgb_get_solve_mode(pdgb_engine* e, int* mode);
+
+/* Tiles of the local step: at most max_tets tets each (32..512; 0 = 512).
+ * Smaller tiles give small meshes more CTAs; vertex and tet order are
+ * unchanged, so the state carries over.  Takes effect at the next step. */
+int pdgb_set_tile_size(pdgb_engine* e, int max_tets);
+
+/* Autotuner: times `steps` steps (after one warm-up step) of every
+ * candidate configuration on the engine's own mesh -- tile sizes 512, 256,
+ * 128, 64 and, on the Cholesky path, the solve schedules CTA and CLUSTER
+ * (and LEVELS for a single system) -- keeps the fastest and leaves the
+ * engine prepared with it.  The simulation state is restored after every
+ * trial, so tuning does not advance the simulation.  Waits for the GPU. */
+typedef struct pdgb_tune_report {
+    int tile_tets;       /* chosen most tets per tile                        */
+    int solve_mode;      /* chosen PDGB_SOLVE_* (AUTO on the Jacobi path)    */
+    int candidates;      /* configurations timed                             */
+    int reserved;
+    double best_ms;      /* device time per step, chosen configuration       */
+    double default_ms;   /* device time per step before tuning               */
+} pdgb_tune_report;
+int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* report);
+
 /* Host-only check of the Cholesky factor for a mesh (no GPU needed): builds
  * the system for params (dt, pin weight), orders and factors it, and applies
  * the factor on the host exactly as the GPU solve does (double):

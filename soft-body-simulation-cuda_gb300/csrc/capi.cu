@@ -63,7 +63,8 @@ struct pdgb_engine {
     DBuf<int> k_rowptr, k_colind;  // FP64 K for refinement residuals
     DBuf<double> k_val;
     DBuf<float4> bsave, dx;
-    bool cta_solve = false;  // whole solve in one CTA (small systems)
+    int solve_req = PDGB_SOLVE_AUTO;  // requested solve schedule
+    int solve_mode = PDGB_SOLVE_LEVELS;  // schedule in use (decided at prepare)
     double factor_ms = 0.0;
     // scene terms: drag and fixed rigid bodies
     bool drag_on = false;
@@ -266,7 +267,8 @@ void record_chol_step(pdgb_engine* e) {
     RefineArgs ra{e->nv, e->k_rowptr.p, e->k_colind.p, e->k_val.p, e->bsave.p, e->sn.p, e->b.p, e->y.p,
                   e->dx.p, e->sn.p, &st->done};
     auto solve = [&](const CholArgs& args) {
-        if (e->cta_solve) launch_chol_solve_cta(args, e->nbodies, s);
+        if (e->solve_mode == PDGB_SOLVE_CTA) launch_chol_solve_cta(args, e->nbodies, s);
+        else if (e->solve_mode == PDGB_SOLVE_CLUSTER) launch_chol_solve_cluster(args, e->nbodies, s);
         else launch_chol_solve_levels(args, e->chol.levels, s);
     };
     for (int i = 0; i < n; ++i) {
@@ -348,10 +350,25 @@ SparseSym engine_system(const HostLayout& L) {
     return assemble_system(L.nv, L.nt, L.tets_int.data(), L.dminv_d.data(), L.coef_d.data(), mdt2);
 }
 
+// Solve schedule: the requested one, or by size.  A single CTA or one
+// cluster per body walks a body's whole tree when the factor is small (the
+// solve is then bound by the tree depth, not by bandwidth, and launches
+// would dominate); batches always run one CTA or cluster per body.
+int choose_solve_mode(const pdgb_engine* e) {
+    const bool small = e->chol.mval.size() <= kCtaSolveMaxEntries;
+    int m = e->solve_req;
+    if (m == PDGB_SOLVE_LEVELS && e->nbodies > 1) m = PDGB_SOLVE_CLUSTER;  // levels interleave bodies
+    if (m != PDGB_SOLVE_AUTO) return m;
+    if (e->nbodies > 1) return PDGB_SOLVE_CTA;
+    return small ? PDGB_SOLVE_CLUSTER : PDGB_SOLVE_LEVELS;
+}
+
 void prepare_cholesky(pdgb_engine* e) {
     if (e->chol_ordering == e->ordering && e->chol_dt == e->prm.dt && e->chol_pw == e->prm.positional_weight &&
-        e->chol.n == e->nv)
+        e->chol.n == e->nv) {
+        e->solve_mode = choose_solve_mode(e);
         return;  // the system matrix depends only on the mesh, dt and the pin weight
+    }
     auto t0 = std::chrono::steady_clock::now();
     SparseSym K;
     if (e->nbodies == 1) K = engine_system(e->L);
@@ -393,7 +410,7 @@ void prepare_cholesky(pdgb_engine* e) {
     // A single CTA walks a body's whole tree when the factor is small (the
     // solve is then bound by the tree depth, not by bandwidth, and launches
     // would dominate); batches of bodies always run one CTA per body.
-    e->cta_solve = e->nbodies > 1 || f.mval.size() <= kCtaSolveMaxEntries;
+    e->solve_mode = choose_solve_mode(e);
     e->chol_ordering = e->ordering;
     e->chol_dt = e->prm.dt;
     e->chol_pw = e->prm.positional_weight;
@@ -683,6 +700,144 @@ int pdgb_set_rotation(pdgb_engine* e, int rotation) {
         e->rotation = rotation;
         e->prepared = false;
     }
+    return PDGB_OK;
+}
+
+namespace {
+void upload_tiles(pdgb_engine* e) {
+    const HostLayout& L = e->L;
+    cudaStream_t s = e->stream;
+    e->inc_ent.upload(L.inc_ent, s);
+    e->inc_end.upload(L.inc_end, s);
+    e->tile_tet_ptr.upload(L.tile_tet_ptr, s);
+    e->tile_vptr.upload(L.tile_vptr, s);
+    e->tile_verts.upload(L.tile_verts, s);
+}
+
+void set_tile_cap(pdgb_engine* e, int cap) {
+    if (cap == e->L.tile_cap) return;
+    PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));  // no step in flight reads the old tiles
+    build_tiles(e->L, e->has_dbc ? e->dbc.data() : nullptr, cap);
+    upload_tiles(e);
+    PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    e->prepared = false;
+}
+
+// Device time of `steps` steps of the current configuration (prepared),
+// one warm-up step first.
+double time_steps(pdgb_engine* e, int steps) {
+    if (!e->prepared) prepare(e);
+    cudaEvent_t ev[2];
+    PDGB_CUDA_TRY(cudaEventCreate(&ev[0]));
+    PDGB_CUDA_TRY(cudaEventCreate(&ev[1]));
+    float ms = 0.f;
+    try {
+        PDGB_CUDA_TRY(cudaGraphLaunch(e->gexec, e->stream));
+        PDGB_CUDA_TRY(cudaEventRecord(ev[0], e->stream));
+        for (int k = 0; k < steps; ++k) PDGB_CUDA_TRY(cudaGraphLaunch(e->gexec, e->stream));
+        PDGB_CUDA_TRY(cudaEventRecord(ev[1], e->stream));
+        PDGB_CUDA_TRY(cudaEventSynchronize(ev[1]));
+        PDGB_CUDA_TRY(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    } catch (...) {
+        cudaEventDestroy(ev[0]);
+        cudaEventDestroy(ev[1]);
+        throw;
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    return (double)ms / std::max(steps, 1);
+}
+}  // namespace
+
+int pdgb_set_tile_size(pdgb_engine* e, int max_tets) {
+    if (!e || max_tets < 0 || (max_tets > 0 && (max_tets < 32 || max_tets > kTileTets))) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or tile size (32..512, 0 = default)");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] { set_tile_cap(e, max_tets ? max_tets : kTileTets); });
+}
+
+int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
+    if (!e || steps < 1 || steps > 1000) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or step count (1..1000)");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        if (!e->prepared) prepare(e);
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        // the simulation state is saved and restored around every trial
+        const size_t nv = (size_t)e->nv;
+        DBuf<float4> save;
+        save.alloc(4 * nv);
+        float4* keep[4] = {e->x.p, e->v.p, e->prev.p, e->xt.p};
+        auto copy_state = [&](bool restore) {
+            for (int k = 0; k < 4; ++k) {
+                if (!keep[k]) continue;
+                float4* a = save.p + k * nv;
+                PDGB_CUDA_TRY(cudaMemcpyAsync(restore ? keep[k] : a, restore ? a : keep[k], nv * sizeof(float4),
+                                              cudaMemcpyDeviceToDevice, e->stream));
+            }
+            PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        };
+        copy_state(false);
+        const int cap0 = e->L.tile_cap, req0 = e->solve_req;
+        const double t0 = time_steps(e, steps);
+        copy_state(true);
+        std::vector<int> caps = {kTileTets, kTileTets / 2, kTileTets / 4, kTileTets / 8};
+        std::vector<int> modes = {e->solve_req};
+        if (e->prm.solver == PDGB_SOLVER_CHOLESKY) {
+            modes = {PDGB_SOLVE_CTA, PDGB_SOLVE_CLUSTER};
+            if (e->nbodies == 1) modes.push_back(PDGB_SOLVE_LEVELS);
+        }
+        double best = t0;
+        int best_cap = cap0, best_mode = req0, tried = 1;
+        for (int cap : caps)
+            for (int mode : modes) {
+                set_tile_cap(e, cap);
+                if (mode != e->solve_req) {
+                    e->solve_req = mode;
+                    e->prepared = false;
+                }
+                const double t = time_steps(e, steps);
+                copy_state(true);
+                ++tried;
+                if (t < best) {
+                    best = t;
+                    best_cap = cap;
+                    best_mode = mode;
+                }
+            }
+        set_tile_cap(e, best_cap);
+        e->solve_req = best_mode;
+        e->prepared = false;
+        prepare(e);
+        copy_state(true);
+        if (rep) {
+            rep->tile_tets = best_cap;
+            rep->solve_mode = e->prm.solver == PDGB_SOLVER_CHOLESKY ? e->solve_mode : PDGB_SOLVE_AUTO;
+            rep->candidates = tried;
+            rep->reserved = 0;
+            rep->best_ms = best;
+            rep->default_ms = t0;
+        }
+    });
+}
+
+int pdgb_set_solve_mode(pdgb_engine* e, int mode) {
+    if (!e || mode < PDGB_SOLVE_AUTO || mode > PDGB_SOLVE_LEVELS) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or solve mode");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (mode != e->solve_req) {
+        e->solve_req = mode;
+        e->prepared = false;
+    }
+    return PDGB_OK;
+}
+
+int pdgb_get_solve_mode(pdgb_engine* e, int* mode) {
+    if (!e || !mode) return PDGB_ERR_INVALID_ARGUMENT;
+    *mode = e->prm.solver == PDGB_SOLVER_CHOLESKY && e->prepared ? e->solve_mode : PDGB_SOLVE_AUTO;
     return PDGB_OK;
 }
 

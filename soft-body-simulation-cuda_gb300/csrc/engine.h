@@ -68,6 +68,7 @@ template <class T> struct DBuf {
 // engine's internal (Morton) vertex and tet order.
 struct HostLayout {
     int nv = 0, nt = 0, nt_pad = 0, ntiles = 0;
+    int tile_cap = 0;         // most tets per tile of the current cut
     std::vector<int> vperm;   // internal vertex -> caller vertex
     std::vector<int> viperm;  // caller vertex -> internal vertex
     std::vector<int> tperm;   // internal tet -> caller tet
@@ -100,7 +101,11 @@ struct HostLayout {
 // contiguous.
 void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const float* mass, const float* mu,
                   const float* dbc, const pdgb_params& prm, HostLayout& L, int nbodies = 1,
-                  const int* body_vstart = nullptr);
+                  const int* body_vstart = nullptr, int max_tile_tets = kTileTets);
+
+// Re-cuts the tiles of a built layout with at most max_tile_tets tets each
+// (vertex and tet orders unchanged).  dbc: caller-order pin flags or null.
+void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets);
 
 // Recomputes the per-vertex coefficients that depend on dt / pin weight.
 void build_vertex_coefficients(const float* mass, const float* dbc, const pdgb_params& prm, HostLayout& L);

@@ -68,8 +68,74 @@ std::vector<float> chebyshev_omegas(int n, float rho) {
     return w;
 }
 
+// Tiles: greedy runs of the Morton-ordered tets, cut at max_tile_tets tets
+// (at most kTileTets), when the patch would exceed kMaxPatch vertices, or
+// at a body boundary.  Each tile gets its sorted vertex patch (pinned bit
+// from the caller-order pin flags) and its incidence lists.
+void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
+    const int nv = L.nv, nt = L.nt, nbodies = L.nbodies;
+    const int cap = max_tile_tets > 0 ? std::min(max_tile_tets, kTileTets) : kTileTets;
+    L.tile_cap = cap;
+    L.tile_tet_ptr.assign(1, 0);
+    L.tile_vptr.assign(1, 0);
+    L.tile_verts.clear();
+    L.inc_end.clear();
+    L.inc_ent.assign((size_t)4 * nt, 0);
+    std::vector<int> mark(nv, -1), loc(nv, 0), cnt;
+    std::vector<int> patch;
+    patch.reserve(kMaxPatch);
+    int tile = 0, start = 0;
+    int body_cursor = 0, next_body_start = nbodies > 1 ? L.body_itstart[1] : nt;
+    auto close_tile = [&](int end) {
+        std::sort(patch.begin(), patch.end());
+        const int np = (int)patch.size();
+        for (int k = 0; k < np; ++k) loc[patch[k]] = k;
+        // incidence lists in patch order
+        cnt.assign(np + 1, 0);
+        for (int i = start; i < end; ++i)
+            for (int c = 0; c < 4; ++c) cnt[loc[L.tets_int[4 * (size_t)i + c]] + 1]++;
+        for (int k = 0; k < np; ++k) cnt[k + 1] += cnt[k];
+        for (int k = 0; k < np; ++k) L.inc_end.push_back((uint16_t)cnt[k + 1]);
+        for (int i = start; i < end; ++i)
+            for (int c = 0; c < 4; ++c) {
+                const int k = loc[L.tets_int[4 * (size_t)i + c]];
+                L.inc_ent[4 * (size_t)start + cnt[k]++] = (uint16_t)(c * kTileTets + (i - start));
+            }
+        for (int v : patch) {
+            const int o = L.vperm[v];
+            const bool pinned = dbc && dbc[o] > 0.f;
+            L.tile_verts.push_back((uint32_t)v | (pinned ? kPinnedBit : 0u));
+        }
+        L.tile_vptr.push_back((int)L.tile_verts.size());
+        L.tile_tet_ptr.push_back(end);
+        patch.clear();
+        ++tile;
+        start = end;
+    };
+    for (int i = 0; i < nt; ++i) {
+        const uint32_t* id = &L.tets_int[4 * (size_t)i];
+        int fresh = 0;
+        for (int k = 0; k < 4; ++k) {
+            bool dup = mark[id[k]] == tile;
+            for (int j = 0; j < k; ++j) dup = dup || id[j] == id[k];
+            fresh += !dup;
+        }
+        const bool new_body = i > start && i == next_body_start;
+        if (i - start == cap || (int)patch.size() + fresh > kMaxPatch || new_body) close_tile(i);
+        while (i >= next_body_start && body_cursor < nbodies) next_body_start = L.body_itstart[++body_cursor];
+        for (int k = 0; k < 4; ++k)
+            if (mark[id[k]] != tile) {
+                mark[id[k]] = tile;
+                patch.push_back((int)id[k]);
+            }
+    }
+    close_tile(nt);
+    L.ntiles = tile;
+}
+
 void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const float* mass, const float* mu,
-                  const float* dbc, const pdgb_params& prm, HostLayout& L, int nbodies, const int* body_vstart) {
+                  const float* dbc, const pdgb_params& prm, HostLayout& L, int nbodies, const int* body_vstart,
+                  int max_tile_tets) {
     if (nv <= 0 || nt <= 0) throw Error{PDGB_ERR_INVALID_ARGUMENT, "num_verts and num_tets must be positive"};
     for (size_t i = 0; i < (size_t)4 * nt; ++i)
         if (tets[i] >= (uint32_t)nv)
@@ -166,63 +232,7 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
         L.coef_d[i] = coef;
         L.geo[(size_t)9 * L.nt_pad + i] = (float)coef;
     }
-    // ---- tiles: greedy runs of Morton-ordered tets, cut at kTileTets tets or
-    // when the patch would exceed kMaxPatch vertices.
-    L.tile_tet_ptr.assign(1, 0);
-    L.tile_vptr.assign(1, 0);
-    L.tile_verts.clear();
-    L.inc_end.clear();
-    L.inc_ent.assign((size_t)4 * nt, 0);
-    std::vector<int> mark(nv, -1), loc(nv, 0), cnt;
-    std::vector<int> patch;
-    patch.reserve(kMaxPatch);
-    int tile = 0, start = 0;
-    int body_cursor = 0, next_body_start = nbodies > 1 ? L.body_itstart[1] : nt;
-    auto close_tile = [&](int end) {
-        std::sort(patch.begin(), patch.end());
-        const int np = (int)patch.size();
-        for (int k = 0; k < np; ++k) loc[patch[k]] = k;
-        // incidence lists in patch order
-        cnt.assign(np + 1, 0);
-        for (int i = start; i < end; ++i)
-            for (int c = 0; c < 4; ++c) cnt[loc[L.tets_int[4 * (size_t)i + c]] + 1]++;
-        for (int k = 0; k < np; ++k) cnt[k + 1] += cnt[k];
-        for (int k = 0; k < np; ++k) L.inc_end.push_back((uint16_t)cnt[k + 1]);
-        for (int i = start; i < end; ++i)
-            for (int c = 0; c < 4; ++c) {
-                const int k = loc[L.tets_int[4 * (size_t)i + c]];
-                L.inc_ent[4 * (size_t)start + cnt[k]++] = (uint16_t)(c * kTileTets + (i - start));
-            }
-        for (int v : patch) {
-            const int o = L.vperm[v];
-            const bool pinned = dbc && dbc[o] > 0.f;
-            L.tile_verts.push_back((uint32_t)v | (pinned ? kPinnedBit : 0u));
-        }
-        L.tile_vptr.push_back((int)L.tile_verts.size());
-        L.tile_tet_ptr.push_back(end);
-        patch.clear();
-        ++tile;
-        start = end;
-    };
-    for (int i = 0; i < nt; ++i) {
-        const uint32_t* id = &L.tets_int[4 * (size_t)i];
-        int fresh = 0;
-        for (int k = 0; k < 4; ++k) {
-            bool dup = mark[id[k]] == tile;
-            for (int j = 0; j < k; ++j) dup = dup || id[j] == id[k];
-            fresh += !dup;
-        }
-        const bool new_body = i > start && i == next_body_start;
-        if (i - start == kTileTets || (int)patch.size() + fresh > kMaxPatch || new_body) close_tile(i);
-        while (i >= next_body_start && body_cursor < nbodies) next_body_start = L.body_itstart[++body_cursor];
-        for (int k = 0; k < 4; ++k)
-            if (mark[id[k]] != tile) {
-                mark[id[k]] = tile;
-                patch.push_back((int)id[k]);
-            }
-    }
-    close_tile(nt);
-    L.ntiles = tile;
+    build_tiles(L, dbc, max_tile_tets);
     // ---- rest positions (internal order)
     L.x0.resize(nv);
     for (int i = 0; i < nv; ++i) {

@@ -11,6 +11,8 @@
 #include "solve.h"
 #include "scene.cuh"
 
+#include <cooperative_groups.h>
+
 namespace pdgb {
 
 // Forward warp item {moff, roff, m, k, r0, c0, c1}: lane = row r0 + lane of
@@ -152,6 +154,42 @@ __global__ void __launch_bounds__(kCtaSolveThreads) k_chol_solve_cta(CholArgs a)
 
 void launch_chol_solve_cta(const CholArgs& a, int nbodies, cudaStream_t s) {
     if (nbodies > 0) k_chol_solve_cta<<<nbodies, kCtaSolveThreads, 0, s>>>(a);
+}
+
+// ---- one body per thread-block cluster: the cluster's warps stride over
+// the items of a level, with a cluster barrier between levels.  The barrier
+// (arrive with release, wait with acquire semantics at cluster scope) makes
+// the level's global writes and atomics of every CTA of the cluster visible
+// to all of them.  All CTAs of a cluster run the same level loops, so every
+// thread arrives at every barrier; the hardware co-schedules the cluster.
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterSolveThreads)
+    k_chol_solve_cluster(CholArgs a) {
+    __shared__ float4 stage[kClusterSolveThreads / 32][32];
+    if (a.done && *a.done) return;  // the flag is fixed for the kernel: uniform over the cluster
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    constexpr int kWarps = kClusterSolveThreads / 32;
+    constexpr int kStride = kWarps * kClusterCtas;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gw = (int)cl.block_rank() * kWarps + warp;
+    const int body = __ldg(&a.body_order[blockIdx.x / kClusterCtas]);
+    const int L0 = __ldg(&a.body_level[body]), L1 = __ldg(&a.body_level[body + 1]);
+    for (int L = L0; L < L1; ++L) {
+        const int4 lv = __ldg(&a.levels[L]);
+        for (int it = lv.x + gw; it < lv.y; it += kStride)
+            fwd_warp_item(a, a.fwd_items + (size_t)kItemInts * it, stage[warp], lane);
+        cl.sync();
+    }
+    for (int L = L1 - 1; L >= L0; --L) {
+        const int4 lv = __ldg(&a.levels[L]);
+        for (int it = lv.z + gw; it < lv.w; it += kStride)
+            bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * it, stage[warp], lane);
+        cl.sync();
+    }
+}
+
+void launch_chol_solve_cluster(const CholArgs& a, int nbodies, cudaStream_t s) {
+    if (nbodies > 0) k_chol_solve_cluster<<<nbodies * kClusterCtas, kClusterSolveThreads, 0, s>>>(a);
 }
 
 // Cholesky-path vertex kernel after each solve (new positions in sn, written

@@ -13,6 +13,8 @@ namespace pdgb {
 
 constexpr int kLevelThreads = 128;     // per-level launches: 4 warps, one warp item each
 constexpr int kCtaSolveThreads = 1024; // whole-solve-in-one-CTA kernel: 32 warps
+constexpr int kClusterCtas = 8;           // CTAs per body in the cluster solve
+constexpr int kClusterSolveThreads = 512; // per CTA of the cluster solve: 16 warps
 
 struct CholArgs {
     const int* fwd_items;  // kItemInts per item
@@ -59,6 +61,9 @@ void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& 
 // The whole solve of one body in one CTA, levels separated by
 // __syncthreads; one CTA per body (small systems and batches of bodies).
 void launch_chol_solve_cta(const CholArgs& a, int nbodies, cudaStream_t s);
+// The whole solve of one body in one thread-block cluster of kClusterCtas
+// CTAs, levels separated by cluster barriers; one cluster per body.
+void launch_chol_solve_cluster(const CholArgs& a, int nbodies, cudaStream_t s);
 // FP64-residual iterative refinement of the global solve:
 //   bsave = b (before the solve destroys it);
 //   r = bsave - K x0 in double (K: FP64 CSR over vertex ids), b = r, y = 0;

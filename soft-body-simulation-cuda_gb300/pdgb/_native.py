@@ -32,6 +32,10 @@ PDGB_ROTATION_QUAT = 0
 PDGB_ROTATION_SVD = 1
 PDGB_ORDER_AMD = 0
 PDGB_ORDER_ND = 1
+PDGB_SOLVE_AUTO = 0
+PDGB_SOLVE_CTA = 1
+PDGB_SOLVE_CLUSTER = 2
+PDGB_SOLVE_LEVELS = 3
 PDGB_TIMING_OFF = 0
 PDGB_TIMING_STEPS = 1
 PDGB_TIMING_KERNELS = 2
@@ -184,6 +188,17 @@ class pdgb_tet_mesh(C.Structure):
     ]
 
 
+class pdgb_tune_report(C.Structure):
+    _fields_ = [
+        ("tile_tets", C.c_int),
+        ("solve_mode", C.c_int),
+        ("candidates", C.c_int),
+        ("reserved", C.c_int),
+        ("best_ms", C.c_double),
+        ("default_ms", C.c_double),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/pdgb.h declares.
 SIGNATURES = {
     "pdgb_default_params": (None, [C.POINTER(pdgb_params)]),
@@ -206,6 +221,10 @@ SIGNATURES = {
     "pdgb_read_timing": (C.c_int, [C.c_void_p, C.POINTER(pdgb_timing)]),
     "pdgb_local_step_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "pdgb_solve_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "pdgb_set_solve_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_set_tile_size": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(pdgb_tune_report)]),
+    "pdgb_get_solve_mode": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "pdgb_destroy": (C.c_int, [C.c_void_p]),
     "pdgb_stream": (C.c_void_p, [C.c_void_p]),
     "pdgb_status_string": (C.c_char_p, [C.c_int]),

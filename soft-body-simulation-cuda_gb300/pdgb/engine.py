@@ -211,6 +211,26 @@ class PdSolver:
         N.check(self._lib.pdgb_local_step_bytes(self._h, C.byref(b)), "pdgb_local_step_bytes")
         return b.value
 
+    def set_solve_mode(self, mode: int) -> None:
+        """PDGB_SOLVE_AUTO / CTA / CLUSTER / LEVELS (schedule of the Cholesky solve)."""
+        N.check(self._lib.pdgb_set_solve_mode(self._h, int(mode)), "pdgb_set_solve_mode")
+
+    def set_tile_size(self, max_tets: int) -> None:
+        """Most tets per local-step tile (32..512; 0 = 512)."""
+        N.check(self._lib.pdgb_set_tile_size(self._h, int(max_tets)), "pdgb_set_tile_size")
+
+    def autotune(self, steps: int = 5) -> dict:
+        """Times tile sizes and solve schedules on this mesh, keeps the fastest
+        (state restored; the simulation does not advance)."""
+        r = N.pdgb_tune_report()
+        N.check(self._lib.pdgb_autotune(self._h, int(steps), C.byref(r)), "pdgb_autotune")
+        return {k: getattr(r, k) for k, _ in r._fields_ if k != "reserved"}
+
+    def solve_mode(self) -> int:
+        m = C.c_int()
+        N.check(self._lib.pdgb_get_solve_mode(self._h, C.byref(m)), "pdgb_get_solve_mode")
+        return m.value
+
     def solve_bytes(self) -> float:
         """Algorithmic bytes of one Cholesky solve (0 on the Jacobi path)."""
         b = C.c_double()

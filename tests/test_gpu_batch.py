@@ -54,3 +54,25 @@ def test_batch_uneven_sizes_cholesky():
             Xb, _ = e.download_body(b)
             Xo, _, _ = O.simulate(body, params, 4, precision=64)
             assert rel_l2(Xb, Xo) < TOL, b
+
+
+def test_batch_cluster_schedule():
+    """One cluster of CTAs per body (PDGB_SOLVE_CLUSTER) gives the same bodies
+    as one CTA per body."""
+    from pdgb import _native as N
+
+    bodies = mesh.batch_c4(nbodies=7, seed=17, lo=3, hi=9)
+    params = SolverParams(num_iterations=10, solver=1)
+    out = {}
+    for mode in (N.PDGB_SOLVE_CTA, N.PDGB_SOLVE_CLUSTER, N.PDGB_SOLVE_LEVELS):
+        with PdSolver(bodies, params) as e:
+            e.set_solve_mode(mode)
+            e.update(4)
+            out[mode] = e.download_state()[0]
+            # batches never use the per-level schedule
+            assert e.solve_mode() == (N.PDGB_SOLVE_CLUSTER if mode == N.PDGB_SOLVE_LEVELS else mode)
+    assert rel_l2(out[N.PDGB_SOLVE_CLUSTER], out[N.PDGB_SOLVE_CTA]) < 1e-5
+    for b, body in enumerate(bodies):
+        Xo, _, _ = O.simulate(body, params, 4, precision=64)
+        lo = sum(x.num_verts for x in bodies[:b])
+        assert rel_l2(out[N.PDGB_SOLVE_CLUSTER][lo:lo + body.num_verts], Xo) < TOL

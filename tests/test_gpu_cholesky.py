@@ -127,3 +127,23 @@ def test_solve_timing_and_bytes():
     assert nbytes == 2 * (8.0 * info["nnz_L"] + 4.0 * (n + 1)) + 48.0 * n
     Xo, _, _ = O.simulate(body, params, 3, precision=64)
     assert rel_l2(X, Xo) < TOL
+
+
+@pytest.mark.parametrize("mode", [N.PDGB_SOLVE_CTA, N.PDGB_SOLVE_CLUSTER, N.PDGB_SOLVE_LEVELS])
+def test_solve_schedules_agree(mode):
+    """The three schedules of the same factor (one CTA, one cluster, one
+    launch per level) give the FP64 oracle's positions; tol > 0 keeps the
+    early exit working in each."""
+    body = mesh.make_grid_body(9, 8, 7, jitter=0.1, seed=13, young=3e4)
+    params = SolverParams(num_iterations=10, tol=1e-4, solver=1)
+    with PdSolver(body, params) as e:
+        e.set_solve_mode(mode)
+        its = []
+        for _ in range(6):
+            e.update(1)
+            its.append(e.last_step_iterations())
+        assert e.solve_mode() == mode
+        X, _ = e.download_state()
+    Xo, _, ito = O.simulate(body, params, 6, precision=64)
+    assert rel_l2(X, Xo) < TOL
+    assert np.abs(np.asarray(its) - ito).max() <= 1

@@ -190,3 +190,39 @@ def test_kernel_timing_hook_counts_launches():
         X, _ = e.download_state()
     Xo, _, _ = O.simulate(body, params, 7, 64)
     assert rel_l2(X, Xo) < TOL
+
+
+@pytest.mark.parametrize("cap", [32, 64, 200, 512])
+def test_tile_size_gives_same_step(cap):
+    """Re-cut tiles (pdgb_set_tile_size) change only the float summation
+    order of the local step."""
+    body = mesh.make_grid_body(7, 6, 5, jitter=0.1, seed=21)
+    params = SolverParams(num_iterations=15, rho=0.999, solver=0)
+    with PdSolver(body, params) as e:
+        e.update(2)
+        e.set_tile_size(cap)
+        e.update(4)
+        X, _ = e.download_state()
+        tiles = e.get_performance_data()["tiles"]
+    assert tiles >= (body.num_tets + cap - 1) // cap
+    Xo, _, _ = O.simulate(body, params, 6, precision=64)
+    assert rel_l2(X, Xo) < TOL
+
+
+@pytest.mark.parametrize("solver", [0, 1])
+def test_autotune_keeps_state_and_result(solver):
+    body = mesh.make_grid_body(8, 8, 8, jitter=0.1, seed=22, young=4e4)
+    params = SolverParams(num_iterations=10 if solver else 20, rho=0.9995, solver=solver)
+    with PdSolver(body, params) as e:
+        e.update(3)
+        X3, V3 = e.download_state()
+        rep = e.autotune(steps=3)
+        Xa, Va = e.download_state()
+        assert np.array_equal(Xa, X3) and np.array_equal(Va, V3)  # tuning does not advance the state
+        assert rep["candidates"] >= (9 if solver else 5)
+        assert 0 < rep["best_ms"] <= rep["default_ms"] * 1.0001
+        assert rep["tile_tets"] in (64, 128, 256, 512)
+        e.update(3)
+        X, _ = e.download_state()
+    Xo, _, _ = O.simulate(body, params, 6, precision=64)
+    assert rel_l2(X, Xo) < TOL
