@@ -647,6 +647,8 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         SolveLevel lv;
         lv.fwd_begin = (int)(out.fwd_items.size() / kItemInts);
         lv.bwd_begin = (int)(out.bwd_items.size() / kItemInts);
+        lv.fwdb_begin = (int)(out.fwd_blocks.size() / kItemInts);
+        lv.bwdb_begin = (int)(out.bwd_blocks.size() / kItemInts);
         for (int s : bylevel[L]) {
             const int k = out.sk[s], m = out.sm[s];
             const int64_t mo = out.moff[s];
@@ -659,9 +661,20 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
                                          {lo, hi, out.roff[s], m, k, r0, c0, std::min(cmax, c0 + kFwdItemCols)});
             }
             for (int c = 0; c < k; ++c) out.bwd_items.insert(out.bwd_items.end(), {lo, hi, out.roff[s], m, k, c, 0, 0});
+            for (int r0 = 0; r0 < m; r0 += kFwdBlockRows) {
+                const int cmax = std::min(k, r0 + kFwdBlockRows);
+                for (int c0 = 0; c0 < cmax; c0 += kFwdBlockCols)
+                    out.fwd_blocks.insert(out.fwd_blocks.end(),
+                                          {lo, hi, out.roff[s], m, k, r0, c0, std::min(cmax, c0 + kFwdBlockCols)});
+            }
+            for (int c0 = 0; c0 < k; c0 += kBwdBlockCols)
+                out.bwd_blocks.insert(out.bwd_blocks.end(),
+                                      {lo, hi, out.roff[s], m, k, c0, std::min(k, c0 + kBwdBlockCols), 0});
         }
         lv.fwd_end = (int)(out.fwd_items.size() / kItemInts);
         lv.bwd_end = (int)(out.bwd_items.size() / kItemInts);
+        lv.fwdb_end = (int)(out.fwd_blocks.size() / kItemInts);
+        lv.bwdb_end = (int)(out.bwd_blocks.size() / kItemInts);
         out.levels[L] = lv;
     }
     out.body_level = {0, nl};
@@ -733,8 +746,11 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         };
         const int fb = shift(out.fwd_items, f.fwd_items);
         const int bb = shift(out.bwd_items, f.bwd_items);
+        const int fbb = shift(out.fwd_blocks, f.fwd_blocks);
+        const int bbb = shift(out.bwd_blocks, f.bwd_blocks);
         for (const SolveLevel& lv : f.levels)
-            out.levels.push_back({lv.fwd_begin + fb, lv.fwd_end + fb, lv.bwd_begin + bb, lv.bwd_end + bb});
+            out.levels.push_back({lv.fwd_begin + fb, lv.fwd_end + fb, lv.bwd_begin + bb, lv.bwd_end + bb,
+                                  lv.fwdb_begin + fbb, lv.fwdb_end + fbb, lv.bwdb_begin + bbb, lv.bwdb_end + bbb});
         out.body_level.push_back((int)out.levels.size());
         mbase += (int64_t)f.mval.size();
         rbase += (int64_t)f.rows.size();

@@ -41,8 +41,10 @@ std::vector<int> amd_order(const SparseSym& A);
 std::vector<int> nd_order(const SparseSym& A, const float* xyz);
 
 struct SolveLevel {
-    int fwd_begin, fwd_end;  // work items of the forward pass for this level
-    int bwd_begin, bwd_end;  // work items of the backward pass
+    int fwd_begin, fwd_end;  // warp work items of the forward pass for this level
+    int bwd_begin, bwd_end;  // warp work items of the backward pass
+    int fwdb_begin, fwdb_end;  // CTA block items of the forward pass (per-level launches)
+    int bwdb_begin, bwdb_end;  // CTA block items of the backward pass
 };
 
 // Warp work items, 8 ints each (two int4 loads, no dependent metadata loads):
@@ -53,6 +55,14 @@ struct SolveLevel {
 constexpr int kItemInts = 8;
 constexpr int kFwdItemRows = 32;
 constexpr int kFwdItemCols = 64;
+// CTA block items (same 8-int layout) of the per-level launches:
+//   forward : {moff_lo, moff_hi, roff, m, k, r0, c0, c1}: rows r0 .. r0+128,
+//             pivot columns c0 .. c1 (at most 256, staged in shared memory)
+//   backward: {moff_lo, moff_hi, roff, m, k, c0, c1, 0}: pivot columns
+//             c0 .. c1 (at most 16) against the staged rows c0 .. m
+constexpr int kFwdBlockRows = 128;
+constexpr int kFwdBlockCols = 256;
+constexpr int kBwdBlockCols = 16;
 
 struct CholFactor {
     int n = 0;
@@ -70,6 +80,8 @@ struct CholFactor {
     // GPU warp work items grouped by level (see kItemInts).
     std::vector<int> fwd_items;
     std::vector<int> bwd_items;
+    std::vector<int> fwd_blocks;     // CTA block items (see kFwdBlockRows)
+    std::vector<int> bwd_blocks;
     std::vector<SolveLevel> levels;  // body-major: body b owns levels[body_level[b] .. body_level[b+1])
     std::vector<int> body_level;     // [nbodies + 1]
     std::vector<int> body_order;     // bodies by decreasing stored factor size (batch solve order)

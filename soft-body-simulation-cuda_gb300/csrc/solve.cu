@@ -115,15 +115,123 @@ __global__ void __launch_bounds__(kLevelThreads) k_chol_bwd_level(CholArgs a, in
     bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * (item0 + it), stage[warp], lane);
 }
 
+// ---- per-level launches with CTA block items.
+// Forward block {moff, roff, m, k, r0, c0, c1}: the pivot right-hand sides
+// r[c0 .. c1) are staged in shared memory once; thread t owns row r0 + t and
+// streams its row of M_s (column-major, so a warp's loads of one column are
+// contiguous), 8 independent loads in flight.  Pivot rows add into y,
+// off-diagonal rows subtract from r (ancestor pivots, read at a later level).
+__global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, int item0) {
+    __shared__ float4 rs[kFwdBlockCols];
+    if (a.done && *a.done) return;
+    const int* w = a.fwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
+    const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
+    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+    const int roff = h0.z, m = h0.w, k = h1.x, r0 = h1.y, c0 = h1.z, c1 = h1.w;
+    const int* rows = a.rows + roff;
+    for (int j = threadIdx.x; j < c1 - c0; j += kBlockThreads) rs[j] = a.r[__ldg(&rows[c0 + j])];
+    __syncthreads();
+    const int row = r0 + threadIdx.x;
+    if (row >= m || row >= r0 + kFwdBlockRows) return;
+    const int cend = row < k ? min(c1, row + 1) : c1;
+    const float* Mr = a.mval + moff + row;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    int c = c0;
+    for (; c + 8 <= cend; c += 8) {
+        float mv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) mv[q] = __ldg(Mr + (size_t)(c + q) * m);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float4 v = rs[c + q - c0];
+            ax = fmaf(mv[q], v.x, ax);
+            ay = fmaf(mv[q], v.y, ay);
+            az = fmaf(mv[q], v.z, az);
+        }
+    }
+    for (; c < cend; ++c) {
+        const float mv = __ldg(Mr + (size_t)c * m);
+        const float4 v = rs[c - c0];
+        ax = fmaf(mv, v.x, ax);
+        ay = fmaf(mv, v.y, ay);
+        az = fmaf(mv, v.z, az);
+    }
+    const int vid = __ldg(&rows[row]);
+    if (row < k) atomicAdd(&a.y[vid], make_float4(ax, ay, az, 0.f));
+    else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
+}
+
+// Backward block {moff, roff, m, k, c0, c1}: z = [y_pivots ; -x_offdiag]
+// over rows c0 .. m is staged in shared memory (kBwdStageRows at a time,
+// one gather per row for the whole block); warp w owns columns
+// c0 + w, c0 + w + 4, ...; lanes stride a column of M_s (contiguous) with 4
+// independent loads in flight, then a warp reduction.
+__global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
+    __shared__ float4 z[kBwdStageRows];
+    if (a.done && *a.done) return;
+    const int* w = a.bwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
+    const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
+    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+    const int roff = h0.z, m = h0.w, k = h1.x, c0 = h1.y, c1 = h1.z;
+    const int* rows = a.rows + roff;
+    constexpr int kWarps = kBlockThreads / 32;
+    constexpr int kCols = kBwdBlockCols / kWarps;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float acc[kCols][3];
+#pragma unroll
+    for (int j = 0; j < kCols; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
+    for (int z0 = c0; z0 < m; z0 += kBwdStageRows) {
+        const int zn = min(kBwdStageRows, m - z0);
+        __syncthreads();  // the previous pass is consumed
+        for (int i = threadIdx.x; i < zn; i += kBlockThreads) {
+            const int r = z0 + i;
+            const int vid = __ldg(&rows[r]);
+            if (r < k) z[i] = a.y[vid];
+            else {
+                const float4 xv = a.x[vid];
+                z[i] = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kCols; ++j) {
+            const int c = c0 + warp + kWarps * j;
+            if (c >= c1) break;
+            const float* Mc = a.mval + moff + (size_t)c * m;
+            const int i0 = max(z0, c);
+#pragma unroll 4
+            for (int i = i0 + lane; i < z0 + zn; i += 32) {
+                const float mv = __ldg(Mc + i);
+                const float4 zz = z[i - z0];
+                acc[j][0] = fmaf(mv, zz.x, acc[j][0]);
+                acc[j][1] = fmaf(mv, zz.y, acc[j][1]);
+                acc[j][2] = fmaf(mv, zz.z, acc[j][2]);
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kCols; ++j) {
+        const int c = c0 + warp + kWarps * j;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            acc[j][0] += __shfl_xor_sync(0xffffffffu, acc[j][0], off);
+            acc[j][1] += __shfl_xor_sync(0xffffffffu, acc[j][1], off);
+            acc[j][2] += __shfl_xor_sync(0xffffffffu, acc[j][2], off);
+        }
+        if (lane == 0 && c < c1) a.x[__ldg(&rows[c])] = make_float4(acc[j][0], acc[j][1], acc[j][2], 0.f);
+    }
+}
+
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
-    constexpr int kWarps = kLevelThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
-        const int n = levels[L].fwd_end - levels[L].fwd_begin;
-        if (n > 0) k_chol_fwd_level<<<(n + kWarps - 1) / kWarps, kLevelThreads, 0, s>>>(a, levels[L].fwd_begin, n);
+        const int n = levels[L].fwdb_end - levels[L].fwdb_begin;
+        if (n > 0) k_chol_fwd_block<<<n, kBlockThreads, 0, s>>>(a, levels[L].fwdb_begin);
     }
     for (size_t L = levels.size(); L-- > 0;) {
-        const int n = levels[L].bwd_end - levels[L].bwd_begin;
-        if (n > 0) k_chol_bwd_level<<<(n + kWarps - 1) / kWarps, kLevelThreads, 0, s>>>(a, levels[L].bwd_begin, n);
+        const int n = levels[L].bwdb_end - levels[L].bwdb_begin;
+        if (n > 0) k_chol_bwd_block<<<n, kBlockThreads, 0, s>>>(a, levels[L].bwdb_begin);
     }
 }
 

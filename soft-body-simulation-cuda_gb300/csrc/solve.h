@@ -28,7 +28,12 @@ struct CholArgs {
     float4* y;  // forward result (must be zero on entry)
     float4* x;  // solution out
     const int* done;  // early-exit flag of the step (tol rule), may be null
+    const int* fwd_blocks;  // CTA block items (per-level launches)
+    const int* bwd_blocks;
 };
+
+constexpr int kBlockThreads = 128;      // block-item kernels: 4 warps
+constexpr int kBwdStageRows = 2048;     // rows of z staged per pass of a backward block
 
 // Convergence state of one step of the Cholesky path (device memory).
 struct StepState {
