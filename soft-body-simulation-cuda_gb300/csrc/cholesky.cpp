@@ -649,6 +649,8 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         lv.bwd_begin = (int)(out.bwd_items.size() / kItemInts);
         lv.fwdb_begin = (int)(out.fwd_blocks.size() / kItemInts);
         lv.bwdb_begin = (int)(out.bwd_blocks.size() / kItemInts);
+        lv.fwdw_begin = (int)(out.fwd_small.size() / kItemInts);
+        lv.bwdw_begin = (int)(out.bwd_small.size() / kItemInts);
         for (int s : bylevel[L]) {
             const int k = out.sk[s], m = out.sm[s];
             const int64_t mo = out.moff[s];
@@ -661,6 +663,16 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
                                          {lo, hi, out.roff[s], m, k, r0, c0, std::min(cmax, c0 + kFwdItemCols)});
             }
             for (int c = 0; c < k; ++c) out.bwd_items.insert(out.bwd_items.end(), {lo, hi, out.roff[s], m, k, c, 0, 0});
+            if (m < kBlockMinRows) {  // small: the warp items, again, for the per-level launches
+                for (int r0 = 0; r0 < m; r0 += kFwdItemRows) {
+                    const int cmax = std::min(k, r0 + kFwdItemRows);
+                    for (int c0 = 0; c0 < cmax; c0 += kFwdItemCols)
+                        out.fwd_small.insert(out.fwd_small.end(),
+                                             {lo, hi, out.roff[s], m, k, r0, c0, std::min(cmax, c0 + kFwdItemCols)});
+                }
+                for (int c = 0; c < k; ++c) out.bwd_small.insert(out.bwd_small.end(), {lo, hi, out.roff[s], m, k, c, 0, 0});
+                continue;
+            }
             for (int r0 = 0; r0 < m; r0 += kFwdBlockRows) {
                 const int cmax = std::min(k, r0 + kFwdBlockRows);
                 for (int c0 = 0; c0 < cmax; c0 += kFwdBlockCols)
@@ -675,6 +687,8 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         lv.bwd_end = (int)(out.bwd_items.size() / kItemInts);
         lv.fwdb_end = (int)(out.fwd_blocks.size() / kItemInts);
         lv.bwdb_end = (int)(out.bwd_blocks.size() / kItemInts);
+        lv.fwdw_end = (int)(out.fwd_small.size() / kItemInts);
+        lv.bwdw_end = (int)(out.bwd_small.size() / kItemInts);
         out.levels[L] = lv;
     }
     out.body_level = {0, nl};
@@ -748,9 +762,12 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         const int bb = shift(out.bwd_items, f.bwd_items);
         const int fbb = shift(out.fwd_blocks, f.fwd_blocks);
         const int bbb = shift(out.bwd_blocks, f.bwd_blocks);
+        const int fws = shift(out.fwd_small, f.fwd_small);
+        const int bws = shift(out.bwd_small, f.bwd_small);
         for (const SolveLevel& lv : f.levels)
             out.levels.push_back({lv.fwd_begin + fb, lv.fwd_end + fb, lv.bwd_begin + bb, lv.bwd_end + bb,
-                                  lv.fwdb_begin + fbb, lv.fwdb_end + fbb, lv.bwdb_begin + bbb, lv.bwdb_end + bbb});
+                                  lv.fwdb_begin + fbb, lv.fwdb_end + fbb, lv.bwdb_begin + bbb, lv.bwdb_end + bbb,
+                                  lv.fwdw_begin + fws, lv.fwdw_end + fws, lv.bwdw_begin + bws, lv.bwdw_end + bws});
         out.body_level.push_back((int)out.levels.size());
         mbase += (int64_t)f.mval.size();
         rbase += (int64_t)f.rows.size();

@@ -43,8 +43,10 @@ std::vector<int> nd_order(const SparseSym& A, const float* xyz);
 struct SolveLevel {
     int fwd_begin, fwd_end;  // warp work items of the forward pass for this level
     int bwd_begin, bwd_end;  // warp work items of the backward pass
-    int fwdb_begin, fwdb_end;  // CTA block items of the forward pass (per-level launches)
-    int bwdb_begin, bwdb_end;  // CTA block items of the backward pass
+    int fwdb_begin, fwdb_end;  // per-level launches: CTA block items (large supernodes)
+    int bwdb_begin, bwdb_end;
+    int fwdw_begin, fwdw_end;  // per-level launches: warp items of the small supernodes
+    int bwdw_begin, bwdw_end;
 };
 
 // Warp work items, 8 ints each (two int4 loads, no dependent metadata loads):
@@ -60,9 +62,21 @@ constexpr int kFwdItemCols = 64;
 //             pivot columns c0 .. c1 (at most 256, staged in shared memory)
 //   backward: {moff_lo, moff_hi, roff, m, k, c0, c1, 0}: pivot columns
 //             c0 .. c1 (at most 16) against the staged rows c0 .. m
+// Supernodes with at least kBlockMinRows rows use block items in the
+// per-level launches; smaller ones keep warp items (packed 4 per CTA).
+#ifndef PDGB_FWDB_COLS
+#define PDGB_FWDB_COLS 64
+#endif
+#ifndef PDGB_BWDB_COLS
+#define PDGB_BWDB_COLS 8
+#endif
+#ifndef PDGB_BLOCK_MIN_ROWS
+#define PDGB_BLOCK_MIN_ROWS 96
+#endif
 constexpr int kFwdBlockRows = 128;
-constexpr int kFwdBlockCols = 256;
-constexpr int kBwdBlockCols = 16;
+constexpr int kFwdBlockCols = PDGB_FWDB_COLS;
+constexpr int kBwdBlockCols = PDGB_BWDB_COLS;
+constexpr int kBlockMinRows = PDGB_BLOCK_MIN_ROWS;
 
 struct CholFactor {
     int n = 0;
@@ -82,6 +96,8 @@ struct CholFactor {
     std::vector<int> bwd_items;
     std::vector<int> fwd_blocks;     // CTA block items (see kFwdBlockRows)
     std::vector<int> bwd_blocks;
+    std::vector<int> fwd_small;      // warp items of the small supernodes (per-level launches)
+    std::vector<int> bwd_small;
     std::vector<SolveLevel> levels;  // body-major: body b owns levels[body_level[b] .. body_level[b+1])
     std::vector<int> body_level;     // [nbodies + 1]
     std::vector<int> body_order;     // bodies by decreasing stored factor size (batch solve order)

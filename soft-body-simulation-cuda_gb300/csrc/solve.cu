@@ -96,34 +96,25 @@ __device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, f
     if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
 }
 
-// ---- one launch per level: each warp takes one item.
-__global__ void __launch_bounds__(kLevelThreads) k_chol_fwd_level(CholArgs a, int item0, int nitems) {
-    __shared__ float4 stage[kLevelThreads / 32][32];
-    if (a.done && *a.done) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int it = blockIdx.x * (kLevelThreads / 32) + warp;
-    if (it >= nitems) return;
-    fwd_warp_item(a, a.fwd_items + (size_t)kItemInts * (item0 + it), stage[warp], lane);
-}
-
-__global__ void __launch_bounds__(kLevelThreads) k_chol_bwd_level(CholArgs a, int item0, int nitems) {
-    __shared__ float4 stage[kLevelThreads / 32][32];
-    if (a.done && *a.done) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int it = blockIdx.x * (kLevelThreads / 32) + warp;
-    if (it >= nitems) return;
-    bwd_warp_item(a, a.bwd_items + (size_t)kItemInts * (item0 + it), stage[warp], lane);
-}
-
 // ---- per-level launches with CTA block items.
 // Forward block {moff, roff, m, k, r0, c0, c1}: the pivot right-hand sides
 // r[c0 .. c1) are staged in shared memory once; thread t owns row r0 + t and
 // streams its row of M_s (column-major, so a warp's loads of one column are
 // contiguous), 8 independent loads in flight.  Pivot rows add into y,
 // off-diagonal rows subtract from r (ancestor pivots, read at a later level).
-__global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, int item0) {
-    __shared__ float4 rs[kFwdBlockCols];
+__global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, int item0, int nblocks, int small0,
+                                                                   int nsmall) {
+    // staged pivot right-hand sides; also the 4 warps' 32-entry stages of the warp items
+    __shared__ float4 rs[kFwdBlockCols > 32 * (kBlockThreads / 32) ? kFwdBlockCols : 32 * (kBlockThreads / 32)];
     if (a.done && *a.done) return;
+    if ((int)blockIdx.x >= nblocks) {  // small supernodes: one warp item per warp
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int it = ((int)blockIdx.x - nblocks) * (kBlockThreads / 32) + warp;
+        if (it < nsmall)
+            fwd_warp_item(a, a.fwd_small + (size_t)kItemInts * (small0 + it),
+                          reinterpret_cast<float4*>(rs) + 32 * warp, lane);
+        return;
+    }
     const int* w = a.fwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
@@ -167,9 +158,16 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
 // one gather per row for the whole block); warp w owns columns
 // c0 + w, c0 + w + 4, ...; lanes stride a column of M_s (contiguous) with 4
 // independent loads in flight, then a warp reduction.
-__global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
+__global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0, int nblocks, int small0,
+                                                                   int nsmall) {
     __shared__ float4 z[kBwdStageRows];
     if (a.done && *a.done) return;
+    if ((int)blockIdx.x >= nblocks) {  // small supernodes: one column per warp
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int it = ((int)blockIdx.x - nblocks) * (kBlockThreads / 32) + warp;
+        if (it < nsmall) bwd_warp_item(a, a.bwd_small + (size_t)kItemInts * (small0 + it), z, lane);
+        return;
+    }
     const int* w = a.bwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
@@ -225,13 +223,18 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
 }
 
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
+    constexpr int kWarps = kBlockThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
-        const int n = levels[L].fwdb_end - levels[L].fwdb_begin;
-        if (n > 0) k_chol_fwd_block<<<n, kBlockThreads, 0, s>>>(a, levels[L].fwdb_begin);
+        const SolveLevel& v = levels[L];
+        const int nb = v.fwdb_end - v.fwdb_begin, nw = v.fwdw_end - v.fwdw_begin;
+        const int grid = nb + (nw + kWarps - 1) / kWarps;
+        if (grid > 0) k_chol_fwd_block<<<grid, kBlockThreads, 0, s>>>(a, v.fwdb_begin, nb, v.fwdw_begin, nw);
     }
     for (size_t L = levels.size(); L-- > 0;) {
-        const int n = levels[L].bwdb_end - levels[L].bwdb_begin;
-        if (n > 0) k_chol_bwd_block<<<n, kBlockThreads, 0, s>>>(a, levels[L].bwdb_begin);
+        const SolveLevel& v = levels[L];
+        const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin;
+        const int grid = nb + (nw + kWarps - 1) / kWarps;
+        if (grid > 0) k_chol_bwd_block<<<grid, kBlockThreads, 0, s>>>(a, v.bwdb_begin, nb, v.bwdw_begin, nw);
     }
 }
 

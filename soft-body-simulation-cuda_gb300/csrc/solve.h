@@ -11,7 +11,6 @@
 
 namespace pdgb {
 
-constexpr int kLevelThreads = 128;     // per-level launches: 4 warps, one warp item each
 constexpr int kCtaSolveThreads = 1024; // whole-solve-in-one-CTA kernel: 32 warps
 constexpr int kClusterCtas = 8;           // CTAs per body in the cluster solve
 constexpr int kClusterSolveThreads = 512; // per CTA of the cluster solve: 16 warps
@@ -30,6 +29,8 @@ struct CholArgs {
     const int* done;  // early-exit flag of the step (tol rule), may be null
     const int* fwd_blocks;  // CTA block items (per-level launches)
     const int* bwd_blocks;
+    const int* fwd_small;   // warp items of small supernodes (per-level launches)
+    const int* bwd_small;
 };
 
 constexpr int kBlockThreads = 128;      // block-item kernels: 4 warps
