@@ -276,12 +276,12 @@ int pdgb_set_rotation(pdgb_engine* e, int rotation);
 /* Schedule of the Cholesky solve.  CTA: one CTA per body walks the body's
  * whole elimination tree (levels separated by block barriers); CLUSTER: one
  * cluster of 8 CTAs per body (cluster barriers); LEVELS: one launch per
- * level and direction over the whole GPU (large single systems).  AUTO
- * picks by size: a batch uses CTA, a single system CLUSTER up to 2^20
- * stored factor entries and LEVELS above.  LEVELS is not used for batches
- * (CLUSTER instead).  Takes effect at the next prepare; pdgb_get_solve_mode
- * returns the schedule in use (AUTO before the first prepare or on the
- * Jacobi path). */
+ * level and direction over the whole GPU, level L of every body of a batch
+ * in the same launch (levels counted from the leaves).  AUTO picks by
+ * size: a batch uses CTA, a single system CLUSTER up to 2^20 stored factor
+ * entries and LEVELS above; pdgb_autotune times all three.  Takes effect at
+ * the next prepare; pdgb_get_solve_mode returns the schedule in use (AUTO
+ * before the first prepare or on the Jacobi path). */
 #define PDGB_SOLVE_AUTO 0
 #define PDGB_SOLVE_CTA 1
 #define PDGB_SOLVE_CLUSTER 2

@@ -270,7 +270,7 @@ void record_chol_step(pdgb_engine* e) {
     auto solve = [&](const CholArgs& args) {
         if (e->solve_mode == PDGB_SOLVE_CTA) launch_chol_solve_cta(args, e->nbodies, s);
         else if (e->solve_mode == PDGB_SOLVE_CLUSTER) launch_chol_solve_cluster(args, e->nbodies, s);
-        else launch_chol_solve_levels(args, e->chol.levels, s);
+        else launch_chol_solve_levels(args, e->chol.step_levels, s);
     };
     for (int i = 0; i < n; ++i) {
         record_local(e, la, false, i);
@@ -357,8 +357,7 @@ SparseSym engine_system(const HostLayout& L) {
 // would dominate); batches always run one CTA or cluster per body.
 int choose_solve_mode(const pdgb_engine* e) {
     const bool small = e->chol.mval.size() <= kCtaSolveMaxEntries;
-    int m = e->solve_req;
-    if (m == PDGB_SOLVE_LEVELS && e->nbodies > 1) m = PDGB_SOLVE_CLUSTER;  // levels interleave bodies
+    const int m = e->solve_req;
     if (m != PDGB_SOLVE_AUTO) return m;
     if (e->nbodies > 1) return PDGB_SOLVE_CTA;
     return small ? PDGB_SOLVE_CLUSTER : PDGB_SOLVE_LEVELS;
@@ -790,10 +789,7 @@ int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
         copy_state(true);
         std::vector<int> caps = {kTileTets, kTileTets / 2, kTileTets / 4, kTileTets / 8};
         std::vector<int> modes = {e->solve_req};
-        if (e->prm.solver == PDGB_SOLVER_CHOLESKY) {
-            modes = {PDGB_SOLVE_CTA, PDGB_SOLVE_CLUSTER};
-            if (e->nbodies == 1) modes.push_back(PDGB_SOLVE_LEVELS);
-        }
+        if (e->prm.solver == PDGB_SOLVER_CHOLESKY) modes = {PDGB_SOLVE_CTA, PDGB_SOLVE_CLUSTER, PDGB_SOLVE_LEVELS};
         double best = t0;
         int best_cap = cap0, best_mode = req0, tried = 1;
         for (int cap : caps)

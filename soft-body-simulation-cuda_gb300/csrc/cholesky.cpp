@@ -693,6 +693,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
     }
     out.body_level = {0, nl};
     out.body_order = {0};
+    out.step_levels = out.levels;
 }
 
 void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const std::vector<int>& tstart,
@@ -730,6 +731,8 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
     int64_t mbase = 0, rbase = 0;
     int sbase = 0;
     out.body_level.assign(1, 0);
+    // per-level buckets of the block / small items of all bodies
+    std::vector<std::vector<int>> bfb, bfw, bbb, bbw;
     for (int b = 0; b < nbodies; ++b) {
         CholFactor& f = fs[b];
         const int v0 = vstart[b];
@@ -760,14 +763,21 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         };
         const int fb = shift(out.fwd_items, f.fwd_items);
         const int bb = shift(out.bwd_items, f.bwd_items);
-        const int fbb = shift(out.fwd_blocks, f.fwd_blocks);
-        const int bbb = shift(out.bwd_blocks, f.bwd_blocks);
-        const int fws = shift(out.fwd_small, f.fwd_small);
-        const int bws = shift(out.bwd_small, f.bwd_small);
-        for (const SolveLevel& lv : f.levels)
+        auto slice = [](const std::vector<int>& v, int b0, int b1) {
+            return std::vector<int>(v.begin() + (size_t)kItemInts * b0, v.begin() + (size_t)kItemInts * b1);
+        };
+        if ((int)bfb.size() < f.nlevels) {
+            bfb.resize(f.nlevels); bfw.resize(f.nlevels); bbb.resize(f.nlevels); bbw.resize(f.nlevels);
+        }
+        for (int L = 0; L < (int)f.levels.size(); ++L) {
+            const SolveLevel& lv = f.levels[L];
             out.levels.push_back({lv.fwd_begin + fb, lv.fwd_end + fb, lv.bwd_begin + bb, lv.bwd_end + bb,
-                                  lv.fwdb_begin + fbb, lv.fwdb_end + fbb, lv.bwdb_begin + bbb, lv.bwdb_end + bbb,
-                                  lv.fwdw_begin + fws, lv.fwdw_end + fws, lv.bwdw_begin + bws, lv.bwdw_end + bws});
+                                  0, 0, 0, 0, 0, 0, 0, 0});
+            shift(bfb[L], slice(f.fwd_blocks, lv.fwdb_begin, lv.fwdb_end));
+            shift(bfw[L], slice(f.fwd_small, lv.fwdw_begin, lv.fwdw_end));
+            shift(bbb[L], slice(f.bwd_blocks, lv.bwdb_begin, lv.bwdb_end));
+            shift(bbw[L], slice(f.bwd_small, lv.bwdw_begin, lv.bwdw_end));
+        }
         out.body_level.push_back((int)out.levels.size());
         mbase += (int64_t)f.mval.size();
         rbase += (int64_t)f.rows.size();
@@ -776,6 +786,20 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         f = CholFactor();  // release the per-body copy
     }
     (void)sbase;
+    for (size_t L = 0; L < bfb.size(); ++L) {
+        SolveLevel lv{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        auto put = [&](std::vector<int>& dst, std::vector<int>& src, int& b0, int& b1) {
+            b0 = (int)(dst.size() / kItemInts);
+            dst.insert(dst.end(), src.begin(), src.end());
+            b1 = (int)(dst.size() / kItemInts);
+            std::vector<int>().swap(src);
+        };
+        put(out.fwd_blocks, bfb[L], lv.fwdb_begin, lv.fwdb_end);
+        put(out.fwd_small, bfw[L], lv.fwdw_begin, lv.fwdw_end);
+        put(out.bwd_blocks, bbb[L], lv.bwdb_begin, lv.bwdb_end);
+        put(out.bwd_small, bbw[L], lv.bwdw_begin, lv.bwdw_end);
+        out.step_levels.push_back(lv);
+    }
     std::vector<std::pair<int64_t, int>> sz(nbodies);
     for (int b = 0; b < nbodies; ++b) {
         int64_t e = 0;

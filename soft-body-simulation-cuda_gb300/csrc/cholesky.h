@@ -65,10 +65,10 @@ constexpr int kFwdItemCols = 64;
 // Supernodes with at least kBlockMinRows rows use block items in the
 // per-level launches; smaller ones keep warp items (packed 4 per CTA).
 #ifndef PDGB_FWDB_COLS
-#define PDGB_FWDB_COLS 64
+#define PDGB_FWDB_COLS 32
 #endif
 #ifndef PDGB_BWDB_COLS
-#define PDGB_BWDB_COLS 8
+#define PDGB_BWDB_COLS 4
 #endif
 #ifndef PDGB_BLOCK_MIN_ROWS
 #define PDGB_BLOCK_MIN_ROWS 96
@@ -99,6 +99,10 @@ struct CholFactor {
     std::vector<int> fwd_small;      // warp items of the small supernodes (per-level launches)
     std::vector<int> bwd_small;
     std::vector<SolveLevel> levels;  // body-major: body b owns levels[body_level[b] .. body_level[b+1])
+    // Per-level launches (block and small items): level L of every body in
+    // one launch, levels counted from the leaves.  Equal to `levels` for a
+    // single body.
+    std::vector<SolveLevel> step_levels;
     std::vector<int> body_level;     // [nbodies + 1]
     std::vector<int> body_order;     // bodies by decreasing stored factor size (batch solve order)
     long long zeros = 0;             // explicit zeros stored by amalgamated supernodes

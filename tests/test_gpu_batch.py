@@ -56,9 +56,10 @@ def test_batch_uneven_sizes_cholesky():
             assert rel_l2(Xb, Xo) < TOL, b
 
 
-def test_batch_cluster_schedule():
-    """One cluster of CTAs per body (PDGB_SOLVE_CLUSTER) gives the same bodies
-    as one CTA per body."""
+def test_batch_solve_schedules():
+    """One cluster of CTAs per body (PDGB_SOLVE_CLUSTER) and one launch per
+    level across all bodies (PDGB_SOLVE_LEVELS) give the same bodies as one
+    CTA per body."""
     from pdgb import _native as N
 
     bodies = mesh.batch_c4(nbodies=7, seed=17, lo=3, hi=9)
@@ -69,10 +70,11 @@ def test_batch_cluster_schedule():
             e.set_solve_mode(mode)
             e.update(4)
             out[mode] = e.download_state()[0]
-            # batches never use the per-level schedule
-            assert e.solve_mode() == (N.PDGB_SOLVE_CLUSTER if mode == N.PDGB_SOLVE_LEVELS else mode)
+            assert e.solve_mode() == mode
     assert rel_l2(out[N.PDGB_SOLVE_CLUSTER], out[N.PDGB_SOLVE_CTA]) < 1e-5
+    assert rel_l2(out[N.PDGB_SOLVE_LEVELS], out[N.PDGB_SOLVE_CTA]) < 1e-5
     for b, body in enumerate(bodies):
         Xo, _, _ = O.simulate(body, params, 4, precision=64)
         lo = sum(x.num_verts for x in bodies[:b])
-        assert rel_l2(out[N.PDGB_SOLVE_CLUSTER][lo:lo + body.num_verts], Xo) < TOL
+        for mode in (N.PDGB_SOLVE_CLUSTER, N.PDGB_SOLVE_LEVELS):
+            assert rel_l2(out[mode][lo:lo + body.num_verts], Xo) < TOL
