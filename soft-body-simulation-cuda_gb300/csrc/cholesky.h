@@ -65,13 +65,13 @@ constexpr int kFwdItemCols = 64;
 // Supernodes with at least kBlockMinRows rows use block items in the
 // per-level launches; smaller ones keep warp items (packed 4 per CTA).
 #ifndef PDGB_FWDB_COLS
-#define PDGB_FWDB_COLS 32
+#define PDGB_FWDB_COLS 16
 #endif
 #ifndef PDGB_BWDB_COLS
 #define PDGB_BWDB_COLS 4
 #endif
 #ifndef PDGB_BLOCK_MIN_ROWS
-#define PDGB_BLOCK_MIN_ROWS 96
+#define PDGB_BLOCK_MIN_ROWS 64
 #endif
 constexpr int kFwdBlockRows = 128;
 constexpr int kFwdBlockCols = PDGB_FWDB_COLS;
