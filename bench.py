@@ -380,8 +380,7 @@ def launches_per_step(info, params) -> int:
     Cholesky epilogue."""
     if params.solver == 0:
         return 1 + 2 * params.num_iterations
-    per_solve = 2 * info["levels"] if info.get("solve_mode") == 3 else 1  # PDGB_SOLVE_LEVELS: per level
-    return 2 + params.num_iterations * (2 + per_solve)
+    return 2 + params.num_iterations * (2 + info["solve_launches"])
 
 
 # Default timed steps per workload: about 1.5 s of device time, so that the
@@ -538,6 +537,7 @@ def main():
     eng_info = eng.get_performance_data()
     eng_info["levels"] = eng.solve_levels() if params.solver == 1 else 0
     eng_info["solve_mode"] = eng.solve_mode() if params.solver == 1 else 0
+    eng_info["solve_launches"] = eng.factor_info()["solve_launches"] if params.solver == 1 else 0
     solve_bytes = eng.solve_bytes()
     eng.close()
 

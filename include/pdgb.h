@@ -323,6 +323,8 @@ typedef struct pdgb_factor_info {
     int bwd_items;          /* GPU work items, backward pass                  */
     double flops;           /* factorisation flops (approx.)                  */
     double factor_ms;       /* host time of ordering + factorisation         */
+    int solve_launches;     /* kernel launches of one solve, current schedule */
+    int reserved;
 } pdgb_factor_info;
 /* Factor statistics of a prepared engine on the Cholesky path (zeros
  * otherwise). */

@@ -1204,6 +1204,18 @@ int pdgb_inspect_layout(const pdgb_mesh_desc* mesh, pdgb_layout_info* info, int*
     });
 }
 
+namespace {
+// Kernel launches of one solve in the schedule in use.
+int solve_launches(const pdgb_engine* e) {
+    if (e->solve_mode != PDGB_SOLVE_LEVELS) return 1;
+    int n = 0;
+    for (const SolveLevel& v : e->chol.step_levels)
+        n += (v.fwdb_end > v.fwdb_begin) + (v.fwdw_end > v.fwdw_begin) + (v.bwdb_end > v.bwdb_begin) +
+             (v.bwdw_end > v.bwdw_begin);
+    return n;
+}
+}  // namespace
+
 int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info) {
     if (!e || !info) return PDGB_ERR_INVALID_ARGUMENT;
     std::memset(info, 0, sizeof(*info));
@@ -1217,6 +1229,7 @@ int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info) {
     info->bwd_items = (int)(f.bwd_items.size() / kItemInts);
     info->flops = f.flops;
     info->factor_ms = e->factor_ms;
+    info->solve_launches = solve_launches(e);
     return PDGB_OK;
 }
 
@@ -1251,6 +1264,8 @@ int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params
             info->bwd_items = (int)(f.bwd_items.size() / kItemInts);
             info->flops = f.flops;
             info->factor_ms = ms;
+            info->solve_launches = 0;
+            info->reserved = 0;
         }
         if (b && x) {
             const int nv = L.nv;

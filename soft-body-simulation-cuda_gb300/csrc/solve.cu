@@ -102,19 +102,9 @@ __device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, f
 // streams its row of M_s (column-major, so a warp's loads of one column are
 // contiguous), 8 independent loads in flight.  Pivot rows add into y,
 // off-diagonal rows subtract from r (ancestor pivots, read at a later level).
-__global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, int item0, int nblocks, int small0,
-                                                                   int nsmall) {
-    // staged pivot right-hand sides; also the 4 warps' 32-entry stages of the warp items
-    __shared__ float4 rs[kFwdBlockCols > 32 * (kBlockThreads / 32) ? kFwdBlockCols : 32 * (kBlockThreads / 32)];
+__global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, int item0) {
+    __shared__ float4 rs[kFwdBlockCols];
     if (a.done && *a.done) return;
-    if ((int)blockIdx.x >= nblocks) {  // small supernodes: one warp item per warp
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        const int it = ((int)blockIdx.x - nblocks) * (kBlockThreads / 32) + warp;
-        if (it < nsmall)
-            fwd_warp_item(a, a.fwd_small + (size_t)kItemInts * (small0 + it),
-                          reinterpret_cast<float4*>(rs) + 32 * warp, lane);
-        return;
-    }
     const int* w = a.fwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
@@ -158,16 +148,9 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
 // one gather per row for the whole block); warp w owns columns
 // c0 + w, c0 + w + 4, ...; lanes stride a column of M_s (contiguous) with 4
 // independent loads in flight, then a warp reduction.
-__global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0, int nblocks, int small0,
-                                                                   int nsmall) {
+__global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
     __shared__ float4 z[kBwdStageRows];
     if (a.done && *a.done) return;
-    if ((int)blockIdx.x >= nblocks) {  // small supernodes: one column per warp
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        const int it = ((int)blockIdx.x - nblocks) * (kBlockThreads / 32) + warp;
-        if (it < nsmall) bwd_warp_item(a, a.bwd_small + (size_t)kItemInts * (small0 + it), z, lane);
-        return;
-    }
     const int* w = a.bwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
@@ -222,19 +205,37 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
     }
 }
 
+// Small supernodes of a level (per-level launches): one warp item per warp,
+// in kernels of their own so that the many warps of the leaf levels are not
+// limited by the block kernels' registers and shared memory.
+__global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_small(CholArgs a, int item0, int nitems) {
+    __shared__ float4 stage[kSmallThreads / 32][32];
+    if (a.done && *a.done) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int it = blockIdx.x * (kSmallThreads / 32) + warp;
+    if (it < nitems) fwd_warp_item(a, a.fwd_small + (size_t)kItemInts * (item0 + it), stage[warp], lane);
+}
+
+__global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_small(CholArgs a, int item0, int nitems) {
+    if (a.done && *a.done) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int it = blockIdx.x * (kSmallThreads / 32) + warp;
+    if (it < nitems) bwd_warp_item(a, a.bwd_small + (size_t)kItemInts * (item0 + it), nullptr, lane);
+}
+
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
-    constexpr int kWarps = kBlockThreads / 32;
+    constexpr int kWarps = kSmallThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
         const SolveLevel& v = levels[L];
         const int nb = v.fwdb_end - v.fwdb_begin, nw = v.fwdw_end - v.fwdw_begin;
-        const int grid = nb + (nw + kWarps - 1) / kWarps;
-        if (grid > 0) k_chol_fwd_block<<<grid, kBlockThreads, 0, s>>>(a, v.fwdb_begin, nb, v.fwdw_begin, nw);
+        if (nw > 0) k_chol_fwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.fwdw_begin, nw);
+        if (nb > 0) k_chol_fwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.fwdb_begin);
     }
     for (size_t L = levels.size(); L-- > 0;) {
         const SolveLevel& v = levels[L];
         const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin;
-        const int grid = nb + (nw + kWarps - 1) / kWarps;
-        if (grid > 0) k_chol_bwd_block<<<grid, kBlockThreads, 0, s>>>(a, v.bwdb_begin, nb, v.bwdw_begin, nw);
+        if (nb > 0) k_chol_bwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.bwdb_begin);
+        if (nw > 0) k_chol_bwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.bwdw_begin, nw);
     }
 }
 

@@ -34,6 +34,7 @@ struct CholArgs {
 };
 
 constexpr int kBlockThreads = 128;      // block-item kernels: 4 warps
+constexpr int kSmallThreads = 256;      // small-supernode kernels: one warp item per warp
 constexpr int kBwdStageRows = 2048;     // rows of z staged per pass of a backward block
 
 // Convergence state of one step of the Cholesky path (device memory).

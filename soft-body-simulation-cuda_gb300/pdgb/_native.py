@@ -139,6 +139,8 @@ class pdgb_factor_info(C.Structure):
         ("bwd_items", C.c_int),
         ("flops", C.c_double),
         ("factor_ms", C.c_double),
+        ("solve_launches", C.c_int),
+        ("reserved", C.c_int),
     ]
 
 
