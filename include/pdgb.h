@@ -484,6 +484,12 @@ typedef struct pdgb_noalloc_mesh {
 int pdgb_step_noalloc(const pdgb_noalloc_mesh* mesh, const pdgb_params* params, float* X, float* V, int nsteps,
                       void* stream);
 
+/* The local step's rotation on n row-major 3x3 matrices F (host arrays,
+ * 9 floats each): R = the closest proper rotation as the engine computes it
+ * (PDGB_ROTATION_QUAT or _SVD), for checking the rotation on its own.
+ * Waits for the GPU. */
+int pdgb_closest_rotations(int n, const float* F, float* R, int rotation);
+
 /* Library version string. */
 const char* pdgb_version(void);
 

@@ -1279,6 +1279,23 @@ int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params
     });
 }
 
+int pdgb_closest_rotations(int n, const float* F, float* R, int rotation) {
+    if (n < 0 || (n > 0 && (!F || !R)) || (rotation != PDGB_ROTATION_QUAT && rotation != PDGB_ROTATION_SVD)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad count, arrays or rotation mode");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return PDGB_OK;
+    return guarded([&] {
+        DBuf<float> dF, dR;
+        dF.alloc(9 * (size_t)n);
+        dR.alloc(9 * (size_t)n);
+        PDGB_CUDA_TRY(cudaMemcpy(dF.p, F, 9 * (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+        launch_rotations(n, dF.p, dR.p, rotation, nullptr);
+        PDGB_CUDA_TRY(cudaGetLastError());
+        PDGB_CUDA_TRY(cudaMemcpy(R, dR.p, 9 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost));
+    });
+}
+
 const char* pdgb_version(void) { return "pdgb 0.2 (sm_103a)"; }
 
 }  // extern "C"

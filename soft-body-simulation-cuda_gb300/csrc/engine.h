@@ -224,6 +224,8 @@ void launch_drag_select(int nv, const float4* x, const float4* coef, int select_
                         double radius_sq, float* drag_w, float4* drag_off, cudaStream_t s);
 void launch_drag_rhs(int nv, const SceneArgs& sc, const float4* base, float4* b, const int* done, cudaStream_t s);
 void launch_copy_state(int nv, const float4* src, float4* dst, cudaStream_t s);
+// The local step's rotation on n row-major 3x3 matrices (device arrays).
+void launch_rotations(int n, const float* F, float* R, int rotation, cudaStream_t s);
 // Surface positions / normals for rendering (tri_nor as float4 per corner).
 void launch_render_surface(int n, const uint32_t* tris, const int* viperm, int nv, const float4* x, float* pos,
                            float* nor, cudaStream_t s);

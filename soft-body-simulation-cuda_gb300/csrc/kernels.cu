@@ -312,6 +312,25 @@ void launch_begin(const BeginArgs& a, cudaStream_t s) {
     if (blocks) k_begin<<<blocks, 256, 0, s>>>(a);
 }
 
+// ------------------------------------------------------- rotation check
+// The local step's rotation on n row-major 3x3 matrices (checking and
+// benchmarking the rotation on its own).
+__global__ void k_rotations(int n, const float* __restrict__ F, float* R, int rotation) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float f[9], r[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) f[k] = F[9 * (size_t)i + k];
+    if (rotation == PDGB_ROTATION_SVD) closest_rotation(f, r);
+    else closest_rotation_horn(f, r);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[9 * (size_t)i + k] = r[k];
+}
+
+void launch_rotations(int n, const float* F, float* R, int rotation, cudaStream_t s) {
+    if (n > 0) k_rotations<<<(n + 255) / 256, 256, 0, s>>>(n, F, R, rotation);
+}
+
 // ------------------------------------------------------- state transfer
 __global__ void k_gather_state(int nv, const int* __restrict__ vperm, const float* __restrict__ X,
                                const float* __restrict__ V, float4* x, float4* v) {

@@ -167,10 +167,12 @@ __device__ __forceinline__ void closest_rotation(const float F[9], float R[9]) {
 // the reference's U V^T with a signed smallest singular value -- is the
 // eigenvector of N's largest eigenvalue.  It is found as the dominant
 // eigenvector of A = N + c I (c = 0.6 |F|_F > |sigma_3| keeps the top
-// eigenvalue dominant even for inverted F) by repeated squaring: 3 squarings
-// unconditionally, then up to kTail more, each preceded by a unit-trace
-// normalisation and stopping once trace(P^2) = 1 to float precision (P is
-// then rank one).  The column of P with the largest diagonal entry is q.
+// eigenvalue dominant even for inverted F) by repeated squaring: P = A^4
+// after 2 squarings, then, while P is not rank one to float precision
+// (trace(P^2) = |P|_F^2 < (1 - 4e-7) trace(P)^2), up to kTail normalised
+// squarings.  Mildly deformed elements (the common case) stop at A^4.  The
+// column of P with the largest diagonal entry, multiplied once more by P
+// (which squares the remaining error), is q.
 __device__ __forceinline__ void sym4_square(float a[10]) {
     // a = {ww, xx, yy, zz, wx, wy, wz, xy, xz, yz}
     const float ww = a[0], xx = a[1], yy = a[2], zz = a[3], wx = a[4], wy = a[5], wz = a[6], xy = a[7], xz = a[8],
@@ -187,7 +189,14 @@ __device__ __forceinline__ void sym4_square(float a[10]) {
     a[9] = fmaf(wy, wz, fmaf(xy, xz, fmaf(yy, yz, yz * zz)));
 }
 
-template <int kTail = 6>
+// |P|_F^2 = trace(P^2) of a symmetric 4x4 in the packed layout above.
+__device__ __forceinline__ float sym4_frob2(const float a[10]) {
+    const float d = fmaf(a[0], a[0], fmaf(a[1], a[1], fmaf(a[2], a[2], a[3] * a[3])));
+    const float o = fmaf(a[4], a[4], fmaf(a[5], a[5], fmaf(a[6], a[6], fmaf(a[7], a[7], fmaf(a[8], a[8], a[9] * a[9])))));
+    return fmaf(2.f, o, d);
+}
+
+template <int kTail = 8>
 __device__ __forceinline__ void closest_rotation_horn(const float F[9], float R[9]) {
     float f2 = 0.f;
 #pragma unroll
@@ -206,32 +215,26 @@ __device__ __forceinline__ void closest_rotation_horn(const float F[9], float R[
     a[7] = (F[1] + F[3]) * sc;
     a[8] = (F[2] + F[6]) * sc;
     a[9] = (F[5] + F[7]) * sc;
-    // A^16: the top eigenvalue of A/(4c) is >= 1/4, so no underflow yet.
+    // A^4: the top eigenvalue of A/(4c) is >= 1/4, so no underflow.
     sym4_square(a);
     sym4_square(a);
-    sym4_square(a);
-    const float t8 = a[0] + a[1] + a[2] + a[3];
-    sym4_square(a);
-    float t = a[0] + a[1] + a[2] + a[3];        // = trace(P8^2)
-    if (t < (1.0f - 4e-7f) * t8 * t8) {
-        // slow convergence (strongly stretched or inverted F): normalised
-        // squarings until P is rank one to float precision.
-        for (int k = 0; k < kTail; ++k) {
-            const float it = __fdividef(1.0f, t);
+    float t = a[0] + a[1] + a[2] + a[3];
+    for (int k = 0; k < kTail && sym4_frob2(a) < (1.0f - 4e-7f) * t * t; ++k) {
+        const float it = __fdividef(1.0f, t);
 #pragma unroll
-            for (int i = 0; i < 10; ++i) a[i] *= it;
-            sym4_square(a);
-            const float tn = a[0] + a[1] + a[2] + a[3];
-            const bool conv = tn >= 1.0f - 4e-7f;
-            t = tn;
-            if (conv) break;
-        }
+        for (int i = 0; i < 10; ++i) a[i] *= it;
+        sym4_square(a);
+        t = a[0] + a[1] + a[2] + a[3];
     }
-    // column with the largest diagonal entry
-    float qw = a[0], qx = a[4], qy = a[5], qz = a[6], best = a[0];
-    if (a[1] > best) { best = a[1]; qw = a[4]; qx = a[1]; qy = a[7]; qz = a[8]; }
-    if (a[2] > best) { best = a[2]; qw = a[5]; qx = a[7]; qy = a[2]; qz = a[9]; }
-    if (a[3] > best) { qw = a[6]; qx = a[8]; qy = a[9]; qz = a[3]; }
+    // dominant column, one more power step, normalised
+    float c0 = a[0], c1 = a[4], c2 = a[5], c3 = a[6], best = a[0];
+    if (a[1] > best) { best = a[1]; c0 = a[4]; c1 = a[1]; c2 = a[7]; c3 = a[8]; }
+    if (a[2] > best) { best = a[2]; c0 = a[5]; c1 = a[7]; c2 = a[2]; c3 = a[9]; }
+    if (a[3] > best) { c0 = a[6]; c1 = a[8]; c2 = a[9]; c3 = a[3]; }
+    float qw = fmaf(a[0], c0, fmaf(a[4], c1, fmaf(a[5], c2, a[6] * c3)));
+    float qx = fmaf(a[4], c0, fmaf(a[1], c1, fmaf(a[7], c2, a[8] * c3)));
+    float qy = fmaf(a[5], c0, fmaf(a[7], c1, fmaf(a[2], c2, a[9] * c3)));
+    float qz = fmaf(a[6], c0, fmaf(a[8], c1, fmaf(a[9], c2, a[3] * c3)));
     const float n = rsqrtf(fmaxf(qw * qw + qx * qx + qy * qy + qz * qz, 1e-37f));
     qw *= n; qx *= n; qy *= n; qz *= n;
     const float xx = qx * qx, yy = qy * qy, zz = qz * qz;

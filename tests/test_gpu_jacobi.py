@@ -4,6 +4,7 @@ Bar: vertex positions after N steps within 1e-4 relative L2 of (a) the
 reference's own kernels (golden fixtures) and (b) the FP64 oracle.
 """
 import ctypes as C
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -226,3 +227,47 @@ def test_autotune_keeps_state_and_result(solver):
         X, _ = e.download_state()
     Xo, _, _ = O.simulate(body, params, 6, precision=64)
     assert rel_l2(X, Xo) < TOL
+
+
+def _deformation_gradients(n, seed):
+    """Rotations times stretches (singular values exp(U(-1.2, 1.2))), with
+    inverted, nearly flat and near-identity cases mixed in."""
+    rng = np.random.default_rng(seed)
+    F = []
+    for k in range(n):
+        Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        if np.linalg.det(Q) < 0:
+            Q[:, 0] = -Q[:, 0]
+        W, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        s = np.exp(rng.uniform(-1.2, 1.2, size=3))
+        if k % 7 == 3:
+            s[2] = -0.3 * s[2]                    # inverted
+        if k % 11 == 5:
+            s[2] = 1e-3                          # nearly flat
+        if k % 5 == 1:
+            s = 1.0 + rng.uniform(-0.05, 0.05, 3)  # mild
+        F.append(Q @ np.diag(s) @ W.T)
+    return np.asarray(F, dtype=np.float32)
+
+
+@pytest.mark.parametrize("mode", [N.PDGB_ROTATION_QUAT, N.PDGB_ROTATION_SVD])
+def test_device_rotation_accuracy(mode):
+    """The local step's rotation on its own (pdgb_closest_rotations) against
+    the exact closest proper rotation (FP64 oracle); the quaternion form is
+    converged to float precision, the SVD form reproduces the reference's
+    4-sweep scheme (golden rotations of the reference's own SVD)."""
+    F = _deformation_gradients(4096, 31)
+    R = np.empty_like(F)
+    N.check(N.lib().pdgb_closest_rotations(len(F), F.ctypes.data, R.ctypes.data, mode), "rotations")
+    Rx = O.rotations(F.astype(np.float64), precision=64).reshape(-1, 3, 3)
+    err = np.abs(R - Rx).max(axis=(1, 2))
+    assert np.isfinite(R).all()
+    assert np.allclose(np.linalg.det(R.astype(np.float64)), 1.0, atol=1e-5)
+    if mode == N.PDGB_ROTATION_QUAT:
+        assert err.max() < 2e-6, err.max()
+    else:
+        z = np.load(Path(__file__).resolve().parent / "golden" / "rotations.npz")
+        Rg = np.empty_like(z["F"])
+        N.check(N.lib().pdgb_closest_rotations(len(z["F"]), np.ascontiguousarray(z["F"]).ctypes.data,
+                                               Rg.ctypes.data, mode), "rotations")
+        assert np.abs(Rg - z["R"]).max() < 5e-6
