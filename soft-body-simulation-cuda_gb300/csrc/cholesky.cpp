@@ -651,6 +651,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         lv.bwdb_begin = (int)(out.bwd_blocks.size() / kItemInts);
         lv.fwdw_begin = (int)(out.fwd_small.size() / kItemInts);
         lv.bwdw_begin = (int)(out.bwd_small.size() / kItemInts);
+        lv.tiny_begin = (int)(out.tiny.size() / kItemInts);
         for (int s : bylevel[L]) {
             const int k = out.sk[s], m = out.sm[s];
             const int64_t mo = out.moff[s];
@@ -663,6 +664,10 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
                                          {lo, hi, out.roff[s], m, k, r0, c0, std::min(cmax, c0 + kFwdItemCols)});
             }
             for (int c = 0; c < k; ++c) out.bwd_items.insert(out.bwd_items.end(), {lo, hi, out.roff[s], m, k, c, 0, 0});
+            if (k <= kTinyCols && m <= kTinyRows) {  // tiny: one thread per supernode (per-level launches)
+                out.tiny.insert(out.tiny.end(), {lo, hi, out.roff[s], m, k, 0, 0, 0});
+                continue;
+            }
             if (m < kBlockMinRows) {  // small: the warp items, again, for the per-level launches
                 for (int r0 = 0; r0 < m; r0 += kFwdItemRows) {
                     const int cmax = std::min(k, r0 + kFwdItemRows);
@@ -689,6 +694,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         lv.bwdb_end = (int)(out.bwd_blocks.size() / kItemInts);
         lv.fwdw_end = (int)(out.fwd_small.size() / kItemInts);
         lv.bwdw_end = (int)(out.bwd_small.size() / kItemInts);
+        lv.tiny_end = (int)(out.tiny.size() / kItemInts);
         out.levels[L] = lv;
     }
     out.body_level = {0, nl};
@@ -732,7 +738,7 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
     int sbase = 0;
     out.body_level.assign(1, 0);
     // per-level buckets of the block / small items of all bodies
-    std::vector<std::vector<int>> bfb, bfw, bbb, bbw;
+    std::vector<std::vector<int>> bfb, bfw, bbb, bbw, btn;
     for (int b = 0; b < nbodies; ++b) {
         CholFactor& f = fs[b];
         const int v0 = vstart[b];
@@ -768,11 +774,13 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         };
         if ((int)bfb.size() < f.nlevels) {
             bfb.resize(f.nlevels); bfw.resize(f.nlevels); bbb.resize(f.nlevels); bbw.resize(f.nlevels);
+            btn.resize(f.nlevels);
         }
         for (int L = 0; L < (int)f.levels.size(); ++L) {
             const SolveLevel& lv = f.levels[L];
             out.levels.push_back({lv.fwd_begin + fb, lv.fwd_end + fb, lv.bwd_begin + bb, lv.bwd_end + bb,
-                                  0, 0, 0, 0, 0, 0, 0, 0});
+                                  0, 0, 0, 0, 0, 0, 0, 0, 0, 0});
+            shift(btn[L], slice(f.tiny, lv.tiny_begin, lv.tiny_end));
             shift(bfb[L], slice(f.fwd_blocks, lv.fwdb_begin, lv.fwdb_end));
             shift(bfw[L], slice(f.fwd_small, lv.fwdw_begin, lv.fwdw_end));
             shift(bbb[L], slice(f.bwd_blocks, lv.bwdb_begin, lv.bwdb_end));
@@ -787,7 +795,7 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
     }
     (void)sbase;
     for (size_t L = 0; L < bfb.size(); ++L) {
-        SolveLevel lv{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        SolveLevel lv{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         auto put = [&](std::vector<int>& dst, std::vector<int>& src, int& b0, int& b1) {
             b0 = (int)(dst.size() / kItemInts);
             dst.insert(dst.end(), src.begin(), src.end());
@@ -798,6 +806,7 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         put(out.fwd_small, bfw[L], lv.fwdw_begin, lv.fwdw_end);
         put(out.bwd_blocks, bbb[L], lv.bwdb_begin, lv.bwdb_end);
         put(out.bwd_small, bbw[L], lv.bwdw_begin, lv.bwdw_end);
+        put(out.tiny, btn[L], lv.tiny_begin, lv.tiny_end);
         out.step_levels.push_back(lv);
     }
     std::vector<std::pair<int64_t, int>> sz(nbodies);

@@ -47,6 +47,7 @@ struct SolveLevel {
     int bwdb_begin, bwdb_end;
     int fwdw_begin, fwdw_end;  // per-level launches: warp items of the small supernodes
     int bwdw_begin, bwdw_end;
+    int tiny_begin, tiny_end;  // per-level launches: tiny supernodes, one thread each
 };
 
 // Warp work items, 8 ints each (two int4 loads, no dependent metadata loads):
@@ -73,6 +74,11 @@ constexpr int kFwdItemCols = 64;
 #ifndef PDGB_BLOCK_MIN_ROWS
 #define PDGB_BLOCK_MIN_ROWS 64
 #endif
+// Tiny supernodes (at most kTinyCols pivots and kTinyRows rows -- most of
+// them are leaves with one pivot) are solved one per thread in the per-level
+// launches: descriptor {moff_lo, moff_hi, roff, m, k, 0, 0, 0}.
+constexpr int kTinyCols = 4;
+constexpr int kTinyRows = 48;
 constexpr int kFwdBlockRows = 128;
 constexpr int kFwdBlockCols = PDGB_FWDB_COLS;
 constexpr int kBwdBlockCols = PDGB_BWDB_COLS;
@@ -98,6 +104,7 @@ struct CholFactor {
     std::vector<int> bwd_blocks;
     std::vector<int> fwd_small;      // warp items of the small supernodes (per-level launches)
     std::vector<int> bwd_small;
+    std::vector<int> tiny;           // tiny supernode descriptors (per-level launches)
     std::vector<SolveLevel> levels;  // body-major: body b owns levels[body_level[b] .. body_level[b+1])
     // Per-level launches (block and small items): level L of every body in
     // one launch, levels counted from the leaves.  Equal to `levels` for a

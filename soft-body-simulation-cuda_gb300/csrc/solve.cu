@@ -223,19 +223,94 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_small(CholArgs a, in
     if (it < nitems) bwd_warp_item(a, a.bwd_small + (size_t)kItemInts * (item0 + it), nullptr, lane);
 }
 
+// Tiny supernodes (at most kTinyCols pivots, kTinyRows rows): one thread
+// solves a whole supernode, so the many leaves of a level cost one thread
+// each instead of one warp per item.  Forward: pivot rows store y (only this
+// supernode writes them), off-diagonal rows subtract from r.  Backward:
+// x_c = sum_{i >= c} M[i, c] z_i over the supernode's rows.
+__global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_tiny(CholArgs a, int t0, int n) {
+    if (a.done && *a.done) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * (t0 + t)));
+    const int k = __ldg(a.tiny + (size_t)kItemInts * (t0 + t) + 4);
+    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+    const int m = h0.w;
+    const int* rows = a.rows + h0.z;
+    const float* M = a.mval + moff;
+    float4 rc[kTinyCols];
+#pragma unroll
+    for (int c = 0; c < kTinyCols; ++c) rc[c] = c < k ? a.r[__ldg(&rows[c])] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+    for (int i = 0; i < m; ++i) {
+        float ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll
+        for (int c = 0; c < kTinyCols; ++c) {
+            if (c < k && c <= i) {
+                const float mv = __ldg(M + (size_t)c * m + i);
+                ax = fmaf(mv, rc[c].x, ax);
+                ay = fmaf(mv, rc[c].y, ay);
+                az = fmaf(mv, rc[c].z, az);
+            }
+        }
+        const int vid = __ldg(&rows[i]);
+        if (i < k) a.y[vid] = make_float4(ax, ay, az, 0.f);
+        else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
+    }
+}
+
+__global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int t0, int n) {
+    if (a.done && *a.done) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * (t0 + t)));
+    const int k = __ldg(a.tiny + (size_t)kItemInts * (t0 + t) + 4);
+    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+    const int m = h0.w;
+    const int* rows = a.rows + h0.z;
+    const float* M = a.mval + moff;
+    float acc[kTinyCols][3];
+#pragma unroll
+    for (int c = 0; c < kTinyCols; ++c) acc[c][0] = acc[c][1] = acc[c][2] = 0.f;
+#pragma unroll 4
+    for (int i = 0; i < m; ++i) {
+        const int vid = __ldg(&rows[i]);
+        float4 z;
+        if (i < k) z = a.y[vid];
+        else {
+            const float4 xv = a.x[vid];
+            z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+        }
+#pragma unroll
+        for (int c = 0; c < kTinyCols; ++c) {
+            if (c < k && c <= i) {
+                const float mv = __ldg(M + (size_t)c * m + i);
+                acc[c][0] = fmaf(mv, z.x, acc[c][0]);
+                acc[c][1] = fmaf(mv, z.y, acc[c][1]);
+                acc[c][2] = fmaf(mv, z.z, acc[c][2]);
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kTinyCols; ++c)
+        if (c < k) a.x[__ldg(&rows[c])] = make_float4(acc[c][0], acc[c][1], acc[c][2], 0.f);
+}
+
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
     constexpr int kWarps = kSmallThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
         const SolveLevel& v = levels[L];
-        const int nb = v.fwdb_end - v.fwdb_begin, nw = v.fwdw_end - v.fwdw_begin;
+        const int nb = v.fwdb_end - v.fwdb_begin, nw = v.fwdw_end - v.fwdw_begin, nt = v.tiny_end - v.tiny_begin;
+        if (nt > 0) k_chol_fwd_tiny<<<(nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s>>>(a, v.tiny_begin, nt);
         if (nw > 0) k_chol_fwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.fwdw_begin, nw);
         if (nb > 0) k_chol_fwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.fwdb_begin);
     }
     for (size_t L = levels.size(); L-- > 0;) {
         const SolveLevel& v = levels[L];
-        const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin;
+        const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin, nt = v.tiny_end - v.tiny_begin;
         if (nb > 0) k_chol_bwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.bwdb_begin);
         if (nw > 0) k_chol_bwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.bwdw_begin, nw);
+        if (nt > 0) k_chol_bwd_tiny<<<(nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s>>>(a, v.tiny_begin, nt);
     }
 }
 

@@ -31,6 +31,7 @@ struct CholArgs {
     const int* bwd_blocks;
     const int* fwd_small;   // warp items of small supernodes (per-level launches)
     const int* bwd_small;
+    const int* tiny;        // tiny supernode descriptors (per-level launches)
 };
 
 constexpr int kBlockThreads = 128;      // block-item kernels: 4 warps

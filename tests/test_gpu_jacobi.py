@@ -264,7 +264,26 @@ def test_device_rotation_accuracy(mode):
     assert np.isfinite(R).all()
     assert np.allclose(np.linalg.det(R.astype(np.float64)), 1.0, atol=1e-5)
     if mode == N.PDGB_ROTATION_QUAT:
-        assert err.max() < 2e-6, err.max()
+        # The closest rotation maximises tr(R^T F).  Where the two largest
+        # eigenvalues of Horn's matrix N(F) nearly coincide (inverted
+        # elements with |sigma_3| close to sigma_2) the maximiser is not
+        # unique: there only the objective is compared.
+        F64 = F.astype(np.float64)
+        obj = np.einsum("nij,nij->n", R.astype(np.float64), F64)
+        objx = np.einsum("nij,nij->n", Rx, F64)
+        scale = np.linalg.norm(F64.reshape(-1, 9), axis=1)
+        assert (np.abs(obj - objx) <= 2e-6 * scale).all()
+        gap = np.empty(len(F))
+        for n, f in enumerate(F64):
+            Nm = np.array([[f[0, 0] + f[1, 1] + f[2, 2], f[2, 1] - f[1, 2], f[0, 2] - f[2, 0], f[1, 0] - f[0, 1]],
+                           [f[2, 1] - f[1, 2], f[0, 0] - f[1, 1] - f[2, 2], f[0, 1] + f[1, 0], f[0, 2] + f[2, 0]],
+                           [f[0, 2] - f[2, 0], f[0, 1] + f[1, 0], f[1, 1] - f[0, 0] - f[2, 2], f[1, 2] + f[2, 1]],
+                           [f[1, 0] - f[0, 1], f[0, 2] + f[2, 0], f[1, 2] + f[2, 1], f[2, 2] - f[0, 0] - f[1, 1]]])
+            ev = np.linalg.eigvalsh(Nm)
+            gap[n] = (ev[3] - ev[2]) / max(ev[3] - ev[0], 1e-300)
+        well = gap > 1e-2
+        assert well.mean() > 0.95
+        assert err[well].max() < 2e-6, err[well].max()
     else:
         z = np.load(Path(__file__).resolve().parent / "golden" / "rotations.npz")
         Rg = np.empty_like(z["F"])
