@@ -77,8 +77,14 @@ constexpr int kFwdItemCols = 64;
 // Tiny supernodes (at most kTinyCols pivots and kTinyRows rows -- most of
 // them are leaves with one pivot) are solved one per thread in the per-level
 // launches: descriptor {moff_lo, moff_hi, roff, m, k, 0, 0, 0}.
-constexpr int kTinyCols = 4;
-constexpr int kTinyRows = 48;
+#ifndef PDGB_TINY_COLS
+#define PDGB_TINY_COLS 4
+#endif
+#ifndef PDGB_TINY_ROWS
+#define PDGB_TINY_ROWS 16
+#endif
+constexpr int kTinyCols = PDGB_TINY_COLS;
+constexpr int kTinyRows = PDGB_TINY_ROWS;
 constexpr int kFwdBlockRows = 128;
 constexpr int kFwdBlockCols = PDGB_FWDB_COLS;
 constexpr int kBwdBlockCols = PDGB_BWDB_COLS;
