@@ -289,6 +289,11 @@ int pdgb_set_rotation(pdgb_engine* e, int rotation);
 int pdgb_set_solve_mode(pdgb_engine* e, int mode);
 int pdgb_get_solve_mode(pdgb_engine* e, int* mode);
 
+/* Average device time of `launches` back-to-back local-step launches on
+ * the current state (the step prologue runs first; the state X, V is not
+ * changed).  For benchmarking the local step alone.  Waits for the GPU. */
+int pdgb_time_local(pdgb_engine* e, int launches, double* ms_per_launch);
+
 /* Tiles of the local step: at most max_tets tets each (32..512; 0 = 512).
  * Smaller tiles give small meshes more CTAs; vertex and tet order are
  * unchanged, so the state carries over.  Takes effect at the next step. */

@@ -754,6 +754,39 @@ double time_steps(pdgb_engine* e, int steps) {
 }
 }  // namespace
 
+int pdgb_time_local(pdgb_engine* e, int launches, double* ms_per_launch) {
+    if (!e || launches < 1 || launches > 100000 || !ms_per_launch) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine, launch count or output");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        if (!e->prepared) prepare(e);
+        // the step prologue fills sn and b from the current state; the local
+        // steps then read the same sn every launch (b only accumulates)
+        BeginArgs ba = begin_args(e);
+        launch_begin(ba, e->stream);
+        const LocalArgs la = local_args(e, nullptr);
+        const bool jf = e->prm.solver == PDGB_SOLVER_JACOBI;
+        launch_local(la, e->L.ntiles, jf, e->rotation, e->stream);  // warm-up
+        cudaEvent_t ev[2];
+        PDGB_CUDA_TRY(cudaEventCreate(&ev[0]));
+        PDGB_CUDA_TRY(cudaEventCreate(&ev[1]));
+        float ms = 0.f;
+        cudaError_t err = cudaEventRecord(ev[0], e->stream);
+        for (int k = 0; k < launches && err == cudaSuccess; ++k) {
+            launch_local(la, e->L.ntiles, jf, e->rotation, e->stream);
+            err = cudaGetLastError();
+        }
+        if (err == cudaSuccess) err = cudaEventRecord(ev[1], e->stream);
+        if (err == cudaSuccess) err = cudaEventSynchronize(ev[1]);
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        cudaEventDestroy(ev[0]);
+        cudaEventDestroy(ev[1]);
+        PDGB_CUDA_TRY(err);
+        *ms_per_launch = (double)ms / launches;
+    });
+}
+
 int pdgb_set_tile_size(pdgb_engine* e, int max_tets) {
     if (!e || max_tets < 0 || (max_tets > 0 && (max_tets < 32 || max_tets > kTileTets))) {
         set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or tile size (32..512, 0 = default)");

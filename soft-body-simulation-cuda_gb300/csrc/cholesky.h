@@ -78,10 +78,10 @@ constexpr int kFwdItemCols = 64;
 // them are leaves with one pivot) are solved one per thread in the per-level
 // launches: descriptor {moff_lo, moff_hi, roff, m, k, 0, 0, 0}.
 #ifndef PDGB_TINY_COLS
-#define PDGB_TINY_COLS 4
+#define PDGB_TINY_COLS 1
 #endif
 #ifndef PDGB_TINY_ROWS
-#define PDGB_TINY_ROWS 16
+#define PDGB_TINY_ROWS 32
 #endif
 constexpr int kTinyCols = PDGB_TINY_COLS;
 constexpr int kTinyRows = PDGB_TINY_ROWS;

@@ -225,6 +225,7 @@ SIGNATURES = {
     "pdgb_solve_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "pdgb_set_solve_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_set_tile_size": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_time_local": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double)]),
     "pdgb_closest_rotations": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
     "pdgb_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(pdgb_tune_report)]),
     "pdgb_get_solve_mode": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),

@@ -215,6 +215,12 @@ class PdSolver:
         """PDGB_SOLVE_AUTO / CTA / CLUSTER / LEVELS (schedule of the Cholesky solve)."""
         N.check(self._lib.pdgb_set_solve_mode(self._h, int(mode)), "pdgb_set_solve_mode")
 
+    def time_local(self, launches: int = 100) -> float:
+        """Average device ms of back-to-back local-step launches on the current state."""
+        ms = C.c_double()
+        N.check(self._lib.pdgb_time_local(self._h, int(launches), C.byref(ms)), "pdgb_time_local")
+        return ms.value
+
     def set_tile_size(self, max_tets: int) -> None:
         """Most tets per local-step tile (32..512; 0 = 512)."""
         N.check(self._lib.pdgb_set_tile_size(self._h, int(max_tets)), "pdgb_set_tile_size")
