@@ -79,9 +79,10 @@ struct HostLayout {
     std::vector<int> tile_tet_ptr;   // [ntiles+1]
     std::vector<int> tile_vptr;      // [ntiles+1]
     std::vector<uint32_t> tile_verts;  // internal vertex ids of each patch (sorted) | kPinnedBit
-    // per tile incidence lists: for patch vertex k of a tile, the tet corner
-    // slots (corner * kTileTets + local tet) it belongs to are inc_ent[4 t0 + inc_end[k-1]
-    // .. 4 t0 + inc_end[k]) (inc_end[-1] = 0), t0 = first tet of the tile.
+    // Slots of a tile: one per tet corner, ordered by patch vertex (then tet,
+    // then corner), so patch vertex k owns the slots inc_end[k-1] ..
+    // inc_end[k] (inc_end[-1] = 0); inc_ent[4 t + c] is the slot of corner c
+    // of tet t.
     std::vector<uint16_t> inc_ent;   // [4 nt]
     std::vector<uint16_t> inc_end;   // [sum of patch sizes]
     std::vector<float> geo;          // SoA [10][nt_pad]: DmInv row-major (9), V0*w

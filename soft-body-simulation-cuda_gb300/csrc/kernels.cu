@@ -16,39 +16,42 @@ namespace pdgb {
 
 // ------------------------------------------------------------ local step
 // One CTA per tile of Morton-ordered tets.  Shared memory holds one float4
-// slot per tet corner.  (1) Every patch vertex is loaded once (coalesced
-// over the sorted patch list) and written into the slots of the corners it
-// belongs to, following the tile's incidence list.  (2) Every tet reads its
-// 4 corner slots, computes F = Ds DmInv, the closest rotation R (minus F in
-// the Jacobi residual form) and the corner contributions c R DmInv^T G, and
-// overwrites its slots with them.  (3) Every patch vertex sums its slots in
-// the fixed incidence order and adds the sum to b with one float4 atomic
-// (pinned vertices are skipped: their RHS is the pin term).  No
-// shared-memory atomics; within a tile the sums are deterministic.
+// slot per tet corner, ordered by patch vertex: patch vertex k owns the
+// contiguous slots inc_end[k-1] .. inc_end[k].  (1) Every patch vertex is
+// loaded once (coalesced over the sorted patch list) and written into its
+// run of slots.  (2) Every tet reads its 4 corner slots (slot numbers
+// inc_ent[4 t + c], loaded with its geometry), computes F = Ds DmInv, the
+// closest rotation R (minus F in the Jacobi residual form) and the corner
+// contributions c R DmInv^T G, and overwrites its slots with them.  (3)
+// Every patch vertex sums its run of slots in order and adds the sum to b
+// with one float4 atomic (pinned vertices are skipped: their RHS is the pin
+// term).  No shared-memory atomics; within a tile the sums are
+// deterministic.
 template <bool kJacobiForm, int kRotation>
 __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4* slot) {
     const int vb = a.tile_vptr[tile];
     const int np = a.tile_vptr[tile + 1] - vb;
     const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
     const int ntile = t1 - t0;
-    const uint16_t* inc = a.inc_ent + 4 * (size_t)t0;
     const uint16_t* iend = a.inc_end + vb;
-    // Issue the per-tet geometry loads of this thread's tets first: they are
-    // in flight while the patch positions are gathered and scattered.
+    // Issue the per-tet geometry and slot-number loads of this thread's tets
+    // first: they are in flight while the patch positions are gathered.
     constexpr int kPer = kTileTets / kLocalThreads;
     const int ntp = a.nt_pad;
     float G[kPer][10];
+    uint2 S[kPer];
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
         const int lt = threadIdx.x + j * kLocalThreads;
         const int t = t0 + (lt < ntile ? lt : 0);
 #pragma unroll
         for (int k = 0; k < 10; ++k) G[j][k] = __ldg(&a.geo[k * ntp + t]);
+        S[j] = __ldg(reinterpret_cast<const uint2*>(a.inc_ent) + t);
     }
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
         const float4 p = __ldg(&a.sn[a.tile_verts[vb + k] & ~kPinnedBit]);
         const int e0 = k ? __ldg(&iend[k - 1]) : 0, e1 = __ldg(&iend[k]);
-        for (int e = e0; e < e1; ++e) slot[__ldg(&inc[e])] = p;
+        for (int e = e0; e < e1; ++e) slot[e] = p;
     }
     __syncthreads();
 #pragma unroll
@@ -57,8 +60,8 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         if (lt >= ntile) break;
         const float* D = G[j];
         const float c = G[j][9];
-        const float4 p0 = slot[lt], p1 = slot[kTileTets + lt], p2 = slot[2 * kTileTets + lt],
-                     p3 = slot[3 * kTileTets + lt];
+        const int s0 = S[j].x & 0xffff, s1 = S[j].x >> 16, s2 = S[j].y & 0xffff, s3 = S[j].y >> 16;
+        const float4 p0 = slot[s0], p1 = slot[s1], p2 = slot[s2], p3 = slot[s3];
         // Ds columns = edges; F = Ds * DmInv (row-major F[r][c])
         const float e[3][3] = {{p1.x - p0.x, p2.x - p0.x, p3.x - p0.x},
                                {p1.y - p0.y, p2.y - p0.y, p3.y - p0.y},
@@ -84,10 +87,10 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) M[3 * r + cc] = fmaf(r0, D[3 * cc], fmaf(r1, D[3 * cc + 1], r2 * D[3 * cc + 2]));
         }
-        slot[lt] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
-        slot[kTileTets + lt] = make_float4(M[0], M[3], M[6], 0.f);
-        slot[2 * kTileTets + lt] = make_float4(M[1], M[4], M[7], 0.f);
-        slot[3 * kTileTets + lt] = make_float4(M[2], M[5], M[8], 0.f);
+        slot[s0] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
+        slot[s1] = make_float4(M[0], M[3], M[6], 0.f);
+        slot[s2] = make_float4(M[1], M[4], M[7], 0.f);
+        slot[s3] = make_float4(M[2], M[5], M[8], 0.f);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
@@ -96,7 +99,7 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         const int e0 = k ? __ldg(&iend[k - 1]) : 0, e1 = __ldg(&iend[k]);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         for (int e = e0; e < e1; ++e) {
-            const float4 q = slot[__ldg(&inc[e])];
+            const float4 q = slot[e];
             sx += q.x;
             sy += q.y;
             sz += q.z;
@@ -107,7 +110,7 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
 
 // Resident CTAs per SM the register allocation of the local step aims for.
 #ifndef PDGB_LOCAL_MIN_BLOCKS
-#define PDGB_LOCAL_MIN_BLOCKS 1
+#define PDGB_LOCAL_MIN_BLOCKS 4
 #endif
 
 template <bool kJacobiForm, int kRotation>

@@ -96,10 +96,13 @@ void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
             for (int c = 0; c < 4; ++c) cnt[loc[L.tets_int[4 * (size_t)i + c]] + 1]++;
         for (int k = 0; k < np; ++k) cnt[k + 1] += cnt[k];
         for (int k = 0; k < np; ++k) L.inc_end.push_back((uint16_t)cnt[k + 1]);
+        // slot of each tet corner: its position in the tile's vertex-sorted
+        // incidence order, so that a patch vertex's corners are one
+        // contiguous run of slots
         for (int i = start; i < end; ++i)
             for (int c = 0; c < 4; ++c) {
                 const int k = loc[L.tets_int[4 * (size_t)i + c]];
-                L.inc_ent[4 * (size_t)start + cnt[k]++] = (uint16_t)(c * kTileTets + (i - start));
+                L.inc_ent[4 * (size_t)i + c] = (uint16_t)(cnt[k]++);
             }
         for (int v : patch) {
             const int o = L.vperm[v];
