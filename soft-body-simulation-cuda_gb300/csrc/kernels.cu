@@ -48,10 +48,20 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         for (int k = 0; k < 10; ++k) G[j][k] = __ldg(&a.geo[k * ntp + t]);
         S[j] = __ldg(reinterpret_cast<const uint2*>(a.inc_ent) + t);
     }
+    // the first patch vertex of each thread keeps its id and slot run in
+    // registers for the gather phase
+    uint32_t v_first = kPinnedBit;
+    int e0_first = 0, e1_first = 0;
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
-        const float4 p = __ldg(&a.sn[a.tile_verts[vb + k] & ~kPinnedBit]);
+        const uint32_t v = __ldg(&a.tile_verts[vb + k]);
+        const float4 p = __ldg(&a.sn[v & ~kPinnedBit]);
         const int e0 = k ? __ldg(&iend[k - 1]) : 0, e1 = __ldg(&iend[k]);
         for (int e = e0; e < e1; ++e) slot[e] = p;
+        if (k == (int)threadIdx.x) {
+            v_first = v;
+            e0_first = e0;
+            e1_first = e1;
+        }
     }
     __syncthreads();
 #pragma unroll
@@ -94,9 +104,11 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
     }
     __syncthreads();
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
-        const uint32_t v = a.tile_verts[vb + k];
+        const bool first = k == (int)threadIdx.x;
+        const uint32_t v = first ? v_first : __ldg(&a.tile_verts[vb + k]);
         if (v & kPinnedBit) continue;
-        const int e0 = k ? __ldg(&iend[k - 1]) : 0, e1 = __ldg(&iend[k]);
+        const int e0 = first ? e0_first : (k ? __ldg(&iend[k - 1]) : 0);
+        const int e1 = first ? e1_first : __ldg(&iend[k]);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         for (int e = e0; e < e1; ++e) {
             const float4 q = slot[e];
