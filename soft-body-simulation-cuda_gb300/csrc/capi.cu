@@ -57,7 +57,9 @@ struct pdgb_engine {
     CholFactor chol;
     int chol_ordering = -1;
     float chol_dt = 0.f, chol_pw = -1.f;
-    DBuf<int> ch_fwd, ch_bwd, ch_rows, ch_body_level, ch_body_order, ch_fwdb, ch_bwdb, ch_fwds, ch_bwds, ch_tiny;
+    DBuf<int> ch_fwd, ch_bwd, ch_rows, ch_body_level, ch_body_order, ch_fwdb, ch_bwdb, ch_fwds, ch_bwds, ch_tiny,
+        ch_zstage;
+    DBuf<float4> ch_zbuf;
     DBuf<int4> ch_levels;
     DBuf<float> ch_mval;
     DBuf<int> k_rowptr, k_colind;  // FP64 K for refinement residuals
@@ -245,7 +247,7 @@ void record_chol_step(pdgb_engine* e) {
     const LocalArgs la = local_args(e, &st->done);
     CholArgs ca{e->ch_fwd.p, e->ch_bwd.p, e->ch_rows.p, e->ch_mval.p, e->ch_levels.p, e->ch_body_level.p,
                 e->ch_body_order.p, e->b.p, e->y.p, e->sn.p, &st->done, e->ch_fwdb.p, e->ch_bwdb.p,
-                e->ch_fwds.p, e->ch_bwds.p, e->ch_tiny.p};
+                e->ch_fwds.p, e->ch_bwds.p, e->ch_tiny.p, e->ch_zstage.p, e->ch_zbuf.p};
     CholVertexArgs cv{};
     cv.nv = e->nv;
     cv.tol = use_tol ? e->prm.tol : 0.f;
@@ -396,6 +398,8 @@ void prepare_cholesky(pdgb_engine* e) {
     e->ch_fwds.upload(f.fwd_small, s);
     e->ch_bwds.upload(f.bwd_small, s);
     e->ch_tiny.upload(f.tiny, s);
+    e->ch_zstage.upload(f.zstage, s);
+    e->ch_zbuf.alloc((size_t)std::max<int64_t>(f.zrows, 1));
     e->ch_rows.upload(f.rows, s);
     e->ch_mval.upload(f.mval, s);
     std::vector<int4> lv(f.levels.size());
@@ -1245,7 +1249,7 @@ int solve_launches(const pdgb_engine* e) {
     int n = 0;
     for (const SolveLevel& v : e->chol.step_levels)
         n += (v.fwdb_end > v.fwdb_begin) + (v.fwdw_end > v.fwdw_begin) + (v.bwdb_end > v.bwdb_begin) +
-             (v.bwdw_end > v.bwdw_begin) + 2 * (v.tiny_end > v.tiny_begin);
+             (v.bwdw_end > v.bwdw_begin) + 2 * (v.tiny_end > v.tiny_begin) + (v.zst_end > v.zst_begin);
     return n;
 }
 }  // namespace

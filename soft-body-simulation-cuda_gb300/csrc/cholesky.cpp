@@ -652,6 +652,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         lv.fwdw_begin = (int)(out.fwd_small.size() / kItemInts);
         lv.bwdw_begin = (int)(out.bwd_small.size() / kItemInts);
         lv.tiny_begin = (int)(out.tiny.size() / kItemInts);
+        lv.zst_begin = (int)(out.zstage.size() / kItemInts);
         for (int s : bylevel[L]) {
             const int k = out.sk[s], m = out.sm[s];
             const int64_t mo = out.moff[s];
@@ -684,9 +685,12 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
                     out.fwd_blocks.insert(out.fwd_blocks.end(),
                                           {lo, hi, out.roff[s], m, k, r0, c0, std::min(cmax, c0 + kFwdBlockCols)});
             }
+            const int zoff = (int)out.zrows;
+            out.zrows += m;
+            out.zstage.insert(out.zstage.end(), {lo, hi, out.roff[s], m, k, 0, 0, zoff});
             for (int c0 = 0; c0 < k; c0 += kBwdBlockCols)
                 out.bwd_blocks.insert(out.bwd_blocks.end(),
-                                      {lo, hi, out.roff[s], m, k, c0, std::min(k, c0 + kBwdBlockCols), 0});
+                                      {lo, hi, out.roff[s], m, k, c0, std::min(k, c0 + kBwdBlockCols), zoff});
         }
         lv.fwd_end = (int)(out.fwd_items.size() / kItemInts);
         lv.bwd_end = (int)(out.bwd_items.size() / kItemInts);
@@ -695,6 +699,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
         lv.fwdw_end = (int)(out.fwd_small.size() / kItemInts);
         lv.bwdw_end = (int)(out.bwd_small.size() / kItemInts);
         lv.tiny_end = (int)(out.tiny.size() / kItemInts);
+        lv.zst_end = (int)(out.zstage.size() / kItemInts);
         out.levels[L] = lv;
     }
     out.body_level = {0, nl};
@@ -734,11 +739,11 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
                                        (failed[b] == PDGB_ERR_NOT_SPD ? "not positive definite" : "error") + ")"};
     out = CholFactor();
     out.n = vstart[nbodies];
-    int64_t mbase = 0, rbase = 0;
+    int64_t mbase = 0, rbase = 0, zbase = 0;
     int sbase = 0;
     out.body_level.assign(1, 0);
     // per-level buckets of the block / small items of all bodies
-    std::vector<std::vector<int>> bfb, bfw, bbb, bbw, btn;
+    std::vector<std::vector<int>> bfb, bfw, bbb, bbw, btn, bzs;
     for (int b = 0; b < nbodies; ++b) {
         CholFactor& f = fs[b];
         const int v0 = vstart[b];
@@ -756,14 +761,15 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         out.nsuper += f.nsuper;
         out.mval.insert(out.mval.end(), f.mval.begin(), f.mval.end());
         for (int r : f.rows) out.rows.push_back(r + v0);
-        auto shift = [&](std::vector<int>& dst, const std::vector<int>& src) {
+        auto shift = [&](std::vector<int>& dst, const std::vector<int>& src, bool zfield = false) {
             const int base_item = (int)(dst.size() / kItemInts);
             for (size_t i = 0; i < src.size(); i += kItemInts) {
                 const int64_t mo = ((int64_t)(uint32_t)src[i] | ((int64_t)src[i + 1] << 32)) + mbase;
                 dst.push_back((int)(mo & 0xffffffff));
                 dst.push_back((int)(mo >> 32));
                 dst.push_back(src[i + 2] + (int)rbase);
-                for (int j = 3; j < kItemInts; ++j) dst.push_back(src[i + j]);
+                for (int j = 3; j < kItemInts - 1; ++j) dst.push_back(src[i + j]);
+                dst.push_back(src[i + kItemInts - 1] + (zfield ? (int)zbase : 0));
             }
             return base_item;
         };
@@ -775,27 +781,31 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         if ((int)bfb.size() < f.nlevels) {
             bfb.resize(f.nlevels); bfw.resize(f.nlevels); bbb.resize(f.nlevels); bbw.resize(f.nlevels);
             btn.resize(f.nlevels);
+            bzs.resize(f.nlevels);
         }
         for (int L = 0; L < (int)f.levels.size(); ++L) {
             const SolveLevel& lv = f.levels[L];
             out.levels.push_back({lv.fwd_begin + fb, lv.fwd_end + fb, lv.bwd_begin + bb, lv.bwd_end + bb,
-                                  0, 0, 0, 0, 0, 0, 0, 0, 0, 0});
+                                  0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0});
             shift(btn[L], slice(f.tiny, lv.tiny_begin, lv.tiny_end));
+            shift(bzs[L], slice(f.zstage, lv.zst_begin, lv.zst_end), true);
             shift(bfb[L], slice(f.fwd_blocks, lv.fwdb_begin, lv.fwdb_end));
             shift(bfw[L], slice(f.fwd_small, lv.fwdw_begin, lv.fwdw_end));
-            shift(bbb[L], slice(f.bwd_blocks, lv.bwdb_begin, lv.bwdb_end));
+            shift(bbb[L], slice(f.bwd_blocks, lv.bwdb_begin, lv.bwdb_end), true);
             shift(bbw[L], slice(f.bwd_small, lv.bwdw_begin, lv.bwdw_end));
         }
         out.body_level.push_back((int)out.levels.size());
         mbase += (int64_t)f.mval.size();
         rbase += (int64_t)f.rows.size();
+        zbase += f.zrows;
+        out.zrows += f.zrows;
         sbase += f.nsuper;
         out.K.n = 0;  // per-body systems are not kept
         f = CholFactor();  // release the per-body copy
     }
     (void)sbase;
     for (size_t L = 0; L < bfb.size(); ++L) {
-        SolveLevel lv{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        SolveLevel lv{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         auto put = [&](std::vector<int>& dst, std::vector<int>& src, int& b0, int& b1) {
             b0 = (int)(dst.size() / kItemInts);
             dst.insert(dst.end(), src.begin(), src.end());
@@ -807,6 +817,7 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         put(out.bwd_blocks, bbb[L], lv.bwdb_begin, lv.bwdb_end);
         put(out.bwd_small, bbw[L], lv.bwdw_begin, lv.bwdw_end);
         put(out.tiny, btn[L], lv.tiny_begin, lv.tiny_end);
+        put(out.zstage, bzs[L], lv.zst_begin, lv.zst_end);
         out.step_levels.push_back(lv);
     }
     std::vector<std::pair<int64_t, int>> sz(nbodies);

@@ -48,6 +48,7 @@ struct SolveLevel {
     int fwdw_begin, fwdw_end;  // per-level launches: warp items of the small supernodes
     int bwdw_begin, bwdw_end;
     int tiny_begin, tiny_end;  // per-level launches: tiny supernodes, one thread each
+    int zst_begin, zst_end;    // per-level launches: backward z staging of the block supernodes
 };
 
 // Warp work items, 8 ints each (two int4 loads, no dependent metadata loads):
@@ -61,8 +62,10 @@ constexpr int kFwdItemCols = 64;
 // CTA block items (same 8-int layout) of the per-level launches:
 //   forward : {moff_lo, moff_hi, roff, m, k, r0, c0, c1}: rows r0 .. r0+128,
 //             pivot columns c0 .. c1 (at most 256, staged in shared memory)
-//   backward: {moff_lo, moff_hi, roff, m, k, c0, c1, 0}: pivot columns
-//             c0 .. c1 (at most 16) against the staged rows c0 .. m
+//   backward: {moff_lo, moff_hi, roff, m, k, c0, c1, zoff}: pivot columns
+//             c0 .. c1 against z = [y_pivots ; -x_offdiag] of the supernode,
+//             staged once per level at zbuf[zoff ..] by a z-staging item
+//             {moff_lo, moff_hi, roff, m, k, 0, 0, zoff}
 // Supernodes with at least kBlockMinRows rows use block items in the
 // per-level launches; smaller ones keep warp items (packed 4 per CTA).
 #ifndef PDGB_FWDB_COLS
@@ -111,6 +114,8 @@ struct CholFactor {
     std::vector<int> fwd_small;      // warp items of the small supernodes (per-level launches)
     std::vector<int> bwd_small;
     std::vector<int> tiny;           // tiny supernode descriptors (per-level launches)
+    std::vector<int> zstage;         // backward z-staging items of the block supernodes
+    int64_t zrows = 0;               // rows of the z staging buffer
     std::vector<SolveLevel> levels;  // body-major: body b owns levels[body_level[b] .. body_level[b+1])
     // Per-level launches (block and small items): level L of every body in
     // one launch, levels counted from the leaves.  Equal to `levels` for a

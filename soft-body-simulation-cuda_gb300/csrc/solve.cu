@@ -143,65 +143,59 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
     else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
 }
 
-// Backward block {moff, roff, m, k, c0, c1}: z = [y_pivots ; -x_offdiag]
-// over rows c0 .. m is staged in shared memory (kBwdStageRows at a time,
-// one gather per row for the whole block); warp w owns columns
-// c0 + w, c0 + w + 4, ...; lanes stride a column of M_s (contiguous) with 4
-// independent loads in flight, then a warp reduction.
+// Backward z staging {roff, m, k, zoff}: z = [y_pivots ; -x_offdiag] over
+// the supernode's rows, gathered once per level into zbuf[zoff ..] so that
+// the backward blocks of all its column groups read it contiguously.
+__global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, int item0) {
+    if (a.done && *a.done) return;
+    const int* w = a.zstage + (size_t)kItemInts * (item0 + blockIdx.x);
+    const int roff = __ldg(w + 2), m = __ldg(w + 3), k = __ldg(w + 4), zoff = __ldg(w + 7);
+    const int* rows = a.rows + roff;
+    for (int i = threadIdx.x; i < m; i += kStageThreads) {
+        const int vid = __ldg(&rows[i]);
+        float4 z;
+        if (i < k) z = a.y[vid];
+        else {
+            const float4 xv = a.x[vid];
+            z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+        }
+        a.zbuf[zoff + i] = z;
+    }
+}
+
+// Backward block {moff, roff, m, k, c0, c1, zoff}: warp w owns columns
+// c0 + w, c0 + w + 4, ...; lanes stride a column of M_s and the staged z
+// (both contiguous), 4 independent load pairs in flight, then a warp
+// reduction.
 __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
-    __shared__ float4 z[kBwdStageRows];
     if (a.done && *a.done) return;
     const int* w = a.bwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
-    const int roff = h0.z, m = h0.w, k = h1.x, c0 = h1.y, c1 = h1.z;
+    const int roff = h0.z, m = h0.w, c0 = h1.y, c1 = h1.z, zoff = h1.w;
     const int* rows = a.rows + roff;
+    const float4* z = a.zbuf + zoff;
     constexpr int kWarps = kBlockThreads / 32;
-    constexpr int kCols = kBwdBlockCols / kWarps;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float acc[kCols][3];
-#pragma unroll
-    for (int j = 0; j < kCols; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
-    for (int z0 = c0; z0 < m; z0 += kBwdStageRows) {
-        const int zn = min(kBwdStageRows, m - z0);
-        __syncthreads();  // the previous pass is consumed
-        for (int i = threadIdx.x; i < zn; i += kBlockThreads) {
-            const int r = z0 + i;
-            const int vid = __ldg(&rows[r]);
-            if (r < k) z[i] = a.y[vid];
-            else {
-                const float4 xv = a.x[vid];
-                z[i] = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
-            }
-        }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < kCols; ++j) {
-            const int c = c0 + warp + kWarps * j;
-            if (c >= c1) break;
-            const float* Mc = a.mval + moff + (size_t)c * m;
-            const int i0 = max(z0, c);
+    for (int c = c0 + warp; c < c1; c += kWarps) {
+        const float* Mc = a.mval + moff + (size_t)c * m;
+        float ax = 0.f, ay = 0.f, az = 0.f;
 #pragma unroll 4
-            for (int i = i0 + lane; i < z0 + zn; i += 32) {
-                const float mv = __ldg(Mc + i);
-                const float4 zz = z[i - z0];
-                acc[j][0] = fmaf(mv, zz.x, acc[j][0]);
-                acc[j][1] = fmaf(mv, zz.y, acc[j][1]);
-                acc[j][2] = fmaf(mv, zz.z, acc[j][2]);
-            }
+        for (int i = c + lane; i < m; i += 32) {
+            const float mv = __ldg(Mc + i);
+            const float4 zz = z[i];
+            ax = fmaf(mv, zz.x, ax);
+            ay = fmaf(mv, zz.y, ay);
+            az = fmaf(mv, zz.z, az);
         }
-    }
-#pragma unroll
-    for (int j = 0; j < kCols; ++j) {
-        const int c = c0 + warp + kWarps * j;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
-            acc[j][0] += __shfl_xor_sync(0xffffffffu, acc[j][0], off);
-            acc[j][1] += __shfl_xor_sync(0xffffffffu, acc[j][1], off);
-            acc[j][2] += __shfl_xor_sync(0xffffffffu, acc[j][2], off);
+            ax += __shfl_xor_sync(0xffffffffu, ax, off);
+            ay += __shfl_xor_sync(0xffffffffu, ay, off);
+            az += __shfl_xor_sync(0xffffffffu, az, off);
         }
-        if (lane == 0 && c < c1) a.x[__ldg(&rows[c])] = make_float4(acc[j][0], acc[j][1], acc[j][2], 0.f);
+        if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
     }
 }
 
@@ -308,6 +302,8 @@ void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& 
     for (size_t L = levels.size(); L-- > 0;) {
         const SolveLevel& v = levels[L];
         const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin, nt = v.tiny_end - v.tiny_begin;
+        const int nz = v.zst_end - v.zst_begin;
+        if (nz > 0) k_chol_bwd_zstage<<<nz, kStageThreads, 0, s>>>(a, v.zst_begin);
         if (nb > 0) k_chol_bwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.bwdb_begin);
         if (nw > 0) k_chol_bwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.bwdw_begin, nw);
         if (nt > 0) k_chol_bwd_tiny<<<(nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s>>>(a, v.tiny_begin, nt);

@@ -32,11 +32,13 @@ struct CholArgs {
     const int* fwd_small;   // warp items of small supernodes (per-level launches)
     const int* bwd_small;
     const int* tiny;        // tiny supernode descriptors (per-level launches)
+    const int* zstage;      // backward z-staging items (per-level launches)
+    float4* zbuf;           // staged z of the block supernodes
 };
 
 constexpr int kBlockThreads = 128;      // block-item kernels: 4 warps
 constexpr int kSmallThreads = 256;      // small-supernode kernels: one warp item per warp
-constexpr int kBwdStageRows = 2048;     // rows of z staged per pass of a backward block
+constexpr int kStageThreads = 128;      // backward z staging: one CTA per block supernode
 
 // Convergence state of one step of the Cholesky path (device memory).
 struct StepState {
