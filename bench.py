@@ -297,6 +297,9 @@ def run_serving(args):
 
     torch.cuda.set_device(local)
     wl = dict(WORKLOADS["c5"])
+    if args.rate > 0:
+        wl["rate"] = args.rate
+        wl["workload"] += f"_rate{args.rate:g}"
     rng = np.random.default_rng(5)
     pool = [mesh.request_body(math.exp(rng.uniform(math.log(1e3), math.log(3e5))), rng) for _ in range(48)]
     window = args.window
@@ -314,6 +317,7 @@ def run_serving(args):
         srv.tick()
     base_completed = srv.stats()["completed"]
     base_ti = srv.stats()["tet_iterations"]
+    base_busy = srv.stats()["busy_ms"]
     ids = []
     t0 = time.perf_counter()
     nxt = 0
@@ -369,6 +373,12 @@ def run_serving(args):
         "wall_s": wall, "completed": int(st["completed"] - base_completed), "failed": int(st["failed"]),
         "alone_vs_mix_max_rel_err": worst_alone, "alone_vs_mix_sample": len(sample),
         "accuracy": acc, "clocks": clocks.summary(),
+        "busy_frac": float(st["busy_ms"] - base_busy) / 1e3 / wall,
+        "e2e": {"value": value, "unit": UNIT,
+                "h2d_bytes_per_request": float(np.mean([48 * pool[p].num_verts + 28 * pool[p].num_tets
+                                                        for _, p, _ in ids])) if ids else 0.0,
+                "d2h_bytes_per_request": float(np.mean([24 * pool[p].num_verts for _, p, _ in ids])) if ids else 0.0,
+                "note": "requests enter as host meshes and leave as host arrays: the serving value is end to end"},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -407,6 +417,7 @@ def main():
                     "reference harness is built")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-oracle error report")
     ap.add_argument("--window", type=float, default=20.0, help="arrival window of the serving workload, seconds")
+    ap.add_argument("--rate", type=float, default=0.0, help="serving: mean arrivals per second (0 = the workload's)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "pdgb":
         args.warmup = 3

@@ -687,7 +687,8 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
             }
             const int zoff = (int)out.zrows;
             out.zrows += m;
-            out.zstage.insert(out.zstage.end(), {lo, hi, out.roff[s], m, k, 0, 0, zoff});
+            for (int r0 = 0; r0 < m; r0 += kStageRows)
+                out.zstage.insert(out.zstage.end(), {lo, hi, out.roff[s], m, k, r0, 0, zoff});
             for (int c0 = 0; c0 < k; c0 += kBwdBlockCols)
                 out.bwd_blocks.insert(out.bwd_blocks.end(),
                                       {lo, hi, out.roff[s], m, k, c0, std::min(k, c0 + kBwdBlockCols), zoff});

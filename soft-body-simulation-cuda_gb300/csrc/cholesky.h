@@ -64,8 +64,8 @@ constexpr int kFwdItemCols = 64;
 //             pivot columns c0 .. c1 (at most 256, staged in shared memory)
 //   backward: {moff_lo, moff_hi, roff, m, k, c0, c1, zoff}: pivot columns
 //             c0 .. c1 against z = [y_pivots ; -x_offdiag] of the supernode,
-//             staged once per level at zbuf[zoff ..] by a z-staging item
-//             {moff_lo, moff_hi, roff, m, k, 0, 0, zoff}
+//             staged once per level at zbuf[zoff ..] by z-staging items
+//             {moff_lo, moff_hi, roff, m, k, r0, 0, zoff} of kStageRows rows
 // Supernodes with at least kBlockMinRows rows use block items in the
 // per-level launches; smaller ones keep warp items (packed 4 per CTA).
 #ifndef PDGB_FWDB_COLS
@@ -91,6 +91,7 @@ constexpr int kTinyRows = PDGB_TINY_ROWS;
 constexpr int kFwdBlockRows = 128;
 constexpr int kFwdBlockCols = PDGB_FWDB_COLS;
 constexpr int kBwdBlockCols = PDGB_BWDB_COLS;
+constexpr int kStageRows = 128;
 constexpr int kBlockMinRows = PDGB_BLOCK_MIN_ROWS;
 
 struct CholFactor {

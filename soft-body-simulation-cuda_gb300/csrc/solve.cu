@@ -143,15 +143,17 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
     else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
 }
 
-// Backward z staging {roff, m, k, zoff}: z = [y_pivots ; -x_offdiag] over
-// the supernode's rows, gathered once per level into zbuf[zoff ..] so that
-// the backward blocks of all its column groups read it contiguously.
+// Backward z staging {roff, m, k, r0, zoff}: z = [y_pivots ; -x_offdiag]
+// over rows r0 .. r0 + kStageRows of the supernode, gathered once per level
+// into zbuf[zoff ..] so that the backward blocks of all its column groups
+// read it contiguously.
 __global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, int item0) {
     if (a.done && *a.done) return;
     const int* w = a.zstage + (size_t)kItemInts * (item0 + blockIdx.x);
-    const int roff = __ldg(w + 2), m = __ldg(w + 3), k = __ldg(w + 4), zoff = __ldg(w + 7);
+    const int roff = __ldg(w + 2), m = __ldg(w + 3), k = __ldg(w + 4), r0 = __ldg(w + 5), zoff = __ldg(w + 7);
     const int* rows = a.rows + roff;
-    for (int i = threadIdx.x; i < m; i += kStageThreads) {
+    const int r1 = min(m, r0 + kStageRows);
+    for (int i = r0 + threadIdx.x; i < r1; i += kStageThreads) {
         const int vid = __ldg(&rows[i]);
         float4 z;
         if (i < k) z = a.y[vid];
