@@ -71,8 +71,8 @@ constexpr int kFwdItemCols = 64;
 #ifndef PDGB_FWDB_COLS
 #define PDGB_FWDB_COLS 16
 #endif
-#ifndef PDGB_BWDB_COLS
-#define PDGB_BWDB_COLS 4
+#ifndef PDGB_BWD_WARP_COLS
+#define PDGB_BWD_WARP_COLS 4
 #endif
 #ifndef PDGB_BLOCK_MIN_ROWS
 #define PDGB_BLOCK_MIN_ROWS 64
@@ -90,7 +90,8 @@ constexpr int kTinyCols = PDGB_TINY_COLS;
 constexpr int kTinyRows = PDGB_TINY_ROWS;
 constexpr int kFwdBlockRows = 128;
 constexpr int kFwdBlockCols = PDGB_FWDB_COLS;
-constexpr int kBwdBlockCols = PDGB_BWDB_COLS;
+constexpr int kBwdWarpCols = PDGB_BWD_WARP_COLS;   // backward block: columns per warp (4 warps)
+constexpr int kBwdBlockCols = 4 * kBwdWarpCols;
 constexpr int kStageRows = 128;
 constexpr int kBlockMinRows = PDGB_BLOCK_MIN_ROWS;
 

@@ -165,10 +165,11 @@ __global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, i
     }
 }
 
-// Backward block {moff, roff, m, k, c0, c1, zoff}: warp w owns columns
-// c0 + w, c0 + w + 4, ...; lanes stride a column of M_s and the staged z
-// (both contiguous), 4 independent load pairs in flight, then a warp
-// reduction.
+// Backward block {moff, roff, m, k, c0, c1, zoff}: warp w owns the
+// kBwdWarpCols consecutive columns c0 + kBwdWarpCols w ..; lanes stride the
+// rows, each z (staged, contiguous) is loaded once and used for all of the
+// warp's columns (contiguous loads of M_s, one per column), then a warp
+// reduction per column.  Column c uses rows i >= c only.
 __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
     if (a.done && *a.done) return;
     const int* w = a.bwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
@@ -178,26 +179,36 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
     const int roff = h0.z, m = h0.w, c0 = h1.y, c1 = h1.z, zoff = h1.w;
     const int* rows = a.rows + roff;
     const float4* z = a.zbuf + zoff;
-    constexpr int kWarps = kBlockThreads / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = c0 + warp; c < c1; c += kWarps) {
-        const float* Mc = a.mval + moff + (size_t)c * m;
-        float ax = 0.f, ay = 0.f, az = 0.f;
-#pragma unroll 4
-        for (int i = c + lane; i < m; i += 32) {
-            const float mv = __ldg(Mc + i);
-            const float4 zz = z[i];
-            ax = fmaf(mv, zz.x, ax);
-            ay = fmaf(mv, zz.y, ay);
-            az = fmaf(mv, zz.z, az);
+    const int cw = c0 + kBwdWarpCols * warp;  // first column of this warp
+    if (cw >= c1) return;
+    const int nc = min(kBwdWarpCols, c1 - cw);
+    const float* Mc = a.mval + moff + (size_t)cw * m;
+    float acc[kBwdWarpCols][3];
+#pragma unroll
+    for (int j = 0; j < kBwdWarpCols; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
+#pragma unroll 2
+    for (int i = cw + lane; i < m; i += 32) {
+        const float4 zz = z[i];
+#pragma unroll
+        for (int j = 0; j < kBwdWarpCols; ++j) {
+            if (j < nc && i >= cw + j) {
+                const float mv = __ldg(Mc + (size_t)j * m + i);
+                acc[j][0] = fmaf(mv, zz.x, acc[j][0]);
+                acc[j][1] = fmaf(mv, zz.y, acc[j][1]);
+                acc[j][2] = fmaf(mv, zz.z, acc[j][2]);
+            }
         }
+    }
+#pragma unroll
+    for (int j = 0; j < kBwdWarpCols; ++j) {
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
-            ax += __shfl_xor_sync(0xffffffffu, ax, off);
-            ay += __shfl_xor_sync(0xffffffffu, ay, off);
-            az += __shfl_xor_sync(0xffffffffu, az, off);
+            acc[j][0] += __shfl_xor_sync(0xffffffffu, acc[j][0], off);
+            acc[j][1] += __shfl_xor_sync(0xffffffffu, acc[j][1], off);
+            acc[j][2] += __shfl_xor_sync(0xffffffffu, acc[j][2], off);
         }
-        if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
+        if (lane == 0 && j < nc) a.x[__ldg(&rows[cw + j])] = make_float4(acc[j][0], acc[j][1], acc[j][2], 0.f);
     }
 }
 

@@ -38,7 +38,7 @@ struct CholArgs {
 
 constexpr int kBlockThreads = 128;      // block-item kernels: 4 warps
 constexpr int kSmallThreads = 256;      // small-supernode kernels: one warp item per warp
-constexpr int kStageThreads = 128;      // backward z staging: one CTA per block supernode
+constexpr int kStageThreads = 128;      // backward z staging: one CTA per 128-row chunk (kStageRows)
 
 // Convergence state of one step of the Cholesky path (device memory).
 struct StepState {
