@@ -469,7 +469,7 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
             // 2. one PD step for every active request
             PDGB_CUDA_TRY(cudaGraphLaunch(S->gexec, S->stream));
             // 3. retire finished requests
-            std::vector<Request*> keep;
+            std::vector<Request*> keep, retired;
             for (Request* r : S->active) {
                 r->steps_done++;
                 S->tet_iterations += (double)r->nt * S->cfg.params.num_iterations;
@@ -487,6 +487,7 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
                     S->bytes_in_use -= r->bytes;
                     r->state = kDone;
                     S->lists_dirty = true;
+                    retired.push_back(r);
                     done_now++;
                 } else {
                     keep.push_back(r);
@@ -495,13 +496,10 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
             S->active.swap(keep);
             PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));
             const auto now = Clock::now();
-            for (auto& kv : S->reqs) {
-                Request* r = kv.second.get();
-                if (r->state == kDone && r->t_done == Clock::time_point{}) {
-                    r->t_done = now;
-                    S->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
-                    S->completed++;
-                }
+            for (Request* r : retired) {  // results are on the host now
+                r->t_done = now;
+                S->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
+                S->completed++;
             }
             PDGB_CUDA_TRY(cudaGetLastError());
         }
