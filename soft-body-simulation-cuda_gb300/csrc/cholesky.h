@@ -72,7 +72,12 @@ constexpr int kFwdItemCols = 64;
 #define PDGB_FWDB_COLS 16
 #endif
 #ifndef PDGB_BWD_WARP_COLS
-#define PDGB_BWD_WARP_COLS 4
+#define PDGB_BWD_WARP_COLS 2
+#endif
+// Backward blocks read z from the per-level staging buffer (1) or gather it
+// themselves, once per warp for all of the warp's columns (0).
+#ifndef PDGB_BWD_ZSTAGE
+#define PDGB_BWD_ZSTAGE 1
 #endif
 #ifndef PDGB_BLOCK_MIN_ROWS
 #define PDGB_BLOCK_MIN_ROWS 64

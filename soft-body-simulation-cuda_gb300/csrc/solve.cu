@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
     const int roff = h0.z, m = h0.w, c0 = h1.y, c1 = h1.z, zoff = h1.w;
     const int* rows = a.rows + roff;
     const float4* z = a.zbuf + zoff;
+    (void)z;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cw = c0 + kBwdWarpCols * warp;  // first column of this warp
     if (cw >= c1) return;
@@ -189,7 +190,17 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
     for (int j = 0; j < kBwdWarpCols; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
 #pragma unroll 2
     for (int i = cw + lane; i < m; i += 32) {
+#if PDGB_BWD_ZSTAGE
         const float4 zz = z[i];
+#else
+        const int vid = __ldg(&rows[i]);
+        float4 zz;
+        if (i < h1.x) zz = a.y[vid];
+        else {
+            const float4 xv = a.x[vid];
+            zz = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+        }
+#endif
 #pragma unroll
         for (int j = 0; j < kBwdWarpCols; ++j) {
             if (j < nc && i >= cw + j) {
@@ -315,7 +326,7 @@ void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& 
     for (size_t L = levels.size(); L-- > 0;) {
         const SolveLevel& v = levels[L];
         const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin, nt = v.tiny_end - v.tiny_begin;
-        const int nz = v.zst_end - v.zst_begin;
+        const int nz = PDGB_BWD_ZSTAGE ? v.zst_end - v.zst_begin : 0;
         if (nz > 0) k_chol_bwd_zstage<<<nz, kStageThreads, 0, s>>>(a, v.zst_begin);
         if (nb > 0) k_chol_bwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.bwdb_begin);
         if (nw > 0) k_chol_bwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.bwdw_begin, nw);
