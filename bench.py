@@ -321,9 +321,15 @@ def run_serving(args):
     ids = []
     t0 = time.perf_counter()
     nxt = 0
+    trace, next_trace = [], 0.0
     with ClockSampler(local) as clocks:
         while True:
             now = time.perf_counter() - t0
+            if now >= next_trace:  # queue state once a second
+                sn = srv.stats()
+                trace.append([round(now, 1), sn["active"], sn["waiting"], sn["ready"],
+                              int(sn["completed"] - base_completed)])
+                next_trace += 1.0
             while nxt < n_req and arrivals[nxt] <= now:
                 ids.append((srv.submit(pool[picks[nxt]], int(ksteps[nxt])), int(picks[nxt]), int(ksteps[nxt])))
                 nxt += 1
@@ -374,6 +380,8 @@ def run_serving(args):
         "alone_vs_mix_max_rel_err": worst_alone, "alone_vs_mix_sample": len(sample),
         "accuracy": acc, "clocks": clocks.summary(),
         "busy_frac": float(st["busy_ms"] - base_busy) / 1e3 / wall,
+        "server_ms": {"admit": st["admit_ms"], "step": st["step_ms"], "ticks": st["ticks"]},
+        "queue_trace": {"fields": ["t_s", "active", "waiting", "ready", "completed"], "rows": trace[::5]},
         "e2e": {"value": value, "unit": UNIT,
                 "h2d_bytes_per_request": float(np.mean([48 * pool[p].num_verts + 28 * pool[p].num_tets
                                                         for _, p, _ in ids])) if ids else 0.0,

@@ -151,6 +151,11 @@ typedef struct pdgb_server_stats {
     size_t bytes_in_use;
     double tet_iterations;    /* sum over steps run of tets x iterations      */
     double busy_ms;           /* host time spent inside pdgb_server_tick      */
+    double admit_ms;          /* of which admission (allocation, uploads)     */
+    double step_ms;           /* of which stepping: launch to step complete   */
+    long long ticks;          /* ticks that ran a step                        */
+    int ready;                /* prepared, waiting for admission              */
+    int reserved;
 } pdgb_server_stats;
 
 typedef struct pdgb_server pdgb_server;

@@ -109,7 +109,8 @@ struct pdgb_server {
     long long completed = 0, failed = 0;
     double tet_iterations = 0.0;
     std::vector<double> latencies_ms;
-    double busy_ms = 0.0;
+    double busy_ms = 0.0, admit_ms = 0.0, step_ms = 0.0;
+    long long ticks = 0;
 
     ~pdgb_server() {
         {
@@ -463,8 +464,11 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
             S->active.push_back(r);
             S->lists_dirty = true;
         }
+        const auto t1 = Clock::now();
+        S->admit_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
         int done_now = 0;
         if (!S->active.empty()) {
+            S->ticks++;
             if (S->lists_dirty) rebuild_lists(S);
             // 2. one PD step for every active request
             PDGB_CUDA_TRY(cudaGraphLaunch(S->gexec, S->stream));
@@ -496,6 +500,7 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
             S->active.swap(keep);
             PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));
             const auto now = Clock::now();
+            S->step_ms += std::chrono::duration<double, std::milli>(now - t1).count();
             for (Request* r : retired) {  // results are on the host now
                 r->t_done = now;
                 S->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
@@ -558,6 +563,11 @@ int pdgb_server_get_stats(pdgb_server* S, pdgb_server_stats* out) {
     out->bytes_in_use = S->bytes_in_use;
     out->tet_iterations = S->tet_iterations;
     out->busy_ms = S->busy_ms;
+    out->admit_ms = S->admit_ms;
+    out->step_ms = S->step_ms;
+    out->ticks = S->ticks;
+    out->ready = (int)S->ready_queue.size();
+    out->reserved = 0;
     return PDGB_OK;
 }
 

@@ -123,6 +123,11 @@ class pdgb_server_stats(C.Structure):
         ("bytes_in_use", C.c_size_t),
         ("tet_iterations", C.c_double),
         ("busy_ms", C.c_double),
+        ("admit_ms", C.c_double),
+        ("step_ms", C.c_double),
+        ("ticks", C.c_longlong),
+        ("ready", C.c_int),
+        ("reserved", C.c_int),
     ]
 
 
