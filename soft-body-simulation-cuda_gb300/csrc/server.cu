@@ -438,8 +438,12 @@ int pdgb_server_submit(pdgb_server* S, const pdgb_mesh_desc* mesh, int nsteps, l
 int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
     if (!S) return PDGB_ERR_INVALID_ARGUMENT;
     return guarded_s([&] {
-        std::lock_guard<std::mutex> lk(S->mu);
+        // The server lock is held for admission and bookkeeping only, not
+        // while the step runs: the layout workers and the submitting threads
+        // need it to make progress.  Only pdgb_server_tick changes the active
+        // set and the step graph, so they need no lock of their own.
         const auto t0 = Clock::now();
+        std::unique_lock<std::mutex> lk(S->mu);
         // 1. admission in arrival order, by HBM budget and slot limit
         while (!S->ready_queue.empty()) {
             if (S->cfg.max_active > 0 && (int)S->active.size() >= S->cfg.max_active) break;
@@ -472,7 +476,7 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
             if (S->lists_dirty) rebuild_lists(S);
             // 2. one PD step for every active request
             PDGB_CUDA_TRY(cudaGraphLaunch(S->gexec, S->stream));
-            // 3. retire finished requests
+            // 3. retire finished requests (copies ordered after the step)
             std::vector<Request*> keep, retired;
             for (Request* r : S->active) {
                 r->steps_done++;
@@ -489,7 +493,6 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
                     PDGB_CUDA_TRY(cudaFreeAsync(r->block, S->stream));
                     r->block = nullptr;
                     S->bytes_in_use -= r->bytes;
-                    r->state = kDone;
                     S->lists_dirty = true;
                     retired.push_back(r);
                     done_now++;
@@ -498,10 +501,13 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
                 }
             }
             S->active.swap(keep);
+            lk.unlock();
             PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));
             const auto now = Clock::now();
+            lk.lock();
             S->step_ms += std::chrono::duration<double, std::milli>(now - t1).count();
             for (Request* r : retired) {  // results are on the host now
+                r->state = kDone;
                 r->t_done = now;
                 S->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
                 S->completed++;
