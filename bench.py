@@ -300,6 +300,7 @@ def run_serving(args):
     if args.rate > 0:
         wl["rate"] = args.rate
         wl["workload"] += f"_rate{args.rate:g}"
+        wl["desc"] = wl["desc"].replace("200 req/s", f"{args.rate:g} req/s", 1)
     rng = np.random.default_rng(5)
     pool = [mesh.request_body(math.exp(rng.uniform(math.log(1e3), math.log(3e5))), rng) for _ in range(48)]
     window = args.window
@@ -381,6 +382,7 @@ def run_serving(args):
         "accuracy": acc, "clocks": clocks.summary(),
         "busy_frac": float(st["busy_ms"] - base_busy) / 1e3 / wall,
         "server_ms": {"admit": st["admit_ms"], "step": st["step_ms"], "ticks": st["ticks"]},
+        "layout_cache_hits": st["layout_cache_hits"],
         "queue_trace": {"fields": ["t_s", "active", "waiting", "ready", "completed"], "rows": trace[::5]},
         "e2e": {"value": value, "unit": UNIT,
                 "h2d_bytes_per_request": float(np.mean([48 * pool[p].num_verts + 28 * pool[p].num_tets

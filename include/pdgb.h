@@ -155,13 +155,15 @@ typedef struct pdgb_server_stats {
     double step_ms;           /* of which stepping: launch to step complete   */
     long long ticks;          /* ticks that ran a step                        */
     int ready;                /* prepared, waiting for admission              */
-    int reserved;
+    int layout_cache_hits;    /* requests that reused a cached host layout    */
 } pdgb_server_stats;
 
 typedef struct pdgb_server pdgb_server;
 void pdgb_server_default_config(pdgb_server_config* cfg);
 int pdgb_server_create(const pdgb_server_config* cfg, void* stream, pdgb_server** out);
-/* Copies the host mesh; returns the request id. */
+/* Copies the host mesh; returns the request id.  Host layouts are cached
+ * by mesh content (the last 256 distinct meshes): a mesh submitted again
+ * skips the layout build. */
 int pdgb_server_submit(pdgb_server* s, const pdgb_mesh_desc* mesh, int nsteps, long long* request_id);
 /* Admission + one step of every active request + retirement (waits for the
  * step).  active / completed (nullable): requests resident after the tick,

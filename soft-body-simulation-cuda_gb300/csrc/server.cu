@@ -46,7 +46,7 @@ struct Request {
     int nv = 0, nt = 0;
     std::vector<float> X, V, mass, mu, dbc;
     std::vector<uint32_t> tets;
-    HostLayout L;
+    std::shared_ptr<const HostLayout> L;  // shared by requests with the same mesh (layout cache)
     std::string error;
     // device block and carved arrays
     unsigned char* block = nullptr;
@@ -65,7 +65,7 @@ template <class T> size_t bytes_of(const std::vector<T>& v) { return align256(v.
 // Device bytes of a prepared request (layout arrays + 8 float4 vectors +
 // staging for the state transfers).
 size_t request_bytes(const Request& r) {
-    const HostLayout& L = r.L;
+    const HostLayout& L = *r.L;
     size_t b = bytes_of(L.inc_ent) + bytes_of(L.inc_end) + bytes_of(L.geo) + bytes_of(L.tile_tet_ptr) +
                bytes_of(L.tile_vptr) + bytes_of(L.tile_verts) + bytes_of(L.vperm) + bytes_of(L.coef) +
                bytes_of(L.pin_rhs);
@@ -111,6 +111,11 @@ struct pdgb_server {
     std::vector<double> latencies_ms;
     double busy_ms = 0.0, admit_ms = 0.0, step_ms = 0.0;
     long long ticks = 0;
+    // layout cache: requests for a mesh seen before reuse its host layout
+    std::mutex cache_mu;
+    std::unordered_map<uint64_t, std::pair<uint64_t, std::shared_ptr<const HostLayout>>> cache;
+    std::deque<uint64_t> cache_order;  // insertion order, for eviction
+    long long cache_hits = 0;
 
     ~pdgb_server() {
         {
@@ -160,6 +165,43 @@ template <class F> int guarded_s(F&& f) {
     }
 }
 
+// Two independent 64-bit hashes of a request's mesh (the layout depends on
+// nothing else for a given server).
+struct MeshKey {
+    uint64_t a, b;
+};
+
+MeshKey mesh_key(const Request& r) {
+    uint64_t a = 0x9e3779b97f4a7c15ull ^ ((uint64_t)r.nv << 32 | (uint32_t)r.nt);
+    uint64_t b = 0xc2b2ae3d27d4eb4full + (uint64_t)r.nv * 31 + (uint64_t)r.nt;
+    auto mix = [&](const void* p, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        size_t i = 0;
+        for (; i + 8 <= n; i += 8) {
+            uint64_t w;
+            std::memcpy(&w, c + i, 8);
+            a = (a ^ w) * 0x100000001b3ull;
+            a ^= a >> 29;
+            b = (b + w) * 0x9fb21c651e98df25ull;
+            b ^= b >> 31;
+        }
+        for (; i < n; ++i) {
+            a = (a ^ c[i]) * 0x100000001b3ull;
+            b = (b + c[i]) * 0x9fb21c651e98df25ull;
+        }
+        a ^= n;
+        b += n;
+    };
+    mix(r.X.data(), r.X.size() * sizeof(float));
+    mix(r.tets.data(), r.tets.size() * sizeof(uint32_t));
+    mix(r.mass.data(), r.mass.size() * sizeof(float));
+    mix(r.mu.data(), r.mu.size() * sizeof(float));
+    mix(r.dbc.data(), r.dbc.size() * sizeof(float));
+    return {a, b};
+}
+
+constexpr size_t kLayoutCacheEntries = 256;
+
 void worker_loop(pdgb_server* S) {
     for (;;) {
         Request* r = nullptr;
@@ -176,8 +218,29 @@ void worker_loop(pdgb_server* S) {
         }
         bool ok = true;
         try {
-            build_layout(r->nv, r->nt, r->X.data(), r->tets.data(), r->mass.data(), r->mu.data(),
-                         r->dbc.empty() ? nullptr : r->dbc.data(), S->cfg.params, r->L);
+            const MeshKey key = mesh_key(*r);
+            {
+                std::lock_guard<std::mutex> ck(S->cache_mu);
+                auto it = S->cache.find(key.a);
+                if (it != S->cache.end() && it->second.first == key.b) {
+                    r->L = it->second.second;
+                    S->cache_hits++;
+                }
+            }
+            if (!r->L) {
+                auto L = std::make_shared<HostLayout>();
+                build_layout(r->nv, r->nt, r->X.data(), r->tets.data(), r->mass.data(), r->mu.data(),
+                             r->dbc.empty() ? nullptr : r->dbc.data(), S->cfg.params, *L);
+                r->L = L;
+                std::lock_guard<std::mutex> ck(S->cache_mu);
+                if (S->cache.emplace(key.a, std::make_pair(key.b, r->L)).second) {
+                    S->cache_order.push_back(key.a);
+                    if (S->cache_order.size() > kLayoutCacheEntries) {
+                        S->cache.erase(S->cache_order.front());
+                        S->cache_order.pop_front();
+                    }
+                }
+            }
             r->bytes = request_bytes(*r);
         } catch (const Error& e) {
             ok = false;
@@ -212,7 +275,7 @@ void admit(pdgb_server* S, Request* r) {
     cudaStream_t s = S->stream;
     PDGB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r->block), r->bytes, S->pool, s));
     unsigned char* p = r->block;
-    const HostLayout& L = r->L;
+    const HostLayout& L = *r->L;
     const int nv = r->nv;
     uint16_t* inc_ent = carve<uint16_t>(p, L.inc_ent.size());
     uint16_t* inc_end = carve<uint16_t>(p, L.inc_end.size());
@@ -325,7 +388,7 @@ void ensure_capacity(pdgb_server* S, int nreq, int ntiles, int nchunks) {
 void rebuild_lists(pdgb_server* S) {
     int ntiles = 0, nchunks = 0;
     for (Request* r : S->active) {
-        ntiles += r->L.ntiles;
+        ntiles += r->L->ntiles;
         nchunks += (r->nv + 255) / 256;
     }
     ensure_capacity(S, (int)S->active.size(), ntiles, nchunks);
@@ -336,7 +399,7 @@ void rebuild_lists(pdgb_server* S) {
         S->h_la[q] = r->la;
         S->h_va[q] = r->va;
         S->h_ba[q] = r->ba;
-        for (int k = 0; k < r->L.ntiles; ++k) S->h_tiles[t++] = make_int2(q, k);
+        for (int k = 0; k < r->L->ntiles; ++k) S->h_tiles[t++] = make_int2(q, k);
         for (int v0 = 0; v0 < r->nv; v0 += 256) S->h_chunks[c++] = make_int2(q, v0);
     }
     S->h_counts[0] = t;
@@ -573,7 +636,10 @@ int pdgb_server_get_stats(pdgb_server* S, pdgb_server_stats* out) {
     out->step_ms = S->step_ms;
     out->ticks = S->ticks;
     out->ready = (int)S->ready_queue.size();
-    out->reserved = 0;
+    {
+        std::lock_guard<std::mutex> ck(S->cache_mu);
+        out->layout_cache_hits = (int)std::min<long long>(S->cache_hits, INT32_MAX);
+    }
     return PDGB_OK;
 }
 

@@ -127,7 +127,7 @@ class pdgb_server_stats(C.Structure):
         ("step_ms", C.c_double),
         ("ticks", C.c_longlong),
         ("ready", C.c_int),
-        ("reserved", C.c_int),
+        ("layout_cache_hits", C.c_int),
     ]
 
 

@@ -116,3 +116,20 @@ def test_slot_limit_and_bad_request():
             X, _ = srv.result(rid)
             Xa, _ = _alone(body, steps)
             assert rel_l2(X, Xa) < 1e-5
+
+
+def test_layout_cache_reuse():
+    """The same mesh submitted again reuses the cached host layout; each
+    request still gets its own device state and result."""
+    body, _ = _bodies()[1]
+    other, _ = _bodies()[2]
+    with PdServer(PARAMS) as srv:
+        first = srv.submit(body, 3)
+        _drain(srv, [first])
+        ids = [srv.submit(body, s) for s in (2, 5)] + [srv.submit(other, 4)]
+        _drain(srv, ids)
+        assert srv.stats()["layout_cache_hits"] >= 2
+        for rid, b, s in zip([first] + ids, [body, body, body, other], [3, 2, 5, 4]):
+            X, _ = srv.result(rid)
+            Xa, _ = _alone(b, s)
+            assert rel_l2(X, Xa) < 1e-5
