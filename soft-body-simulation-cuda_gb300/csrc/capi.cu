@@ -208,7 +208,7 @@ BeginArgs begin_args(pdgb_engine* e) {
 void record_local(pdgb_engine* e, const LocalArgs& la, bool jacobi_form, int i) {
     cudaStream_t s = e->stream;
     if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i], s, cudaEventRecordExternal));
-    launch_local(la, e->L.ntiles, jacobi_form, e->rotation, s);
+    launch_local(la, e->L.ntiles, e->L.max_patch, jacobi_form, e->rotation, s);
     if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i + 1], s, cudaEventRecordExternal));
 }
 
@@ -771,14 +771,14 @@ int pdgb_time_local(pdgb_engine* e, int launches, double* ms_per_launch) {
         launch_begin(ba, e->stream);
         const LocalArgs la = local_args(e, nullptr);
         const bool jf = e->prm.solver == PDGB_SOLVER_JACOBI;
-        launch_local(la, e->L.ntiles, jf, e->rotation, e->stream);  // warm-up
+        launch_local(la, e->L.ntiles, e->L.max_patch, jf, e->rotation, e->stream);  // warm-up
         cudaEvent_t ev[2];
         PDGB_CUDA_TRY(cudaEventCreate(&ev[0]));
         PDGB_CUDA_TRY(cudaEventCreate(&ev[1]));
         float ms = 0.f;
         cudaError_t err = cudaEventRecord(ev[0], e->stream);
         for (int k = 0; k < launches && err == cudaSuccess; ++k) {
-            launch_local(la, e->L.ntiles, jf, e->rotation, e->stream);
+            launch_local(la, e->L.ntiles, e->L.max_patch, jf, e->rotation, e->stream);
             err = cudaGetLastError();
         }
         if (err == cudaSuccess) err = cudaEventRecord(ev[1], e->stream);

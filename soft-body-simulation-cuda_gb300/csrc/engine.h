@@ -32,6 +32,12 @@ void set_last_error(int status, const std::string& msg);
 // vertices they touch.  kMaxPatch bounds the patch so that its positions and
 // accumulators fit in shared memory (16 + 12 bytes per vertex).
 constexpr int kMaxPatch = 1024;
+// A tet corner is recorded as patch index k (kPatchBits) | rank r of the
+// corner within k's run of slots (the remaining bits of a uint16), so a
+// vertex has at most kMaxRun corners in one tile.
+constexpr int kPatchBits = 10;
+constexpr int kMaxRun = 1 << (16 - kPatchBits);
+static_assert(kMaxPatch <= (1 << kPatchBits), "patch index field");
 constexpr int kLocalThreads = 256;
 constexpr int kTileTets = 2 * kLocalThreads;
 
@@ -69,6 +75,7 @@ template <class T> struct DBuf {
 struct HostLayout {
     int nv = 0, nt = 0, nt_pad = 0, ntiles = 0;
     int tile_cap = 0;         // most tets per tile of the current cut
+    int max_patch = 0;        // largest tile patch of the current cut
     std::vector<int> vperm;   // internal vertex -> caller vertex
     std::vector<int> viperm;  // caller vertex -> internal vertex
     std::vector<int> tperm;   // internal tet -> caller tet
@@ -81,8 +88,9 @@ struct HostLayout {
     std::vector<uint32_t> tile_verts;  // internal vertex ids of each patch (sorted) | kPinnedBit
     // Slots of a tile: one per tet corner, ordered by patch vertex (then tet,
     // then corner), so patch vertex k owns the slots inc_end[k-1] ..
-    // inc_end[k] (inc_end[-1] = 0); inc_ent[4 t + c] is the slot of corner c
-    // of tet t.
+    // inc_end[k] (inc_end[-1] = 0).  inc_ent[4 t + c] = k | r << kPatchBits
+    // for corner c of tet t: its patch vertex k and its rank r in k's run
+    // (slot inc_end[k-1] + r).
     std::vector<uint16_t> inc_ent;   // [4 nt]
     std::vector<uint16_t> inc_end;   // [sum of patch sizes]
     std::vector<float> geo;          // SoA [10][nt_pad]: DmInv row-major (9), V0*w
@@ -208,7 +216,7 @@ void launch_begin_multi(const BeginArgs* req, const int2* list, const int* count
 void launch_local_multi(const LocalArgs* req, const int2* list, const int* count, int grid, cudaStream_t s);
 void launch_jacobi_vertex_multi(const VertexArgs* req, const int2* list, const int* count, int grid, int mode,
                                 float omega, cudaStream_t s);
-void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, int rotation, cudaStream_t s);
+void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_form, int rotation, cudaStream_t s);
 void launch_jacobi_vertex(const VertexArgs& a, int mode, cudaStream_t s);
 void launch_gather_state(int nv, const int* vperm, const float* X, const float* V, float4* x, float4* v,
                          cudaStream_t s);

@@ -15,28 +15,29 @@
 namespace pdgb {
 
 // ------------------------------------------------------------ local step
-// One CTA per tile of Morton-ordered tets.  Shared memory holds one float4
-// slot per tet corner, ordered by patch vertex: patch vertex k owns the
-// contiguous slots inc_end[k-1] .. inc_end[k].  (1) Every patch vertex is
-// loaded once (coalesced over the sorted patch list) and written into its
-// run of slots.  (2) Every tet reads its 4 corner slots (slot numbers
-// inc_ent[4 t + c], loaded with its geometry), computes F = Ds DmInv, the
-// closest rotation R (minus F in the Jacobi residual form) and the corner
-// contributions c R DmInv^T G, and overwrites its slots with them.  (3)
-// Every patch vertex sums its run of slots in order and adds the sum to b
-// with one float4 atomic (pinned vertices are skipped: their RHS is the pin
-// term).  No shared-memory atomics; within a tile the sums are
+// One CTA per tile of Morton-ordered tets.  (1) Every patch vertex k is
+// loaded once (coalesced over the sorted patch list) into pos[k], with the
+// start of its run of slots in the w lane.  (2) Every tet reads its 4 corner
+// positions (corner records k | r << kPatchBits, loaded with its geometry),
+// computes F = Ds DmInv, the closest rotation R (minus F in the Jacobi
+// residual form) and the corner contributions c R DmInv^T G, and writes each
+// to its slot: run start of k + rank r.  The slots of a tile are ordered by
+// patch vertex, so patch vertex k owns the contiguous slots inc_end[k-1] ..
+// inc_end[k].  (3) Every patch vertex sums its run of slots in order and adds
+// the sum to b with one float4 atomic (pinned vertices are skipped: their RHS
+// is the pin term).  No shared-memory atomics; within a tile the sums are
 // deterministic.
 template <bool kJacobiForm, int kRotation>
-__device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4* slot) {
+__device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4* slot, float4* pos) {
     const int vb = a.tile_vptr[tile];
     const int np = a.tile_vptr[tile + 1] - vb;
     const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
     const int ntile = t1 - t0;
     const uint16_t* iend = a.inc_end + vb;
-    // Issue the per-tet geometry and slot-number loads of this thread's tets
-    // first: they are in flight while the patch positions are gathered.
+    // Issue the per-tet geometry and corner-record loads of this thread's
+    // tets first: they are in flight while the patch positions are gathered.
     constexpr int kPer = kTileTets / kLocalThreads;
+    constexpr uint32_t kPatchMask = (1u << kPatchBits) - 1u;
     const int ntp = a.nt_pad;
     float G[kPer][10];
     uint2 S[kPer];
@@ -49,18 +50,18 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         S[j] = __ldg(reinterpret_cast<const uint2*>(a.inc_ent) + t);
     }
     // the first patch vertex of each thread keeps its id and slot run in
-    // registers for the gather phase
+    // registers for the reduction phase
     uint32_t v_first = kPinnedBit;
     int e0_first = 0, e1_first = 0;
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
         const uint32_t v = __ldg(&a.tile_verts[vb + k]);
         const float4 p = __ldg(&a.sn[v & ~kPinnedBit]);
-        const int e0 = k ? __ldg(&iend[k - 1]) : 0, e1 = __ldg(&iend[k]);
-        for (int e = e0; e < e1; ++e) slot[e] = p;
+        const int e0 = k ? __ldg(&iend[k - 1]) : 0;
+        pos[k] = make_float4(p.x, p.y, p.z, __int_as_float(e0));
         if (k == (int)threadIdx.x) {
             v_first = v;
             e0_first = e0;
-            e1_first = e1;
+            e1_first = __ldg(&iend[k]);
         }
     }
     __syncthreads();
@@ -70,8 +71,14 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         if (lt >= ntile) break;
         const float* D = G[j];
         const float c = G[j][9];
-        const int s0 = S[j].x & 0xffff, s1 = S[j].x >> 16, s2 = S[j].y & 0xffff, s3 = S[j].y >> 16;
-        const float4 p0 = slot[s0], p1 = slot[s1], p2 = slot[s2], p3 = slot[s3];
+        const uint32_t w0 = S[j].x & 0xffffu, w1 = S[j].x >> 16, w2 = S[j].y & 0xffffu, w3 = S[j].y >> 16;
+        const float4 p0 = pos[w0 & kPatchMask], p1 = pos[w1 & kPatchMask], p2 = pos[w2 & kPatchMask],
+                     p3 = pos[w3 & kPatchMask];
+        // slots of the 4 corners, two 16-bit slot numbers per register
+        const uint32_t s01 = (uint32_t)(__float_as_int(p0.w) + (int)(w0 >> kPatchBits)) |
+                             ((uint32_t)(__float_as_int(p1.w) + (int)(w1 >> kPatchBits)) << 16);
+        const uint32_t s23 = (uint32_t)(__float_as_int(p2.w) + (int)(w2 >> kPatchBits)) |
+                             ((uint32_t)(__float_as_int(p3.w) + (int)(w3 >> kPatchBits)) << 16);
         // Ds columns = edges; F = Ds * DmInv (row-major F[r][c])
         const float e[3][3] = {{p1.x - p0.x, p2.x - p0.x, p3.x - p0.x},
                                {p1.y - p0.y, p2.y - p0.y, p3.y - p0.y},
@@ -97,6 +104,7 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) M[3 * r + cc] = fmaf(r0, D[3 * cc], fmaf(r1, D[3 * cc + 1], r2 * D[3 * cc + 2]));
         }
+        const int s0 = s01 & 0xffff, s1 = s01 >> 16, s2 = s23 & 0xffff, s3 = s23 >> 16;
         slot[s0] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
         slot[s1] = make_float4(M[0], M[3], M[6], 0.f);
         slot[s2] = make_float4(M[1], M[4], M[7], 0.f);
@@ -107,7 +115,7 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         const bool first = k == (int)threadIdx.x;
         const uint32_t v = first ? v_first : __ldg(&a.tile_verts[vb + k]);
         if (v & kPinnedBit) continue;
-        const int e0 = first ? e0_first : (k ? __ldg(&iend[k - 1]) : 0);
+        const int e0 = first ? e0_first : __ldg(&iend[k - 1]);
         const int e1 = first ? e1_first : __ldg(&iend[k]);
         float sx = 0.f, sy = 0.f, sz = 0.f;
         for (int e = e0; e < e1; ++e) {
@@ -125,12 +133,14 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
 #define PDGB_LOCAL_MIN_BLOCKS 4
 #endif
 
+// Shared memory: the tile's slots (static) and its patch positions
+// (dynamic, 16 bytes per patch vertex of the largest tile).
 template <bool kJacobiForm, int kRotation>
 __global__ void __launch_bounds__(kLocalThreads, PDGB_LOCAL_MIN_BLOCKS) k_local(LocalArgs a) {
-    // corner-major slots: corner c of local tet lt lives at c * kTileTets + lt
     __shared__ float4 slot[4 * kTileTets];
+    extern __shared__ float4 pos[];
     if (a.done && *a.done) return;
-    local_tile<kJacobiForm, kRotation>(a, blockIdx.x, slot);
+    local_tile<kJacobiForm, kRotation>(a, blockIdx.x, slot, pos);
 }
 
 // Multi-request form (serving): CTA i runs tile list[i] of request
@@ -140,23 +150,27 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_multi(const LocalArgs* 
                                                                const int2* __restrict__ list,
                                                                const int* __restrict__ count) {
     __shared__ float4 slot[4 * kTileTets];
+    extern __shared__ float4 pos[];
     if ((int)blockIdx.x >= *count) return;
     const int2 w = list[blockIdx.x];
-    local_tile<kJacobiForm, PDGB_ROTATION_QUAT>(req[w.x], w.y, slot);
+    local_tile<kJacobiForm, PDGB_ROTATION_QUAT>(req[w.x], w.y, slot, pos);
 }
 
 void launch_local_multi(const LocalArgs* req, const int2* list, const int* count, int grid, cudaStream_t s) {
-    if (grid > 0) k_local_multi<true><<<grid, kLocalThreads, 0, s>>>(req, list, count);
+    if (grid > 0) k_local_multi<true><<<grid, kLocalThreads, kMaxPatch * sizeof(float4), s>>>(req, list, count);
 }
 
-void launch_local(const LocalArgs& a, int ntiles, bool jacobi_form, int rotation, cudaStream_t s) {
+void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_form, int rotation, cudaStream_t s) {
     if (ntiles <= 0) return;
+    if (max_patch < 1 || max_patch > kMaxPatch)
+        throw Error{PDGB_ERR_INVALID_ARGUMENT, "local step: tile patch size out of range"};
+    const size_t sm = (size_t)max_patch * sizeof(float4);
     if (rotation == PDGB_ROTATION_SVD) {
-        if (jacobi_form) k_local<true, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, 0, s>>>(a);
-        else k_local<false, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, 0, s>>>(a);
+        if (jacobi_form) k_local<true, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, sm, s>>>(a);
+        else k_local<false, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, sm, s>>>(a);
     } else {
-        if (jacobi_form) k_local<true, PDGB_ROTATION_QUAT><<<ntiles, kLocalThreads, 0, s>>>(a);
-        else k_local<false, PDGB_ROTATION_QUAT><<<ntiles, kLocalThreads, 0, s>>>(a);
+        if (jacobi_form) k_local<true, PDGB_ROTATION_QUAT><<<ntiles, kLocalThreads, sm, s>>>(a);
+        else k_local<false, PDGB_ROTATION_QUAT><<<ntiles, kLocalThreads, sm, s>>>(a);
     }
 }
 

@@ -81,9 +81,11 @@ void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
     L.tile_verts.clear();
     L.inc_end.clear();
     L.inc_ent.assign((size_t)4 * nt, 0);
-    std::vector<int> mark(nv, -1), loc(nv, 0), cnt;
+    std::vector<int> mark(nv, -1), loc(nv, 0), cnt, run(nv, 0);
     std::vector<int> patch;
     patch.reserve(kMaxPatch);
+    std::vector<int> vcount(nv, 0);  // corners of each patch vertex in the open tile
+    L.max_patch = 0;
     int tile = 0, start = 0;
     int body_cursor = 0, next_body_start = nbodies > 1 ? L.body_itstart[1] : nt;
     auto close_tile = [&](int end) {
@@ -96,14 +98,17 @@ void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
             for (int c = 0; c < 4; ++c) cnt[loc[L.tets_int[4 * (size_t)i + c]] + 1]++;
         for (int k = 0; k < np; ++k) cnt[k + 1] += cnt[k];
         for (int k = 0; k < np; ++k) L.inc_end.push_back((uint16_t)cnt[k + 1]);
-        // slot of each tet corner: its position in the tile's vertex-sorted
-        // incidence order, so that a patch vertex's corners are one
-        // contiguous run of slots
+        // corner record: patch index k and the corner's rank r within k's
+        // run of slots (tile order), so that a patch vertex's corners are one
+        // contiguous run of slots and the slot is inc_end[k-1] + r
         for (int i = start; i < end; ++i)
             for (int c = 0; c < 4; ++c) {
                 const int k = loc[L.tets_int[4 * (size_t)i + c]];
-                L.inc_ent[4 * (size_t)i + c] = (uint16_t)(cnt[k]++);
+                const int r = run[k]++;
+                L.inc_ent[4 * (size_t)i + c] = (uint16_t)(k | (r << kPatchBits));
             }
+        for (int k = 0; k < np; ++k) run[k] = 0;
+        L.max_patch = std::max(L.max_patch, np);
         for (int v : patch) {
             const int o = L.vperm[v];
             const bool pinned = dbc && dbc[o] > 0.f;
@@ -124,13 +129,21 @@ void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
             fresh += !dup;
         }
         const bool new_body = i > start && i == next_body_start;
-        if (i - start == cap || (int)patch.size() + fresh > kMaxPatch || new_body) close_tile(i);
+        bool run_full = false;  // a corner run would outgrow the rank field
+        for (int k = 0; k < 4; ++k) {
+            int extra = 0;
+            for (int j = 0; j < 4; ++j) extra += id[j] == id[k];
+            run_full = run_full || (mark[id[k]] == tile && vcount[id[k]] + extra > kMaxRun);
+        }
+        if (i - start == cap || (int)patch.size() + fresh > kMaxPatch || new_body || run_full) close_tile(i);
         while (i >= next_body_start && body_cursor < nbodies) next_body_start = L.body_itstart[++body_cursor];
         for (int k = 0; k < 4; ++k)
             if (mark[id[k]] != tile) {
                 mark[id[k]] = tile;
+                vcount[id[k]] = 0;
                 patch.push_back((int)id[k]);
             }
+        for (int k = 0; k < 4; ++k) vcount[id[k]]++;
     }
     close_tile(nt);
     L.ntiles = tile;

@@ -75,3 +75,29 @@ def scene_fixed_bodies(rows):
         else:
             out.append(scene.cylinder(pos, rot, sc))
     return out
+
+
+def fan_body(n: int = 100, seed: int = 0):
+    """Bicone of 2n tets around one centre vertex (valence 2n): a ring of n
+    vertices, an apex above and below; the upper apex is pinned.  Used to
+    exercise a vertex with more corners than one tile run holds."""
+    from pdgb import mesh
+
+    rng = np.random.default_rng(seed)
+    ang = np.sort(rng.uniform(0.0, 2.0 * np.pi, n))
+    rad = rng.uniform(0.8, 1.2, n)
+    ring = np.stack([rad * np.cos(ang), rng.uniform(-0.05, 0.05, n), rad * np.sin(ang)], axis=1)
+    X = np.concatenate([[[0.0, 0.0, 0.0]], ring, [[0.0, 1.0, 0.0], [0.0, -1.0, 0.0]]]).astype(np.float64)
+    c, top, bot = 0, n + 1, n + 2
+    tets = []
+    for i in range(n):
+        a, b = 1 + i, 1 + (i + 1) % n
+        tets.append([c, a, b, top])
+        tets.append([c, b, a, bot])
+    tets = mesh.orient_positive(X, np.array(tets, np.uint32))
+    mass = mesh.lumped_mass(X, tets, 1000.0)
+    mu = np.full(tets.shape[0], mesh.lame_mu(1e5, 0.4), np.float32)
+    dbc = np.zeros(X.shape[0], np.float32)
+    dbc[top] = 1.0
+    return mesh.SoftBody(X=X.astype(np.float32), tets=tets.astype(np.uint32), mass=mass.astype(np.float32), mu=mu,
+                         dbc=dbc)

@@ -114,3 +114,18 @@ def test_chebyshev_schedule_matches_reference_host_loop():
             om = np.float32(4) / (np.float32(4) - rho * rho * om)
         seq.append(om)
     assert seq[11] > 1.9 and all(1.0 <= w < 2.0 for w in seq)
+
+
+def test_layout_splits_tiles_at_long_vertex_runs():
+    """A vertex with 200 corners: a tile holds at most 64 corners of one
+    vertex (the rank field of a corner record), so the 200 tets span at
+    least 4 tiles; orders stay permutations."""
+    from conftest import fan_body
+
+    body = fan_body(100)
+    st, info, vperm, tperm = inspect(body)
+    assert st == N.PDGB_OK
+    assert info.num_tiles >= 4
+    assert info.max_tile_tets <= 64
+    assert np.array_equal(np.sort(vperm), np.arange(body.num_verts))
+    assert np.array_equal(np.sort(tperm), np.arange(body.num_tets))

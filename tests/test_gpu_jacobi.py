@@ -45,6 +45,22 @@ def test_engine_vs_fp64_oracle_jittered_grid():
     assert rel_l2(V, Vo) < 1e-2
 
 
+@pytest.mark.parametrize("solver", [0, 1])
+def test_high_valence_vertex_vs_oracle(solver):
+    """A centre vertex shared by 200 tets spans several tiles (at most 64
+    of its corners per tile); the step still matches the FP64 oracle."""
+    from conftest import fan_body
+
+    body = fan_body(100, seed=5)
+    params = SolverParams(num_iterations=20, rho=0.999, solver=solver)
+    with PdSolver(body, params) as e:
+        e.update(10)
+        X, _ = e.download_state()
+    Xo, _, _ = O.simulate(body, params, 10, precision=64)
+    assert np.isfinite(X).all()
+    assert rel_l2(X, Xo) < TOL
+
+
 def test_large_grid_first_steps_vs_oracle():
     """64^3 cells (274,625 verts / 1,310,720 tets): 2 steps vs the FP64 oracle."""
     body = mesh.cube_c2()
