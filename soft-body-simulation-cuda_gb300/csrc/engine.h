@@ -93,7 +93,7 @@ struct HostLayout {
     // (slot inc_end[k-1] + r).
     std::vector<uint16_t> inc_ent;   // [4 nt]
     std::vector<uint16_t> inc_end;   // [sum of patch sizes]
-    std::vector<float> geo;          // SoA [10][nt_pad]: DmInv row-major (9), V0*w
+    std::vector<float> geo;          // planes float4 [nt_pad] x2 + float2 [nt_pad]: g DmInv (row major), g = sqrt(V0 w)
     std::vector<uint32_t> tets_int;  // [4*nt] internal vertex ids (Cholesky assembly, checks)
     std::vector<double> dminv_d;     // [9*nt] double DmInv (system assembly)
     std::vector<double> coef_d;      // [nt]   double V0*w

@@ -14,6 +14,7 @@
 
 namespace pdgb {
 
+
 // ------------------------------------------------------------ local step
 // One CTA per tile of Morton-ordered tets.  (1) Every patch vertex k is
 // loaded once (coalesced over the sorted patch list) into pos[k], with the
@@ -39,16 +40,21 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
     constexpr int kPer = kTileTets / kLocalThreads;
     constexpr uint32_t kPatchMask = (1u << kPatchBits) - 1u;
     const int ntp = a.nt_pad;
-    float G[kPer][10];
+    const float4* geo0 = reinterpret_cast<const float4*>(a.geo);
+    const float2* geo2 = reinterpret_cast<const float2*>(a.geo + 8 * (size_t)ntp);
+    float4 GA[kPer], GB[kPer];
+    float2 GC[kPer];
     uint2 S[kPer];
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
         const int lt = threadIdx.x + j * kLocalThreads;
         const int t = t0 + (lt < ntile ? lt : 0);
-#pragma unroll
-        for (int k = 0; k < 10; ++k) G[j][k] = __ldg(&a.geo[k * ntp + t]);
+        GA[j] = __ldg(geo0 + t);
+        GB[j] = __ldg(geo0 + ntp + t);
+        GC[j] = __ldg(geo2 + t);
         S[j] = __ldg(reinterpret_cast<const uint2*>(a.inc_ent) + t);
     }
+    if (a.done && *a.done) return;
     // the first patch vertex of each thread keeps its id and slot run in
     // registers for the reduction phase
     uint32_t v_first = kPinnedBit;
@@ -69,8 +75,9 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
     for (int j = 0; j < kPer; ++j) {
         const int lt = threadIdx.x + j * kLocalThreads;
         if (lt >= ntile) break;
-        const float* D = G[j];
-        const float c = G[j][9];
+        // D' = g DmInv (row major) and g = sqrt(V0 w)
+        const float D[9] = {GA[j].x, GA[j].y, GA[j].z, GA[j].w, GB[j].x, GB[j].y, GB[j].z, GB[j].w, GC[j].x};
+        const float g = GC[j].y;
         const uint32_t w0 = S[j].x & 0xffffu, w1 = S[j].x >> 16, w2 = S[j].y & 0xffffu, w3 = S[j].y >> 16;
         const float4 p0 = pos[w0 & kPatchMask], p1 = pos[w1 & kPatchMask], p2 = pos[w2 & kPatchMask],
                      p3 = pos[w3 & kPatchMask];
@@ -79,7 +86,7 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
                              ((uint32_t)(__float_as_int(p1.w) + (int)(w1 >> kPatchBits)) << 16);
         const uint32_t s23 = (uint32_t)(__float_as_int(p2.w) + (int)(w2 >> kPatchBits)) |
                              ((uint32_t)(__float_as_int(p3.w) + (int)(w3 >> kPatchBits)) << 16);
-        // Ds columns = edges; F = Ds * DmInv (row-major F[r][c])
+        // Ds columns = edges; F' = Ds * D' = g F (row-major F[r][c])
         const float e[3][3] = {{p1.x - p0.x, p2.x - p0.x, p3.x - p0.x},
                                {p1.y - p0.y, p2.y - p0.y, p3.y - p0.y},
                                {p1.z - p0.z, p2.z - p0.z, p3.z - p0.z}};
@@ -89,20 +96,20 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc)
                 F[3 * r + cc] = fmaf(e[r][0], D[cc], fmaf(e[r][1], D[3 + cc], e[r][2] * D[6 + cc]));
+        // closest rotation of F' (that of F: g > 0 scales the singular values)
         float R[9];
         if (kRotation == PDGB_ROTATION_SVD) closest_rotation(F, R);
         else closest_rotation_horn(F, R);
-        if (kJacobiForm) {
+        // c (R - F) DmInv^T = (g R - F') D'^T ; c R DmInv^T = (g R) D'^T
 #pragma unroll
-            for (int k = 0; k < 9; ++k) R[k] -= F[k];
-        }
-        // M = (c R) DmInv^T ; contributions: corner 0 = -(M0+M1+M2), corner j = M_{j-1}
+        for (int k = 0; k < 9; ++k) R[k] = kJacobiForm ? fmaf(g, R[k], -F[k]) : g * R[k];
+        // M = R D'^T ; contributions: corner 0 = -(M0+M1+M2), corner j = M_{j-1}
         float M[9];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-            const float r0 = c * R[3 * r], r1 = c * R[3 * r + 1], r2 = c * R[3 * r + 2];
 #pragma unroll
-            for (int cc = 0; cc < 3; ++cc) M[3 * r + cc] = fmaf(r0, D[3 * cc], fmaf(r1, D[3 * cc + 1], r2 * D[3 * cc + 2]));
+            for (int cc = 0; cc < 3; ++cc)
+                M[3 * r + cc] = fmaf(R[3 * r], D[3 * cc], fmaf(R[3 * r + 1], D[3 * cc + 1], R[3 * r + 2] * D[3 * cc + 2]));
         }
         const int s0 = s01 & 0xffff, s1 = s01 >> 16, s2 = s23 & 0xffff, s3 = s23 >> 16;
         slot[s0] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
@@ -139,7 +146,6 @@ template <bool kJacobiForm, int kRotation>
 __global__ void __launch_bounds__(kLocalThreads, PDGB_LOCAL_MIN_BLOCKS) k_local(LocalArgs a) {
     __shared__ float4 slot[4 * kTileTets];
     extern __shared__ float4 pos[];
-    if (a.done && *a.done) return;
     local_tile<kJacobiForm, kRotation>(a, blockIdx.x, slot, pos);
 }
 

@@ -214,7 +214,11 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
     L.tets_int.resize((size_t)4 * nt);
     for (int i = 0; i < nt; ++i)
         for (int k = 0; k < 4; ++k) L.tets_int[4 * (size_t)i + k] = (uint32_t)L.viperm[tets[4 * (size_t)L.tperm[i] + k]];
-    // ---- geometry: DmInv and V0 * w (solverUtil.cuh:98-138, pdUtil.cu:19)
+    // ---- geometry: DmInv and V0 * w (solverUtil.cuh:98-138, pdUtil.cu:19).
+    // The local step reads g = sqrt(V0 w) and D' = g DmInv: F' = Ds D' = g F
+    // has the same closest rotation R as F, and c (R - F) DmInv^T =
+    // (g R - F') D'^T, c R DmInv^T = g R D'^T.  Planes: D'[0..3] (float4),
+    // D'[4..7] (float4), {D'[8], g} (float2).
     L.nt_pad = (nt + 31) & ~31;
     L.geo.assign((size_t)10 * L.nt_pad, 0.f);
     L.dminv_d.resize((size_t)9 * nt);
@@ -240,13 +244,20 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
         inv[6] = (D[1][0] * D[2][1] - D[1][1] * D[2][0]) / det;
         inv[7] = (D[0][1] * D[2][0] - D[0][0] * D[2][1]) / det;
         inv[8] = (D[0][0] * D[1][1] - D[0][1] * D[1][0]) / det;
+        if (!(mu[t] >= 0.f) || !std::isfinite(mu[t]))
+            throw Error{PDGB_ERR_BAD_MESH, "tet " + std::to_string(t) + " has a negative or non-finite weight"};
         const double coef = std::fabs(det) / 6.0 * (double)mu[t];
+        const double g = std::sqrt(coef);
+        const size_t np4 = (size_t)4 * L.nt_pad;
         for (int k = 0; k < 9; ++k) {
             L.dminv_d[9 * (size_t)i + k] = inv[k];
-            L.geo[(size_t)k * L.nt_pad + i] = (float)inv[k];
+            const float v = (float)(g * inv[k]);
+            if (k < 4) L.geo[4 * (size_t)i + k] = v;
+            else if (k < 8) L.geo[np4 + 4 * (size_t)i + (k - 4)] = v;
+            else L.geo[2 * np4 + 2 * (size_t)i] = v;
         }
         L.coef_d[i] = coef;
-        L.geo[(size_t)9 * L.nt_pad + i] = (float)coef;
+        L.geo[2 * np4 + 2 * (size_t)i + 1] = (float)g;
     }
     build_tiles(L, dbc, max_tile_tets);
     // ---- rest positions (internal order)

@@ -129,3 +129,12 @@ def test_layout_splits_tiles_at_long_vertex_runs():
     assert info.max_tile_tets <= 64
     assert np.array_equal(np.sort(vperm), np.arange(body.num_verts))
     assert np.array_equal(np.sort(tperm), np.arange(body.num_tets))
+
+
+def test_negative_weight_is_rejected():
+    body = mesh.make_grid_body(2, 2, 2)
+    body.mu = body.mu.copy()
+    body.mu[3] = -1.0
+    st, _, _, _ = inspect(body)
+    assert st == N.PDGB_ERR_BAD_MESH
+    assert "weight" in N.lib().pdgb_last_error().decode()
