@@ -61,6 +61,30 @@ def test_high_valence_vertex_vs_oracle(solver):
     assert rel_l2(X, Xo) < TOL
 
 
+def test_vertices_outside_every_tet_vs_oracle():
+    """Vertices that no tet references (free particles, one of them pinned)
+    are in no tile: they keep the inertial iterate through the fused
+    iterations and still get the final velocity / position update."""
+    body = mesh.make_grid_body(4, 3, 5, young=1e5, poisson=0.4, jitter=0.1, seed=9)
+    extra = np.array([[2.0, 0.5, 0.5], [-1.0, 0.2, 0.1], [0.5, 3.0, 0.5]], np.float32)
+    body.X = np.concatenate([body.X, extra])
+    body.mass = np.concatenate([body.mass, np.array([0.5, 2.0, 1.0], np.float32)])
+    body.dbc = np.concatenate([body.dbc, np.array([0.0, 0.0, 1.0], np.float32)])
+    body.V = np.zeros_like(body.X)
+    body.V[-2] = (0.3, 0.0, -0.2)
+    for solver, rho in ((0, 0.9995), (1, 0.9992)):
+        params = SolverParams(num_iterations=20, rho=rho, solver=solver)
+        with PdSolver(body, params) as e:
+            e.update(12)
+            X, V = e.download_state()
+        Xo, Vo, _ = O.simulate(body, params, 12, precision=64, V=body.V)
+        assert rel_l2(X, Xo) < TOL, solver
+        assert np.allclose(X[-3:], Xo[-3:], rtol=0, atol=1e-5), solver
+        # velocities are position changes / h: one float ulp of a 2 m
+        # coordinate is 2.4e-7 m, i.e. 3e-5 m/s at h = 1/120
+        assert np.allclose(V[-3:], Vo[-3:], rtol=0, atol=5e-4), solver
+
+
 def test_large_grid_first_steps_vs_oracle():
     """64^3 cells (274,625 verts / 1,310,720 tets): 2 steps vs the FP64 oracle."""
     body = mesh.cube_c2()
