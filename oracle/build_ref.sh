@@ -52,6 +52,31 @@ kernel_text() {  # kernel_text FILE NAME TEMPLATE-HEAD: one __global__ function,
     echo '#include "fixed_harness.inc"'
 } | "${CXX[@]}" -x c++ -include "$HERE/refshim/shim.h" "${SINC[@]}" -c - -o "$OUT/ref_scene.o"
 "${CXX[@]}" -include "$HERE/refshim/shim.h" "${SINC[@]}" -c "$RR/rigid.cpp" -o "$OUT/rigid.o"
+
+# Collision unit: the reference's continuous-collision query from
+# src/collision/intersections.cu -- stp, solveQuadratic, newtonsMethod,
+# solveCubic, signed_vf_distance, signed_ee_distance and ccdCollisionTest --
+# read function by function and piped to the compiler like the scene unit.
+fn_text() {  # fn_text FILE NAME: one template function definition, its template line included
+    awk -v name="$2" '
+        /^template<typename (T|Scalar)>[ ]*$/ { hold = $0; next }
+        {
+            if (!p && hold != "" && index($0, " " name "(") > 0 && $0 !~ /\);[ ]*$/) {
+                print hold; print; hold = ""
+                if ($0 ~ /{/ && $0 ~ /}[ ]*$/) next
+                p = 1; next
+            }
+            if (p) { print; if ($0 ~ /^}/) p = 0; next }
+            hold = ""
+        }' "$1"
+}
+{
+    echo '#include "ccd_prelude.h"'
+    for f in stp solveQuadratic newtonsMethod solveCubic signed_vf_distance signed_ee_distance ccdCollisionTest; do
+        fn_text "$R/src/collision/intersections.cu" "$f"
+    done
+    echo '#include "ccd_harness.inc"'
+} | "${CXX[@]}" -x c++ -include "$HERE/refshim/shim.h" "${SINC[@]}" -c - -o "$OUT/ref_ccd.o"
 g++ -shared -fopenmp -o "$OUT/libref_pd.so.tmp" "$OUT/pdUtil.o" "$OUT/ref_harness.o" "$OUT/pd_oracle.o" \
-    "$OUT/ref_scene.o" "$OUT/rigid.o"
+    "$OUT/ref_scene.o" "$OUT/rigid.o" "$OUT/ref_ccd.o"
 mv "$OUT/libref_pd.so.tmp" "$OUT/libref_pd.so"

@@ -24,6 +24,9 @@
  *   - response: tI < 1 -> V = -(d . n) n with d = XTilde - X and X kept,
  *     else X = XTilde (CCDKernel, collisionUtil.cu:50-70).
  *
+ * Thresholds are double constants compared against float values, as in the
+ * reference (its literals are doubles); the arithmetic itself is float.
+ *
  * Deterministic where the reference is not: the reference picks among equal
  * contact times by an unstable sort and lets concurrent writes of a
  * vertex's normal race; here ties go to the smaller face / edge index, and
@@ -64,8 +67,8 @@ int quad_roots(float a, float b, float c, float* x) {
     const float sgn = (b > 0) ? 1.0f : (b < 0 ? -1.0f : 0.0f);
     const float q = -(b + sgn * std::sqrt(d)) / 2;
     int n = 0;
-    if (std::fabs(a) > 1e-12f * std::fabs(q)) x[n++] = q / a;
-    if (std::fabs(q) > 1e-12f * std::fabs(c)) x[n++] = c / q;
+    if (std::fabs(a) > 1e-12 * std::fabs(q)) x[n++] = q / a;
+    if (std::fabs(q) > 1e-12 * std::fabs(c)) x[n++] = c / q;
     if (n == 2 && x[0] > x[1]) std::swap(x[0], x[1]);
     return n;
 }
@@ -83,7 +86,7 @@ float cubic_newton(float a, float b, float c, float d, float x0, int dir) {
         const float dy = c + x0 * (2 * b + x0 * 3 * a);
         if (dy == 0) return x0;
         const float x1 = x0 - y / dy;
-        if (std::fabs(x0 - x1) < 1e-6f) return x0;
+        if (std::fabs(x0 - x1) < 1e-6) return x0;
         x0 = x1;
     }
     return x0;
@@ -113,7 +116,7 @@ int cubic_roots(float a, float b, float c, float d, float* x) {
 // barycentric weights w (w0 = 1, w1..3 = minus the face coordinates).
 float face_distance(V3 p, V3 y0, V3 y1, V3 y2, V3& n, float w[4]) {
     n = cross(unit(y1 - y0), unit(y2 - y0));
-    if (len2(n) < 1e-6f) return FLT_MAX;
+    if (len2(n) < 1e-6) return FLT_MAX;
     n = unit(n);
     const float h = dot(p - y0, n);
     const float b0 = triple(y1 - p, y2 - p, n), b1 = triple(y2 - p, y0 - p, n), b2 = triple(y0 - p, y1 - p, n);
@@ -129,7 +132,7 @@ float face_distance(V3 p, V3 y0, V3 y1, V3 y2, V3& n, float w[4]) {
 // and weights (w0, w1 on the first edge, -w2, -w3 on the second).
 float edge_distance(V3 x0, V3 x1, V3 y0, V3 y1, V3& n, float w[4]) {
     n = cross(unit(x1 - x0), unit(y1 - y0));
-    if (len2(n) < 1e-6f) return FLT_MAX;
+    if (len2(n) < 1e-6) return FLT_MAX;
     n = unit(n);
     const float h = dot(x0 - y0, n);
     const float a0 = triple(y1 - x1, y0 - x1, n), a1 = triple(y0 - x0, y1 - x0, n);
@@ -151,11 +154,11 @@ float contact_time(bool face, const V3 x[4], const V3 v[4], V3& n) {
     const float a2 = triple(x01, v02, v03) + triple(v01, x02, v03) + triple(v01, v02, x03);
     const float a3 = triple(v01, v02, v03);
     n = {0, 0, 0};
-    if (std::fabs(a0) < 1e-12f * len(x01) * len(x02) * len(x03)) return 1.0f;  // coplanar at t = 0
+    if (std::fabs(a0) < 1e-12 * len(x01) * len(x02) * len(x03)) return 1.0f;  // coplanar at t = 0
     float t[3];
     const int nr = cubic_roots(a3, a2, a1, a0, t);
     for (int i = 0; i < nr; ++i) {
-        if (t[i] < -1e-12f || t[i] > 1) continue;
+        if (t[i] < -1e-12 || t[i] > 1) continue;
         V3 xt[4];
         for (int k = 0; k < 4; ++k) xt[k] = x[k] + t[i] * v[k];
         float w[4] = {0, 0, 0, 0};
@@ -163,13 +166,13 @@ float contact_time(bool face, const V3 x[4], const V3 v[4], V3& n) {
         bool inside;
         if (face) {
             d = face_distance(xt[0], xt[1], xt[2], xt[3], n, w);
-            inside = std::min(-w[1], std::min(-w[2], -w[3])) >= -1e-3f;
+            inside = std::min(-w[1], std::min(-w[2], -w[3])) >= -1e-3;
         } else {
             d = edge_distance(xt[0], xt[1], xt[2], xt[3], n, w);
-            inside = std::min(w[0], std::min(w[1], std::min(-w[2], -w[3]))) >= -1e-3f;
+            inside = std::min(w[0], std::min(w[1], std::min(-w[2], -w[3]))) >= -1e-3;
         }
         if (dot(n, w[1] * v[1] + w[2] * v[2] + w[3] * v[3]) > 0) n = -1.0f * n;
-        if (std::fabs(d) < 1e-6f && inside) return t[i];
+        if (std::fabs(d) < 1e-6 && inside) return t[i];
     }
     return 1.0f;
 }

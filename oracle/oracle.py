@@ -80,6 +80,12 @@ def _load_oracle():
         h.orc_solve3.restype = C.c_int
         h.orc_solve3.argtypes = [C.c_int, C.c_int, _F32, _U32, _F32, _F32, C.c_void_p, C.c_float, C.c_float,
                                  _F64, _F64]
+        h.orc_ccd_query.restype = C.c_float
+        h.orc_ccd_query.argtypes = [C.c_int, _U32, _F32, _F32, _F32]
+        h.orc_ccd_detect.restype = C.c_int
+        h.orc_ccd_detect.argtypes = [C.c_int, C.c_int, _U32, _I32, _F32, _F32, _F32, _F32, _I64]
+        h.orc_ccd_response.restype = None
+        h.orc_ccd_response.argtypes = [C.c_int, _F32, _F32, _F32, _F32, _F32]
         _orc = h
     return _orc
 
@@ -106,6 +112,8 @@ def _load_ref():
         h.ref_fixed_frame.argtypes = [C.c_int, _F32, _F32, _F32, _F32, _F32]
         h.ref_rotation.restype = None
         h.ref_rotation.argtypes = [_F32, _F32]
+        h.ref_ccd_query.restype = C.c_float
+        h.ref_ccd_query.argtypes = [C.c_int, _U32, _F32, _F32, _F32]
         _ref = h
     return _ref
 
@@ -355,3 +363,49 @@ def solve3(body, dt: float, b: np.ndarray, positional_weight: float = 1e6) -> np
     if st != 0:
         raise RuntimeError("orc_solve3 failed")
     return x.reshape(-1, 3)
+
+
+# ------------------------------------------------------- continuous collision
+def _f32(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    return a
+
+
+def ccd_query(face: bool, ids, X, XT):
+    """Contact time and normal of one query (face: vertex ids[0] against face
+    ids[1:4]; else edge ids[0:2] against edge ids[2:4]), float, restating the
+    reference's ccdCollisionTest (intersections.cu:286-334)."""
+    n = np.zeros(3, np.float32)
+    t = _load_oracle().orc_ccd_query(1 if face else 0, np.ascontiguousarray(ids, np.uint32), _f32(X), _f32(XT), n)
+    return float(t), n
+
+
+def reference_ccd_query(face: bool, ids, X, XT):
+    """The same query evaluated by the reference's own code (oracle/_ref)."""
+    n = np.zeros(3, np.float32)
+    t = _load_ref().ref_ccd_query(1 if face else 0, np.ascontiguousarray(ids, np.uint32), _f32(X), _f32(XT), n)
+    return float(t), n
+
+
+def ccd_detect(tris, tri_body, X, XT):
+    """Collision detection between bodies (the reference's DetectCollision
+    with ignoreSelfCollision): returns (tI [nv], normals [nv, 3], stats)
+    where stats = (candidate pairs, vertices with a face contact, vertices
+    marked)."""
+    X = _f32(X)
+    nv = X.size // 3
+    tris = np.ascontiguousarray(tris, np.uint32).reshape(-1)
+    body = np.ascontiguousarray(tri_body, np.int32)
+    tI = np.empty(nv, np.float32)
+    nrm = np.empty(3 * nv, np.float32)
+    stats = np.zeros(3, np.int64)
+    _load_oracle().orc_ccd_detect(nv, tris.size // 3, tris, body, X, _f32(XT), tI, nrm, stats)
+    return tI, nrm.reshape(nv, 3), tuple(int(v) for v in stats)
+
+
+def ccd_response(tI, normals, X, XT, V):
+    """CCDKernel (collisionUtil.cu:50-70) on copies of X and V; returns them."""
+    X = _f32(X).copy()
+    V = _f32(V).copy()
+    _load_oracle().orc_ccd_response(tI.size, np.ascontiguousarray(tI, np.float32), _f32(normals), X, _f32(XT), V)
+    return X.reshape(-1, 3), V.reshape(-1, 3)

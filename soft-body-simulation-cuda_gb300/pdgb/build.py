@@ -79,13 +79,14 @@ def build_engine(force: bool = False, verbose: bool = False) -> Path:
 
 
 def build_oracle(force: bool = False) -> Path:
-    src = ORACLE_DIR / "pd_oracle.cpp"
-    deps = [src, ORACLE_DIR / "pd_oracle.h"]
+    srcs = [ORACLE_DIR / "pd_oracle.cpp", ORACLE_DIR / "ccd_oracle.cpp"]
+    deps = srcs + [ORACLE_DIR / "pd_oracle.h"]
     if not force and not _stale(ORACLE_LIB, deps):
         return ORACLE_LIB
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
     tmp = ORACLE_LIB.with_suffix(".so.tmp")
-    _run(["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", str(src), "-o", str(tmp)])
+    _run(["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"] + [str(x) for x in srcs]
+         + ["-o", str(tmp)])
     os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
 
@@ -97,8 +98,7 @@ def build_reference_harness(force: bool = False) -> Path | None:
     if not ref_root.exists() or not script.exists():
         return None
     out = ORACLE_DIR / "_ref" / "libref_pd.so"
-    deps = [script, ORACLE_DIR / "refshim" / "shim.h", ORACLE_DIR / "refshim" / "ref_harness.cpp",
-            ORACLE_DIR / "pd_oracle.cpp"]
+    deps = [script, ORACLE_DIR / "pd_oracle.cpp"] + sorted((ORACLE_DIR / "refshim").glob("*.*"))
     if not force and not _stale(out, [d for d in deps if d.exists()]):
         return out
     _run(["bash", str(script), str(ref_root)], cwd=ORACLE_DIR)

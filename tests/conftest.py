@@ -101,3 +101,38 @@ def fan_body(n: int = 100, seed: int = 0):
     dbc[top] = 1.0
     return mesh.SoftBody(X=X.astype(np.float32), tets=tets.astype(np.uint32), mass=mass.astype(np.float32), mu=mu,
                          dbc=dbc)
+
+
+def ccd_scene(kind: str, seed: int = 0):
+    """Two-body continuous-collision scenes: (tris [m, 3], tri_body [m], X,
+    XT, bodies).  X are start positions, XT end positions of one step.
+      "drop"  : body 1 (a 3x2x3-cell block) falls through the top of body 0
+      "apart" : the same bodies moving away from each other
+      "shear" : body 1 slides sideways across body 0 while sinking into it
+    """
+    from pdgb import mesh
+    from pdgb.meshio import surface_triangles
+
+    rng = np.random.default_rng(seed)
+    a = mesh.make_grid_body(4, 2, 4, size=(0.4, 0.2, 0.4), jitter=0.05, seed=seed, pin=None)
+    b = mesh.make_grid_body(3, 2, 3, size=(0.3, 0.2, 0.3), origin=(0.05, 0.23, 0.05), jitter=0.05,
+                            seed=seed + 1, pin=None)
+    body = mesh.concat([a, b])
+    nva = a.num_verts
+    tris = np.concatenate([surface_triangles(a.tets), surface_triangles(b.tets) + nva])
+    tri_body = np.concatenate([np.zeros(len(surface_triangles(a.tets)), np.int32),
+                               np.ones(len(surface_triangles(b.tets)), np.int32)])
+    X = body.X.astype(np.float32)
+    D = np.zeros_like(X)
+    noise = rng.uniform(-0.004, 0.004, X.shape).astype(np.float32)
+    if kind == "drop":
+        D[nva:] = (0.0, -0.12, 0.0)
+    elif kind == "apart":
+        D[nva:] = (0.0, 0.12, 0.0)
+        D[:nva] = (0.0, -0.05, 0.0)
+    elif kind == "shear":
+        D[nva:] = (0.15, -0.08, 0.05)
+    else:
+        raise ValueError(kind)
+    XT = (X + D + noise).astype(np.float32)
+    return tris.astype(np.uint32), tri_body, X, XT, body

@@ -15,7 +15,9 @@ fixed rigid bodies (see make_scene_case).
 
 Also `rotations.npz`: random deformation gradients (including inverted and
 nearly flat ones) with the reference's rotation R = U V^T (svd.cuh:7-14 +
-pdUtil.cu:113-122).
+pdUtil.cu:113-122), and `ccd_queries.npz`: random continuous-collision
+queries with the reference's contact times and normals
+(src/collision/intersections.cu:286-334).
 
 The reference's Cholesky branch calls cuSOLVER; the CPU harness solves the
 same 3n x 3n system exactly in double instead.
@@ -148,6 +150,26 @@ def make_rotations() -> Path:
     return out
 
 
+def make_ccd_queries() -> Path:
+    """Random point-face and edge-edge continuous-collision queries (4 points
+    moving from X to XT each) with the reference's own contact time and normal
+    (ccdCollisionTest, intersections.cu:286-334).  About 1 in 14 collides."""
+    rng = np.random.default_rng(17)
+    q = 2048
+    X = rng.uniform(-1.0, 1.0, (q, 4, 3)).astype(np.float32)
+    D = (rng.uniform(-1.0, 1.0, (q, 4, 3)) * rng.uniform(0.2, 2.0, (q, 1, 1))).astype(np.float32)
+    XT = (X + D).astype(np.float32)
+    face = (np.arange(q) % 2).astype(np.int32)
+    toi = np.empty(q, np.float32)
+    nrm = np.empty((q, 3), np.float32)
+    ids = np.arange(4, dtype=np.uint32)
+    for k in range(q):
+        toi[k], nrm[k] = O.reference_ccd_query(bool(face[k]), ids, X[k], XT[k])
+    out = HERE / "ccd_queries.npz"
+    np.savez_compressed(out, X=X, XT=XT, face=face, toi=toi, normal=nrm)
+    return out
+
+
 def main() -> None:
     if not O.reference_available():
         raise SystemExit("oracle/_ref/libref_pd.so is missing: build it with oracle/build_ref.sh")
@@ -158,6 +180,8 @@ def main() -> None:
         p = make_scene_case(name)
         print("wrote", p.relative_to(ROOT), p.stat().st_size, "bytes")
     p = make_rotations()
+    print("wrote", p.relative_to(ROOT), p.stat().st_size, "bytes")
+    p = make_ccd_queries()
     print("wrote", p.relative_to(ROOT), p.stat().st_size, "bytes")
 
 
