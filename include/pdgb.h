@@ -403,6 +403,45 @@ int pdgb_set_fixed_bodies(pdgb_engine* e, const pdgb_fixed_body* bodies, int n, 
 int pdgb_download_xtilde(pdgb_engine* e, float* XT, int memory);
 
 /* ---------------------------------------------------------------------
+ * Continuous collision between bodies.  Replaces the reference's
+ * CollisionDetection::DetectCollision(..., ignoreSelfCollision = true) +
+ * CCDKernel that PdSolver::Update runs after each step when collision
+ * handling is on (src/simulation/solver/projective/pdSolver.cu:218-224;
+ * src/collision/bvh.cu:153-165, broadphase.cu, narrowphase.cu,
+ * intersections.cu:286-334; src/simulation/collisionUtil.cu:50-70):
+ *   - candidates: surface triangles of different bodies that share no
+ *     vertex and whose swept boxes (X -> XTilde) overlap (GPU LBVH);
+ *   - per pair, both ways: 3 point-face and 9 edge-edge continuous tests
+ *     (coplanarity cubic, proximity 1e-6, barycentric slack 1e-3);
+ *   - per vertex / per edge the earliest contact; every vertex of such a
+ *     contact before t = 1 gets tI = 0.5 and the normal of the earliest
+ *     contact touching it (the reference lets these writes race);
+ *   - response: tI < 1 -> X is kept and V = -(d . n) n with
+ *     d = XTilde - X (a displacement, as in the reference); else X = XTilde.
+ *     The fixed-body correction of XTilde and V follows (pdSolver.cu:228).
+ * Triangles are caller vertex ids (3 per triangle); tri_body gives each
+ * triangle's body (NULL: the body of its first vertex, from the engine's
+ * body ranges).  Detection waits for the stream once per step (the
+ * candidate count sizes the narrow phase, as in the reference). */
+typedef struct pdgb_collision_info {
+    long long candidate_pairs;  /* triangle pairs tested by the last detection */
+    int vertices_hit;           /* vertices with tI < 1 after it               */
+    int regrows;                /* candidate-buffer enlargements so far        */
+    double detect_ms;           /* device time of the last detection           */
+} pdgb_collision_info;
+int pdgb_set_collision_surface(pdgb_engine* e, const uint32_t* tris, const int* tri_body, int num_tris);
+/* on != 0: every step runs detection + response (needs a surface). */
+int pdgb_enable_collision(pdgb_engine* e, int on);
+/* tI [nv], normals [3 nv] (host, caller order, nullable) and statistics of
+ * the last detection. */
+int pdgb_get_collision(pdgb_engine* e, float* tI, float* normals, pdgb_collision_info* info);
+/* One detection on host arrays, no engine: X (start) and XT (end) [3 nv];
+ * outputs tI [nv] and normals [3 nv] (zero where tI = 1).  Uses the current
+ * CUDA device and its default stream. */
+int pdgb_ccd_detect(int num_verts, int num_tris, const uint32_t* tris, const int* tri_body, const float* X,
+                    const float* XT, float* tI, float* normals, pdgb_collision_info* info);
+
+/* ---------------------------------------------------------------------
  * Tet-mesh files (host only, no GPU needed).  Replaces the reference's
  * DataLoader::CollectData for one soft body (src/simulation/dataLoader.cu:
  * 38-290; Gmsh reader src/simulation/MshLoader.cpp):

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "ccd.h"
 #include "cholesky.h"
 #include "engine.h"
 #include "solve.h"
@@ -76,6 +77,9 @@ struct pdgb_engine {
     DBuf<FixedBodyDev> fixed;
     int nfixed = 0;
     float mu_t = 0.5f, mu_n = 0.5f;
+    // continuous collision between bodies
+    std::unique_ptr<CcdContext> ccd;
+    bool ccd_on = false;
     int num_pinned = 0;
     // step graph
     cudaGraph_t graph = nullptr;
@@ -184,7 +188,15 @@ SceneArgs scene_args(pdgb_engine* e) {
     sc.nfixed = e->nfixed;
     sc.mu_t = e->mu_t;
     sc.mu_n = e->mu_n;
+    sc.ccd = e->ccd_on ? 1 : 0;
     return sc;
+}
+
+// Collision detection + response after a step (PdSolver::Update,
+// pdSolver.cu:218-231).
+void run_collision(pdgb_engine* e) {
+    e->ccd->detect(e->x.p, e->xt.p);
+    e->ccd->respond(e->x.p, e->xt.p, e->v.p, scene_args(e));
 }
 
 BeginArgs begin_args(pdgb_engine* e) {
@@ -639,11 +651,13 @@ int pdgb_step(pdgb_engine* e, int nsteps) {
                 cudaEvent_t* pr = &e->step_pairs[2 * e->step_pairs_used++];
                 PDGB_CUDA_TRY(cudaEventRecord(pr[0], e->stream));
                 PDGB_CUDA_TRY(cudaGraphLaunch(e->gexec, e->stream));
+                if (e->ccd_on) run_collision(e);
                 PDGB_CUDA_TRY(cudaEventRecord(pr[1], e->stream));
                 continue;
             }
             if (e->timing) PDGB_CUDA_TRY(cudaEventRecord(e->step_ev[0], e->stream));
             PDGB_CUDA_TRY(cudaGraphLaunch(e->gexec, e->stream));
+            if (e->ccd_on) run_collision(e);
             if (e->timing) {
                 PDGB_CUDA_TRY(cudaEventRecord(e->step_ev[1], e->stream));
                 PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
@@ -1082,6 +1096,116 @@ int pdgb_download_xtilde(pdgb_engine* e, float* XT, int memory) {
             throw Error{PDGB_ERR_INVALID_ARGUMENT, "bad memory kind"};
         }
         PDGB_CUDA_TRY(cudaGetLastError());
+    });
+}
+
+int pdgb_set_collision_surface(pdgb_engine* e, const uint32_t* tris, const int* tri_body, int num_tris) {
+    if (!e || num_tris < 0 || (num_tris > 0 && !tris)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or triangle list");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        std::vector<int> body(num_tris, 0);
+        for (int t = 0; t < num_tris; ++t) {
+            if (tri_body) {
+                body[t] = tri_body[t];
+            } else {
+                const uint32_t v = tris[3 * (size_t)t];
+                if (v < (uint32_t)e->nv && e->nbodies > 1)
+                    body[t] = (int)(std::upper_bound(e->body_vstart.begin(), e->body_vstart.end(), (int)v) -
+                                    e->body_vstart.begin()) - 1;
+            }
+        }
+        const CcdSurface surf = build_ccd_surface(e->nv, num_tris, tris, body.data(), e->L.viperm.data());
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        e->ccd.reset(new CcdContext(surf, e->vperm.p, e->stream));
+    });
+}
+
+int pdgb_enable_collision(pdgb_engine* e, int on) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (on && !e->ccd) throw Error{PDGB_ERR_INVALID_ARGUMENT, "no collision surface set"};
+        if (on && !e->xt.p) {  // XTilde starts as X
+            e->xt.alloc(e->nv);
+            launch_copy_state(e->nv, e->x.p, e->xt.p, e->stream);
+            PDGB_CUDA_TRY(cudaGetLastError());
+            PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+        }
+        if ((on != 0) != e->ccd_on) {
+            e->ccd_on = on != 0;
+            e->prepared = false;  // the step epilogue changes
+        }
+    });
+}
+
+int pdgb_get_collision(pdgb_engine* e, float* tI, float* normals, pdgb_collision_info* info) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (!e->ccd) throw Error{PDGB_ERR_INVALID_ARGUMENT, "no collision surface set"};
+        const size_t nv = e->nv;
+        if (tI || normals) {
+            std::vector<float> t(nv);
+            std::vector<float4> n(nv);
+            PDGB_CUDA_TRY(cudaMemcpyAsync(t.data(), e->ccd->tI(), nv * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+            PDGB_CUDA_TRY(cudaMemcpyAsync(n.data(), e->ccd->normals(), nv * sizeof(float4), cudaMemcpyDeviceToHost,
+                                          e->stream));
+            PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+            for (size_t i = 0; i < nv; ++i) {
+                const size_t o = (size_t)e->L.vperm[i];
+                if (tI) tI[o] = t[i];
+                if (normals) {
+                    normals[3 * o] = n[i].x;
+                    normals[3 * o + 1] = n[i].y;
+                    normals[3 * o + 2] = n[i].z;
+                }
+            }
+        }
+        if (info) {
+            const CcdStats& st = e->ccd->stats();
+            info->candidate_pairs = st.pairs;
+            info->vertices_hit = st.marked;
+            info->regrows = st.regrows;
+            info->detect_ms = st.ms;
+        }
+    });
+}
+
+int pdgb_ccd_detect(int num_verts, int num_tris, const uint32_t* tris, const int* tri_body, const float* X,
+                    const float* XT, float* tI, float* normals, pdgb_collision_info* info) {
+    if (num_verts <= 0 || num_tris < 0 || !X || !XT || !tI || !normals || (num_tris > 0 && (!tris || !tri_body))) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad sizes or null arrays");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    return guarded([&] {
+        const size_t nv = num_verts;
+        for (size_t i = 0; i < 3 * nv; ++i)
+            if (!std::isfinite(X[i]) || !std::isfinite(XT[i])) throw Error{PDGB_ERR_NONFINITE, "non-finite position"};
+        const CcdSurface surf = build_ccd_surface(num_verts, num_tris, tris, tri_body, nullptr);
+        std::vector<float4> h(2 * nv);
+        for (size_t i = 0; i < nv; ++i) {
+            h[i] = make_float4(X[3 * i], X[3 * i + 1], X[3 * i + 2], 0.f);
+            h[nv + i] = make_float4(XT[3 * i], XT[3 * i + 1], XT[3 * i + 2], 0.f);
+        }
+        DBuf<float4> d;
+        d.upload(h, nullptr);
+        CcdContext ctx(surf, nullptr, nullptr);
+        ctx.detect(d.p, d.p + nv);
+        std::vector<float4> n(nv);
+        PDGB_CUDA_TRY(cudaMemcpyAsync(tI, ctx.tI(), nv * sizeof(float), cudaMemcpyDeviceToHost, nullptr));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(n.data(), ctx.normals(), nv * sizeof(float4), cudaMemcpyDeviceToHost, nullptr));
+        PDGB_CUDA_TRY(cudaStreamSynchronize(nullptr));
+        for (size_t i = 0; i < nv; ++i) {
+            normals[3 * i] = n[i].x;
+            normals[3 * i + 1] = n[i].y;
+            normals[3 * i + 2] = n[i].z;
+        }
+        if (info) {
+            info->candidate_pairs = ctx.stats().pairs;
+            info->vertices_hit = ctx.stats().marked;
+            info->regrows = ctx.stats().regrows;
+            info->detect_ms = ctx.stats().ms;
+        }
     });
 }
 

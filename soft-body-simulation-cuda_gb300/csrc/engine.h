@@ -170,6 +170,8 @@ struct SceneArgs {
     const FixedBodyDev* fixed;
     int nfixed;
     float mu_t, mu_n;
+    int ccd;                  // collision handling on: the step writes XTilde only; X and the
+                              // fixed-body correction follow the collision response
 };
 
 struct VertexArgs {

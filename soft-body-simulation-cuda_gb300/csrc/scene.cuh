@@ -70,12 +70,19 @@ __device__ __forceinline__ void collide_fixed(const SceneArgs& sc, float3& X, fl
 // Step epilogue for one vertex: v = (q - XTilde) / h (0 for dragged
 // vertices), X = XTilde = q, then the fixed-body correction of XTilde and v
 // (updateVelPos pdUtil.cu:180-193; Update tail pdSolver.cu:218-232: X is
-// copied before the correction, so X keeps the uncorrected position).
+// copied before the correction, so X keeps the uncorrected position).  With
+// collision handling on, only XTilde and v are written here: the collision
+// response decides X, then corrects for the fixed bodies.
 __device__ __forceinline__ void finish_vertex(const SceneArgs& sc, int i, float4 q, float dt_inv, float4* x,
                                               float4* v) {
     const float4 xo = sc.xt ? sc.xt[i] : x[i];
     float3 V = make_float3((q.x - xo.x) * dt_inv, (q.y - xo.y) * dt_inv, (q.z - xo.z) * dt_inv);
     if (drag_weight(sc, i) > 0.f) V = make_float3(0.f, 0.f, 0.f);
+    if (sc.ccd) {
+        sc.xt[i] = make_float4(q.x, q.y, q.z, 0.f);
+        v[i] = make_float4(V.x, V.y, V.z, 0.f);
+        return;
+    }
     x[i] = make_float4(q.x, q.y, q.z, 0.f);
     if (sc.xt) {
         float3 X = make_float3(q.x, q.y, q.z);

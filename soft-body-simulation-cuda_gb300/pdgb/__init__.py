@@ -6,7 +6,8 @@ provides the synthetic soft bodies used by tests and benchmarks.
 """
 from . import mesh, meshio, scene
 from ._native import PdgbError, library_path
-from .engine import PdSolver, SolverParams, SolverType
+from .engine import PdSolver, SolverParams, SolverType, ccd_detect
 from .server import PdServer
 
-__all__ = ["mesh", "meshio", "scene", "PdSolver", "PdServer", "SolverParams", "SolverType", "PdgbError", "library_path"]
+__all__ = ["mesh", "meshio", "scene", "PdSolver", "PdServer", "SolverParams", "SolverType", "PdgbError", "library_path",
+           "ccd_detect"]

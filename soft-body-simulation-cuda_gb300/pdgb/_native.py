@@ -207,6 +207,15 @@ class pdgb_tune_report(C.Structure):
 
 
 # name -> (restype, argtypes); every symbol include/pdgb.h declares.
+class pdgb_collision_info(C.Structure):
+    _fields_ = [
+        ("candidate_pairs", C.c_longlong),
+        ("vertices_hit", C.c_int),
+        ("regrows", C.c_int),
+        ("detect_ms", C.c_double),
+    ]
+
+
 SIGNATURES = {
     "pdgb_default_params": (None, [C.POINTER(pdgb_params)]),
     "pdgb_create": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_params), C.c_void_p, C.POINTER(C.c_void_p)]),
@@ -263,6 +272,11 @@ SIGNATURES = {
     "pdgb_clear_drag": (C.c_int, [C.c_void_p]),
     "pdgb_set_fixed_bodies": (C.c_int, [C.c_void_p, C.POINTER(pdgb_fixed_body), C.c_int, C.c_float, C.c_float]),
     "pdgb_download_xtilde": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "pdgb_set_collision_surface": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "pdgb_enable_collision": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_get_collision": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(pdgb_collision_info)]),
+    "pdgb_ccd_detect": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.POINTER(pdgb_collision_info)]),
     "pdgb_load_body_file": (C.c_int, [C.POINTER(pdgb_body_file), C.POINTER(C.POINTER(pdgb_tet_mesh))]),
     "pdgb_free_tet_mesh": (None, [C.POINTER(pdgb_tet_mesh)]),
     "pdgb_surface_triangles": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_int)]),

@@ -53,7 +53,7 @@ def engine_sources() -> list[Path]:
 
 def build_engine(force: bool = False, verbose: bool = False) -> Path:
     srcs = engine_sources()
-    deps = srcs + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "pdgb.h"]
+    deps = srcs + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "pdgb.h", Path(__file__)]
     if not force and not _stale(LIB_PATH, deps):
         return LIB_PATH
     nvcc = _nvcc()
@@ -62,9 +62,12 @@ def build_engine(force: bool = False, verbose: bool = False) -> Path:
     common = ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off,-fopenmp",
                            "-I", str(ROOT / "include")]
 
+    # the collision narrow phase matches the CPU oracle operation for operation
+    per_file = {"ccd.cu": ["--fmad=false"]}
+
     def compile_one(src: Path) -> Path:
         obj = obj_dir / (src.name + ".o")
-        cmd = [nvcc] + common + ["-c", str(src), "-o", str(obj)]
+        cmd = [nvcc] + common + per_file.get(src.name, []) + ["-c", str(src), "-o", str(obj)]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         _run(cmd)

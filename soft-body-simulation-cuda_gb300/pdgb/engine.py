@@ -134,6 +134,27 @@ class PdSolver:
         N.check(self._lib.pdgb_download_xtilde(self._h, _ptr(XT), N.PDGB_MEM_HOST), "pdgb_download_xtilde")
         return XT
 
+    def set_collision_surface(self, tris: np.ndarray, tri_body: np.ndarray | None = None) -> None:
+        """Surface triangles (caller vertex ids) for continuous collision
+        between bodies; tri_body: body of each triangle (None: from the
+        engine's body ranges)."""
+        t = np.ascontiguousarray(tris, dtype=np.uint32).reshape(-1, 3)
+        b = None if tri_body is None else np.ascontiguousarray(tri_body, dtype=np.int32)
+        N.check(self._lib.pdgb_set_collision_surface(self._h, t.ctypes.data, None if b is None else b.ctypes.data,
+                                                     t.shape[0]), "pdgb_set_collision_surface")
+
+    def enable_collision(self, on: bool = True) -> None:
+        N.check(self._lib.pdgb_enable_collision(self._h, 1 if on else 0), "pdgb_enable_collision")
+
+    def collision(self) -> tuple[np.ndarray, np.ndarray, dict]:
+        """tI [nv], normals [nv, 3] and statistics of the last detection."""
+        tI = np.empty(self.num_verts, np.float32)
+        nrm = np.empty((self.num_verts, 3), np.float32)
+        info = N.pdgb_collision_info()
+        N.check(self._lib.pdgb_get_collision(self._h, tI.ctypes.data, nrm.ctypes.data, C.byref(info)),
+                "pdgb_get_collision")
+        return tI, nrm, {k: getattr(info, k) for k, _ in info._fields_}
+
     def render_surface(self, tris_ptr: int, num_tris: int, pos_ptr: int, nor_ptr: int) -> None:
         """Per-triangle corner positions (float[9 n]) and normals (float[12 n])
         of the current state into device buffers; tris_ptr: device uint32[3 n]
@@ -263,3 +284,19 @@ class PdSolver:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def ccd_detect(tris: np.ndarray, tri_body: np.ndarray, X: np.ndarray, XT: np.ndarray):
+    """One continuous-collision detection on the GPU between start positions
+    X and end positions XT (host arrays): (tI [nv], normals [nv, 3], info)."""
+    lib = N.lib()
+    X = np.ascontiguousarray(X, np.float32).reshape(-1, 3)
+    XT = np.ascontiguousarray(XT, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(tris, np.uint32).reshape(-1, 3)
+    b = np.ascontiguousarray(tri_body, np.int32)
+    tI = np.empty(X.shape[0], np.float32)
+    nrm = np.empty((X.shape[0], 3), np.float32)
+    info = N.pdgb_collision_info()
+    N.check(lib.pdgb_ccd_detect(X.shape[0], t.shape[0], t.ctypes.data, b.ctypes.data, X.ctypes.data, XT.ctypes.data,
+                                tI.ctypes.data, nrm.ctypes.data, C.byref(info)), "pdgb_ccd_detect")
+    return tI, nrm, {k: getattr(info, k) for k, _ in info._fields_}
