@@ -428,6 +428,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-oracle error report")
     ap.add_argument("--window", type=float, default=20.0, help="arrival window of the serving workload, seconds")
     ap.add_argument("--rate", type=float, default=0.0, help="serving: mean arrivals per second (0 = the workload's)")
+    ap.add_argument("--collision", action="store_true", help="run continuous collision between bodies after every "
+                    "step (inside the timed region)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "pdgb":
         args.warmup = 3
@@ -489,6 +491,21 @@ def main():
             flush.add_(1.0)
 
     eng.prepare()
+    collision = None
+    if args.collision:
+        # continuous collision between bodies after every step (the
+        # reference's PdSolver::Update with collision handling on)
+        from pdgb.meshio import surface_triangles
+
+        parts, off = [], 0
+        for b in (bodies if bodies is not None else [body]):
+            parts.append(surface_triangles(b.tets) + np.uint32(off))
+            off += b.num_verts
+        ctris = np.concatenate(parts)
+        eng.set_collision_surface(ctris)
+        eng.enable_collision(True)
+        collision = {"surface_tris": int(ctris.shape[0])}
+        WORKLOAD["collision"] = "continuous collision between bodies after every step"
     tune = None
     if not args.no_autotune:
         tune = eng.autotune(steps=3)  # set-up, outside the timed region; the state is restored
@@ -512,6 +529,10 @@ def main():
     barrier(dist)
     tm = eng.read_timing()
     assert tm["steps"] == args.steps
+    if collision is not None:
+        _, _, cinfo = eng.collision()
+        collision.update(candidate_pairs=cinfo["candidate_pairs"], vertices_hit=cinfo["vertices_hit"],
+                         detect_ms_last_step=cinfo["detect_ms"])
     t_local = tm["step_ms"] / 1e3
     # Kernel pass (not part of the value): the same steps with every
     # local-step launch bracketed by events inside the graph, for the
@@ -619,6 +640,7 @@ def main():
         "roofline": roofline,
         "kernels": kernels,
         "autotune": tune,
+        "collision": collision,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
                 "d2h_bytes_per_step": 2 * 3 * 4 * nv},
