@@ -1374,7 +1374,7 @@ int solve_launches(const pdgb_engine* e) {
     for (const SolveLevel& v : e->chol.step_levels)
         n += (v.fwdb_end > v.fwdb_begin) + (v.fwdw_end > v.fwdw_begin) + (v.bwdb_end > v.bwdb_begin) +
              (v.bwdw_end > v.bwdw_begin) + 2 * (v.tiny_end > v.tiny_begin) +
-             (PDGB_BWD_ZSTAGE && v.zst_end > v.zst_begin);
+             (v.zst_end > v.zst_begin);
     return n;
 }
 }  // namespace

@@ -407,7 +407,7 @@ bool partial_cholesky(double* F, int m, int k) {
 
 }  // namespace
 
-void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out) {
+void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out, int bwd_chunk_rows) {
     const int n = K.n;
     out = CholFactor();
     out.n = n;
@@ -687,11 +687,16 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
             }
             const int zoff = (int)out.zrows;
             out.zrows += m;
+            const int chunk = bwd_chunk_rows > 0 ? bwd_chunk_rows : m;
+            const int split = chunk < m ? 1 : 0;  // columns split into row chunks: x is accumulated
             for (int r0 = 0; r0 < m; r0 += kStageRows)
-                out.zstage.insert(out.zstage.end(), {lo, hi, out.roff[s], m, k, r0, 0, zoff});
-            for (int c0 = 0; c0 < k; c0 += kBwdBlockCols)
-                out.bwd_blocks.insert(out.bwd_blocks.end(),
-                                      {lo, hi, out.roff[s], m, k, c0, std::min(k, c0 + kBwdBlockCols), zoff});
+                out.zstage.insert(out.zstage.end(), {lo, hi, out.roff[s], m, k, r0, split, zoff});
+            for (int c0 = 0; c0 < k; c0 += kBwdBlockCols) {
+                const int cpack = c0 | ((std::min(k, c0 + kBwdBlockCols) - c0) << kBwdColShift);
+                for (int r0 = c0 - c0 % chunk; r0 < m; r0 += chunk)  // rows >= c0 only
+                    out.bwd_blocks.insert(out.bwd_blocks.end(),
+                                          {lo, hi, out.roff[s], m, r0, cpack, std::min(m, r0 + chunk), zoff});
+            }
         }
         lv.fwd_end = (int)(out.fwd_items.size() / kItemInts);
         lv.bwd_end = (int)(out.bwd_items.size() / kItemInts);
@@ -727,7 +732,7 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
             for (size_t i = 0; i < lt.size(); ++i) lt[i] = tets4[4 * (size_t)t0 + i] - (uint32_t)v0;
             std::vector<double> md(mdt2.begin() + v0, mdt2.begin() + v0 + nvb);
             SparseSym Kb = assemble_system(nvb, ntb, lt.data(), dminv + 9 * (size_t)t0, coef + t0, md);
-            cholesky_factor(Kb, ordering, xyz ? xyz + 3 * (size_t)v0 : nullptr, fs[b]);
+            cholesky_factor(Kb, ordering, xyz ? xyz + 3 * (size_t)v0 : nullptr, fs[b], 0);
         } catch (const Error& e) {
             failed[b] = e.status;
         } catch (...) {

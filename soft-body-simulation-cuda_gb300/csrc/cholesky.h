@@ -62,10 +62,14 @@ constexpr int kFwdItemCols = 64;
 // CTA block items (same 8-int layout) of the per-level launches:
 //   forward : {moff_lo, moff_hi, roff, m, k, r0, c0, c1}: rows r0 .. r0+128,
 //             pivot columns c0 .. c1 (at most 256, staged in shared memory)
-//   backward: {moff_lo, moff_hi, roff, m, k, c0, c1, zoff}: pivot columns
-//             c0 .. c1 against z = [y_pivots ; -x_offdiag] of the supernode,
-//             staged once per level at zbuf[zoff ..] by z-staging items
-//             {moff_lo, moff_hi, roff, m, k, r0, 0, zoff} of kStageRows rows
+//   backward: {moff_lo, moff_hi, roff, m, r0, c0 | (c1 - c0) << 27, r1,
+//             zoff}: pivot columns c0 .. c1 against rows r0 .. r1 of
+//             z = [y_pivots ; -x_offdiag] of the supernode, staged once per
+//             level at zbuf[zoff ..] by z-staging items
+//             {moff_lo, moff_hi, roff, m, k, r0, split, zoff} of kStageRows
+//             rows; when split != 0 the columns are split into row chunks
+//             that add their partial sums into x, and staging clears x at
+//             the pivot rows first
 // Supernodes with at least kBlockMinRows rows use block items in the
 // per-level launches; smaller ones keep warp items (packed 4 per CTA).
 #ifndef PDGB_FWDB_COLS
@@ -74,11 +78,15 @@ constexpr int kFwdItemCols = 64;
 #ifndef PDGB_BWD_WARP_COLS
 #define PDGB_BWD_WARP_COLS 2
 #endif
-// Backward blocks read z from the per-level staging buffer (1) or gather it
-// themselves, once per warp for all of the warp's columns (0).
-#ifndef PDGB_BWD_ZSTAGE
-#define PDGB_BWD_ZSTAGE 1
+// Rows of one backward block item of a single-body factor: a column's rows
+// are split into chunks so that no warp walks a long column alone.  (A
+// batch's levels hold many bodies' supernodes, enough parallelism without
+// the split, which would only add items and atomics: there a column is one
+// item.)
+#ifndef PDGB_BWD_CHUNK_ROWS
+#define PDGB_BWD_CHUNK_ROWS 256
 #endif
+constexpr int kBwdColShift = 27;  // backward block: c1 - c0 above c0 in one int
 #ifndef PDGB_BLOCK_MIN_ROWS
 #define PDGB_BLOCK_MIN_ROWS 64
 #endif
@@ -98,6 +106,7 @@ constexpr int kFwdBlockCols = PDGB_FWDB_COLS;
 constexpr int kBwdWarpCols = PDGB_BWD_WARP_COLS;   // backward block: columns per warp (4 warps)
 constexpr int kBwdBlockCols = 4 * kBwdWarpCols;
 constexpr int kStageRows = 128;
+constexpr int kBwdChunkRows = PDGB_BWD_CHUNK_ROWS;
 constexpr int kBlockMinRows = PDGB_BLOCK_MIN_ROWS;
 
 struct CholFactor {
@@ -138,7 +147,9 @@ struct CholFactor {
 // Factors K (vertex-indexed, n x n SPD).  ordering: 0 = AMD, 1 = nested
 // dissection (xyz required).  Throws Error(PDGB_ERR_NOT_SPD) if a pivot is
 // not positive.
-void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out);
+// bwd_chunk_rows: rows per backward block item (0: whole columns).
+void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out,
+                     int bwd_chunk_rows = kBwdChunkRows);
 
 // Factors the block-diagonal system of independent bodies, one block per
 // body (vertex range vstart[b]..vstart[b+1], tets tstart[b]..tstart[b+1] in

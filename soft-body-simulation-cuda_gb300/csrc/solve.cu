@@ -146,18 +146,23 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
 // Backward z staging {roff, m, k, r0, zoff}: z = [y_pivots ; -x_offdiag]
 // over rows r0 .. r0 + kStageRows of the supernode, gathered once per level
 // into zbuf[zoff ..] so that the backward blocks of all its column groups
-// read it contiguously.
+// read it contiguously.  For a supernode whose columns are split into row
+// chunks, x at the pivot rows is cleared here: the backward blocks of the
+// level add their chunk sums into it.
 __global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, int item0) {
     if (a.done && *a.done) return;
     const int* w = a.zstage + (size_t)kItemInts * (item0 + blockIdx.x);
-    const int roff = __ldg(w + 2), m = __ldg(w + 3), k = __ldg(w + 4), r0 = __ldg(w + 5), zoff = __ldg(w + 7);
+    const int roff = __ldg(w + 2), m = __ldg(w + 3), k = __ldg(w + 4), r0 = __ldg(w + 5), split = __ldg(w + 6),
+              zoff = __ldg(w + 7);
     const int* rows = a.rows + roff;
     const int r1 = min(m, r0 + kStageRows);
     for (int i = r0 + threadIdx.x; i < r1; i += kStageThreads) {
         const int vid = __ldg(&rows[i]);
         float4 z;
-        if (i < k) z = a.y[vid];
-        else {
+        if (i < k) {
+            z = a.y[vid];
+            if (split) a.x[vid] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
             const float4 xv = a.x[vid];
             z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
         }
@@ -165,42 +170,34 @@ __global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, i
     }
 }
 
-// Backward block {moff, roff, m, k, c0, c1, zoff}: warp w owns the
-// kBwdWarpCols consecutive columns c0 + kBwdWarpCols w ..; lanes stride the
-// rows, each z (staged, contiguous) is loaded once and used for all of the
-// warp's columns (contiguous loads of M_s, one per column), then a warp
-// reduction per column.  Column c uses rows i >= c only.
+// Backward block {moff, roff, m, r0, c0 | ncols, r1, zoff}: warp w owns the
+// kBwdWarpCols consecutive columns c0 + kBwdWarpCols w .. over the rows
+// r0 .. r1; lanes stride the rows, each z (staged,
+// contiguous) is loaded once and used for all of the warp's columns
+// (contiguous loads of M_s, one per column), then a warp reduction per
+// column whose sum is added into x.  Column c uses rows i >= c only.
 __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
     if (a.done && *a.done) return;
     const int* w = a.bwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
-    const int roff = h0.z, m = h0.w, c0 = h1.y, c1 = h1.z, zoff = h1.w;
+    const int roff = h0.z, m = h0.w, r0 = h1.x, c0 = h1.y & ((1 << kBwdColShift) - 1),
+              c1 = c0 + (h1.y >> kBwdColShift), rend = h1.z, zoff = h1.w;
     const int* rows = a.rows + roff;
     const float4* z = a.zbuf + zoff;
-    (void)z;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cw = c0 + kBwdWarpCols * warp;  // first column of this warp
     if (cw >= c1) return;
     const int nc = min(kBwdWarpCols, c1 - cw);
+    if (cw >= rend) return;
     const float* Mc = a.mval + moff + (size_t)cw * m;
     float acc[kBwdWarpCols][3];
 #pragma unroll
     for (int j = 0; j < kBwdWarpCols; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
 #pragma unroll 2
-    for (int i = cw + lane; i < m; i += 32) {
-#if PDGB_BWD_ZSTAGE
+    for (int i = max(cw, r0) + lane; i < rend; i += 32) {
         const float4 zz = z[i];
-#else
-        const int vid = __ldg(&rows[i]);
-        float4 zz;
-        if (i < h1.x) zz = a.y[vid];
-        else {
-            const float4 xv = a.x[vid];
-            zz = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
-        }
-#endif
 #pragma unroll
         for (int j = 0; j < kBwdWarpCols; ++j) {
             if (j < nc && i >= cw + j) {
@@ -219,7 +216,12 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
             acc[j][1] += __shfl_xor_sync(0xffffffffu, acc[j][1], off);
             acc[j][2] += __shfl_xor_sync(0xffffffffu, acc[j][2], off);
         }
-        if (lane == 0 && j < nc) a.x[__ldg(&rows[cw + j])] = make_float4(acc[j][0], acc[j][1], acc[j][2], 0.f);
+        if (lane == 0 && j < nc) {
+            float4* xc = &a.x[__ldg(&rows[cw + j])];
+            const float4 sum = make_float4(acc[j][0], acc[j][1], acc[j][2], 0.f);
+            if (r0 == 0 && rend == m) *xc = sum;  // the whole column in one item
+            else atomicAdd(xc, sum);
+        }
     }
 }
 
@@ -326,7 +328,7 @@ void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& 
     for (size_t L = levels.size(); L-- > 0;) {
         const SolveLevel& v = levels[L];
         const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin, nt = v.tiny_end - v.tiny_begin;
-        const int nz = PDGB_BWD_ZSTAGE ? v.zst_end - v.zst_begin : 0;
+        const int nz = v.zst_end - v.zst_begin;
         if (nz > 0) k_chol_bwd_zstage<<<nz, kStageThreads, 0, s>>>(a, v.zst_begin);
         if (nb > 0) k_chol_bwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.bwdb_begin);
         if (nw > 0) k_chol_bwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.bwdw_begin, nw);
