@@ -24,10 +24,10 @@ namespace pdgb {
 // residual form) and the corner contributions c R DmInv^T G, and writes each
 // to its slot: run start of k + rank r.  The slots of a tile are ordered by
 // patch vertex, so patch vertex k owns the contiguous slots inc_end[k-1] ..
-// inc_end[k].  (3) Every patch vertex sums its run of slots in order and adds
-// the sum to b with one float4 atomic (pinned vertices are skipped: their RHS
-// is the pin term).  No shared-memory atomics; within a tile the sums are
-// deterministic.
+// inc_end[k].  (3) Every patch vertex sums its run of slots (a fixed
+// rotation of it, see below) and adds the sum to b with one float4 atomic
+// (pinned vertices are skipped: their RHS is the pin term).  No shared-memory
+// atomics; within a tile the sums are deterministic.
 template <bool kJacobiForm, int kRotation>
 __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4* slot, float4* pos) {
     const int vb = a.tile_vptr[tile];
@@ -124,12 +124,20 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         if (v & kPinnedBit) continue;
         const int e0 = first ? e0_first : __ldg(&iend[k - 1]);
         const int e1 = first ? e1_first : __ldg(&iend[k]);
+        // The run is summed from a lane-dependent start (then wrapping), so
+        // that the 8 lanes of a quarter-warp read 8 different 16-byte bank
+        // groups while their runs last, instead of colliding at random.
         float sx = 0.f, sy = 0.f, sz = 0.f;
-        for (int e = e0; e < e1; ++e) {
+        const int len = e1 - e0;
+        int off = (k - e0) & 7;
+        if (off >= len) off = 0;
+        int e = e0 + off;
+        for (int j = 0; j < len; ++j) {
             const float4 q = slot[e];
             sx += q.x;
             sy += q.y;
             sz += q.z;
+            if (++e == e1) e = e0;
         }
         atomicAdd(&a.b[v], make_float4(sx, sy, sz, 0.f));
     }
