@@ -581,6 +581,10 @@ def main():
     eng_info["solve_mode"] = eng.solve_mode() if params.solver == 1 else 0
     eng_info["solve_launches"] = eng.factor_info()["solve_launches"] if params.solver == 1 else 0
     solve_bytes = eng.solve_bytes()
+    # the local step alone, back to back (CUDA events around 200 launches on
+    # the engine's stream, after the timed region): no event nodes between
+    # launches inflate it, unlike the in-graph pairs above
+    local_b2b_ms = min(eng.time_local(200) for _ in range(3))
     eng.close()
 
     if rank != 0:
@@ -595,7 +599,10 @@ def main():
                   "kernel": "k_local<jacobi_form=%d>" % (1 if params.solver == 0 else 0),
                   "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_local_s * 1e6,
                   "launches": local_launches,
-                  "share_of_step": (local_ms / step_ms_kernel_pass) if step_ms_kernel_pass > 0 else None}
+                  "share_of_step": (local_ms / step_ms_kernel_pass) if step_ms_kernel_pass > 0 else None,
+                  "back_to_back": {"avg_launch_us": local_b2b_ms * 1e3,
+                                   "achieved": bytes_per_launch / (local_b2b_ms / 1e3) / 1e9,
+                                   "frac": bytes_per_launch / (local_b2b_ms / 1e3) / 1e9 / peak}}
     roofline, kernels = local_roof, {"local": local_roof}
     if params.solver == 1 and solves > 0 and solve_bytes > 0:
         avg_solve_s = (solve_ms / 1e3) / solves
