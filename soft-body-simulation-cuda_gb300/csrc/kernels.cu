@@ -35,8 +35,9 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
     const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
     const int ntile = t1 - t0;
     const uint16_t* iend = a.inc_end + vb;
-    // Issue the per-tet geometry and corner-record loads of this thread's
-    // tets first: they are in flight while the patch positions are gathered.
+    // The first tet's geometry and corner records are issued before the
+    // patch positions are gathered (in flight meanwhile); the second tet's
+    // after the barrier, so that phase 1 holds one tet's registers, not two.
     constexpr int kPer = kTileTets / kLocalThreads;
     constexpr uint32_t kPatchMask = (1u << kPatchBits) - 1u;
     const int ntp = a.nt_pad;
@@ -45,14 +46,13 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
     float4 GA[kPer], GB[kPer];
     float2 GC[kPer];
     uint2 S[kPer];
-#pragma unroll
-    for (int j = 0; j < kPer; ++j) {
-        const int lt = threadIdx.x + j * kLocalThreads;
+    {
+        const int lt = threadIdx.x;
         const int t = t0 + (lt < ntile ? lt : 0);
-        GA[j] = __ldg(geo0 + t);
-        GB[j] = __ldg(geo0 + ntp + t);
-        GC[j] = __ldg(geo2 + t);
-        S[j] = __ldg(reinterpret_cast<const uint2*>(a.inc_ent) + t);
+        GA[0] = __ldg(geo0 + t);
+        GB[0] = __ldg(geo0 + ntp + t);
+        GC[0] = __ldg(geo2 + t);
+        S[0] = __ldg(reinterpret_cast<const uint2*>(a.inc_ent) + t);
     }
     if (a.done && *a.done) return;
     // the first patch vertex of each thread keeps its id and slot run in
@@ -71,6 +71,15 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         }
     }
     __syncthreads();
+#pragma unroll
+    for (int j = 1; j < kPer; ++j) {
+        const int lt = threadIdx.x + j * kLocalThreads;
+        const int t = t0 + (lt < ntile ? lt : 0);
+        GA[j] = __ldg(geo0 + t);
+        GB[j] = __ldg(geo0 + ntp + t);
+        GC[j] = __ldg(geo2 + t);
+        S[j] = __ldg(reinterpret_cast<const uint2*>(a.inc_ent) + t);
+    }
 #pragma unroll
     for (int j = 0; j < kPer; ++j) {
         const int lt = threadIdx.x + j * kLocalThreads;
