@@ -609,7 +609,7 @@ def main():
         s_ach = solve_bytes / avg_solve_s / 1e9
         solve_roof = {"bound": "hbm", "achieved": s_ach, "peak": peak, "unit": "GB/s", "frac": s_ach / peak,
                       "traffic": None, "peak_kind": peak_kind,
-                      "kernel": {1: "k_chol_solve_cta", 2: "k_chol_solve_cluster",
+                      "kernel": {1: "k_chol_solve_cta", 2: "k_chol_solve_cluster", 4: "k_chol_solve_dsm",
                                  3: "k_chol_fwd_level + k_chol_bwd_level"}.get(eng_info.get("solve_mode"), "solve"),
                       "bytes_per_launch": solve_bytes, "avg_launch_us": avg_solve_s * 1e6, "launches": solves,
                       "share_of_step": solve_ms / step_ms_kernel_pass if step_ms_kernel_pass > 0 else None,

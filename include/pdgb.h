@@ -284,15 +284,22 @@ int pdgb_set_rotation(pdgb_engine* e, int rotation);
  * whole elimination tree (levels separated by block barriers); CLUSTER: one
  * cluster of 8 CTAs per body (cluster barriers); LEVELS: one launch per
  * level and direction over the whole GPU, level L of every body of a batch
- * in the same launch (levels counted from the leaves).  AUTO picks by
- * size: a batch uses CTA, a single system CLUSTER up to 2^20 stored factor
- * entries and LEVELS above; pdgb_autotune times all three.  Takes effect at
- * the next prepare; pdgb_get_solve_mode returns the schedule in use (AUTO
- * before the first prepare or on the Jacobi path). */
+ * in the same launch (levels counted from the leaves); DSM: a single body
+ * whose factor fits the shared memory of an 8-CTA cluster is solved by that
+ * cluster with the factor blocks, row lists and vectors on chip
+ * (distributed shared memory between the CTAs; PDGB_ERR_UNSUPPORTED at
+ * prepare when it does not fit; on request only: with whole supernodes
+ * per CTA and remote float atomics it measures slower than CLUSTER on the
+ * bodies that fit).  AUTO picks by size: a batch uses CTA, a single system
+ * CLUSTER up to 2^20 stored factor entries and LEVELS above;
+ * pdgb_autotune times CTA, CLUSTER and LEVELS.  Takes
+ * effect at the next prepare; pdgb_get_solve_mode returns the schedule in
+ * use (AUTO before the first prepare or on the Jacobi path). */
 #define PDGB_SOLVE_AUTO 0
 #define PDGB_SOLVE_CTA 1
 #define PDGB_SOLVE_CLUSTER 2
 #define PDGB_SOLVE_LEVELS 3
+#define PDGB_SOLVE_DSM 4
 int pdgb_set_solve_mode(pdgb_engine* e, int mode);
 int pdgb_get_solve_mode(pdgb_engine* e, int* mode);
 

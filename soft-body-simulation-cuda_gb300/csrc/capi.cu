@@ -62,6 +62,10 @@ struct pdgb_engine {
         ch_zstage;
     DBuf<float4> ch_zbuf;
     DBuf<int4> ch_levels;
+    // distributed-shared-memory solve of a single body (when it fits)
+    DsmPlan dsm;
+    DBuf<float> dsm_mcopy;
+    DBuf<int> dsm_mcopy_ptr, dsm_rcopy, dsm_rcopy_ptr, dsm_items, dsm_lvl;
     DBuf<float> ch_mval;
     DBuf<int> k_rowptr, k_colind;  // FP64 K for refinement residuals
     DBuf<double> k_val;
@@ -217,6 +221,22 @@ BeginArgs begin_args(pdgb_engine* e) {
     return ba;
 }
 
+DsmArgs dsm_args(const pdgb_engine* e) {
+    DsmArgs d{};
+    d.mcopy = e->dsm_mcopy.p;
+    d.mcopy_ptr = e->dsm_mcopy_ptr.p;
+    d.rcopy = e->dsm_rcopy.p;
+    d.rcopy_ptr = e->dsm_rcopy_ptr.p;
+    d.items = e->dsm_items.p;
+    d.lvl = reinterpret_cast<const int4*>(e->dsm_lvl.p);
+    d.nlevels = e->dsm.nlevels;
+    d.n = e->dsm.n;
+    d.slots = e->dsm.slots;
+    d.m_area = e->dsm.m_area;
+    d.r_area = e->dsm.r_area;
+    return d;
+}
+
 void record_local(pdgb_engine* e, const LocalArgs& la, bool jacobi_form, int i) {
     cudaStream_t s = e->stream;
     if (e->timing) PDGB_CUDA_TRY(cudaEventRecordWithFlags(e->events[2 * i], s, cudaEventRecordExternal));
@@ -284,6 +304,7 @@ void record_chol_step(pdgb_engine* e) {
     auto solve = [&](const CholArgs& args) {
         if (e->solve_mode == PDGB_SOLVE_CTA) launch_chol_solve_cta(args, e->nbodies, s);
         else if (e->solve_mode == PDGB_SOLVE_CLUSTER) launch_chol_solve_cluster(args, e->nbodies, s);
+        else if (e->solve_mode == PDGB_SOLVE_DSM) launch_chol_solve_dsm(args, dsm_args(e), e->dsm.smem_bytes, s);
         else launch_chol_solve_levels(args, e->chol.step_levels, s);
     };
     for (int i = 0; i < n; ++i) {
@@ -372,6 +393,8 @@ SparseSym engine_system(const HostLayout& L) {
 int choose_solve_mode(const pdgb_engine* e) {
     const bool small = e->chol.mval.size() <= kCtaSolveMaxEntries;
     const int m = e->solve_req;
+    if (m == PDGB_SOLVE_DSM && !e->dsm.ok)
+        throw Error{PDGB_ERR_UNSUPPORTED, "the factor does not fit the shared memory of one cluster (DSM solve)"};
     if (m != PDGB_SOLVE_AUTO) return m;
     if (e->nbodies > 1) return PDGB_SOLVE_CTA;
     return small ? PDGB_SOLVE_CLUSTER : PDGB_SOLVE_LEVELS;
@@ -428,6 +451,21 @@ void prepare_cholesky(pdgb_engine* e) {
     }
     e->ch_body_level.upload(f.body_level, s);
     e->ch_body_order.upload(f.body_order, s);
+    e->dsm = DsmPlan{};
+    if (e->solve_req == PDGB_SOLVE_DSM) {
+        int dev = 0, optin = 0;
+        PDGB_CUDA_TRY(cudaGetDevice(&dev));
+        PDGB_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        build_dsm_plan(f, kClusterCtas, kClusterSolveThreads / 32, (size_t)optin, e->dsm);
+        if (e->dsm.ok) {
+            e->dsm_mcopy.upload(e->dsm.mcopy, s);
+            e->dsm_mcopy_ptr.upload(e->dsm.mcopy_ptr, s);
+            e->dsm_rcopy.upload(e->dsm.rcopy, s);
+            e->dsm_rcopy_ptr.upload(e->dsm.rcopy_ptr, s);
+            e->dsm_items.upload(e->dsm.items, s);
+            e->dsm_lvl.upload(e->dsm.lvl, s);
+        }
+    }
     // A single CTA walks a body's whole tree when the factor is small (the
     // solve is then bound by the tree depth, not by bandwidth, and launches
     // would dominate); batches of bodies always run one CTA per body.
@@ -841,7 +879,9 @@ int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
         copy_state(true);
         std::vector<int> caps = {kTileTets, kTileTets / 2, kTileTets / 4, kTileTets / 8};
         std::vector<int> modes = {e->solve_req};
-        if (e->prm.solver == PDGB_SOLVER_CHOLESKY) modes = {PDGB_SOLVE_CTA, PDGB_SOLVE_CLUSTER, PDGB_SOLVE_LEVELS};
+        if (e->prm.solver == PDGB_SOLVER_CHOLESKY) {
+            modes = {PDGB_SOLVE_CTA, PDGB_SOLVE_CLUSTER, PDGB_SOLVE_LEVELS};
+        }
         double best = t0;
         int best_cap = cap0, best_mode = req0, tried = 1;
         for (int cap : caps)
@@ -877,7 +917,7 @@ int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
 }
 
 int pdgb_set_solve_mode(pdgb_engine* e, int mode) {
-    if (!e || mode < PDGB_SOLVE_AUTO || mode > PDGB_SOLVE_LEVELS) {
+    if (!e || mode < PDGB_SOLVE_AUTO || mode > PDGB_SOLVE_DSM) {
         set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or solve mode");
         return PDGB_ERR_INVALID_ARGUMENT;
     }

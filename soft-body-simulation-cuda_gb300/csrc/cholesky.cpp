@@ -879,3 +879,88 @@ void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3) {
 }
 
 }  // namespace pdgb
+
+namespace pdgb {
+
+void build_dsm_plan(const CholFactor& f, int ctas, int warps_per_cta, size_t max_smem, DsmPlan& plan) {
+    plan = DsmPlan();
+    if (f.body_level.size() != 2 || f.nsuper == 0 || ctas < 1) return;  // single bodies only
+    const int ns = f.nsuper;
+    plan.ctas = ctas;
+    plan.n = f.n;
+    plan.slots = (f.n + ctas - 1) / ctas;
+    plan.nlevels = f.nlevels;
+    // supernodes to CTAs: largest M_s first, each to the least loaded CTA
+    std::vector<int> order(ns);
+    std::iota(order.begin(), order.end(), 0);
+    auto msize = [&](int s) { return (int64_t)f.sm[s] * f.sk[s]; };
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return msize(a) > msize(b); });
+    std::vector<int64_t> load(ctas, 0);
+    std::vector<int> owner(ns);
+    for (int s : order) {
+        const int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        owner[s] = c;
+        load[c] += msize(s) + f.sm[s];
+    }
+    // staged areas, per CTA: its supernodes' M_s blocks and row lists back to back
+    std::vector<std::vector<int>> mine(ctas);
+    for (int s = 0; s < ns; ++s) mine[owner[s]].push_back(s);
+    std::vector<int> moff_smem(ns), roff_smem(ns);
+    int max_m = 0, max_r = 0;
+    plan.mcopy_ptr.assign(1, 0);
+    plan.rcopy_ptr.assign(1, 0);
+    for (int c = 0; c < ctas; ++c) {
+        int mo = 0, ro = 0;
+        for (int s : mine[c]) {
+            moff_smem[s] = mo;
+            const int64_t cnt = (int64_t)f.sm[s] * f.sk[s];
+            plan.mcopy.insert(plan.mcopy.end(), f.mval.begin() + f.moff[s], f.mval.begin() + f.moff[s] + cnt);
+            mo += (int)cnt;
+            roff_smem[s] = ro;
+            plan.rcopy.insert(plan.rcopy.end(), f.rows.begin() + f.roff[s], f.rows.begin() + f.roff[s] + f.sm[s]);
+            ro += f.sm[s];
+        }
+        while (plan.mcopy.size() & 3) plan.mcopy.push_back(0.f);
+        while (plan.rcopy.size() & 3) plan.rcopy.push_back(0);
+        plan.mcopy_ptr.push_back((int)plan.mcopy.size());
+        plan.rcopy_ptr.push_back((int)plan.rcopy.size());
+        max_m = std::max(max_m, mo);
+        max_r = std::max(max_r, ro);
+    }
+    // shared memory: 3 vectors + warp staging (float4), M, rows
+    const int vec_f4 = 3 * plan.slots + warps_per_cta * 32;
+    plan.m_area = 4 * vec_f4;
+    plan.r_area = plan.m_area + ((max_m + 3) & ~3);
+    plan.smem_bytes = 4 * (size_t)plan.r_area + 4 * (size_t)((max_r + 3) & ~3);
+    if (plan.smem_bytes > max_smem) return;
+    // items per CTA and level
+    std::vector<std::vector<int>> bylevel(f.nlevels);
+    for (int s = 0; s < ns; ++s) bylevel[f.level[s]].push_back(s);
+    plan.lvl.assign((size_t)ctas * f.nlevels * 4, 0);
+    for (int c = 0; c < ctas; ++c)
+        for (int L = 0; L < f.nlevels; ++L) {
+            int* lv = &plan.lvl[((size_t)c * f.nlevels + L) * 4];
+            lv[0] = (int)(plan.items.size() / kItemInts);
+            for (int s : bylevel[L]) {
+                if (owner[s] != c) continue;
+                const int k = f.sk[s], m = f.sm[s];
+                for (int r0 = 0; r0 < m; r0 += kFwdItemRows) {
+                    const int cmax = std::min(k, r0 + kFwdItemRows);
+                    for (int c0 = 0; c0 < cmax; c0 += kFwdItemCols)
+                        plan.items.insert(plan.items.end(), {moff_smem[s], roff_smem[s], m, k, r0, c0,
+                                                             std::min(cmax, c0 + kFwdItemCols), 0});
+                }
+            }
+            lv[1] = (int)(plan.items.size() / kItemInts);
+            lv[2] = lv[1];
+            for (int s : bylevel[L]) {
+                if (owner[s] != c) continue;
+                for (int col = 0; col < f.sk[s]; ++col)
+                    plan.items.insert(plan.items.end(), {moff_smem[s], roff_smem[s], f.sm[s], f.sk[s], col, 0, 0, 0});
+            }
+            lv[3] = (int)(plan.items.size() / kItemInts);
+        }
+    plan.ok = true;
+}
+
+}  // namespace pdgb

@@ -144,10 +144,38 @@ struct CholFactor {
     SparseSym K;
 };
 
+// Plan of the distributed-shared-memory solve of a single body: an 8-CTA
+// cluster, each CTA owning a set of supernodes whose M_s blocks and row
+// lists it stages into its shared memory once per solve; the right-hand
+// side, y and x live in the cluster's shared memory, vertex v in CTA v % 8
+// at slot v / 8.  Items use the warp-item layout with shared-memory offsets:
+//   forward : {m_off, r_off, m, k, r0, c0, c1, 0}; backward: {m_off, r_off, m, k, c, 0, 0, 0}.
+struct DsmPlan {
+    bool ok = false;
+    int ctas = 0;                 // cluster size
+    int n = 0;                    // vertices
+    int slots = 0;                // vector slots per CTA (ceil(n / ctas))
+    int nlevels = 0;
+    int m_area = 0;               // float index of the staged M area in shared memory
+    int r_area = 0;               // int index of the staged row area
+    size_t smem_bytes = 0;        // dynamic shared memory per CTA
+    // Each CTA's staged areas, laid out as in its shared memory and stored
+    // contiguously per CTA, so that staging is one wide copy per CTA.
+    std::vector<float> mcopy;     // M_s blocks of CTA c at [mcopy_ptr[c], mcopy_ptr[c+1])
+    std::vector<int> mcopy_ptr;   // [ctas + 1], multiples of 4
+    std::vector<int> rcopy;       // row lists of CTA c at [rcopy_ptr[c], rcopy_ptr[c+1])
+    std::vector<int> rcopy_ptr;   // [ctas + 1], multiples of 4
+    std::vector<int> items;       // kItemInts per item, each CTA's items grouped by level
+    std::vector<int> lvl;         // [ctas][nlevels] x {fwd_begin, fwd_end, bwd_begin, bwd_end}
+};
+// Fills the plan for a single-body factor when the busiest CTA's share fits
+// max_smem bytes of shared memory; plan.ok tells whether it does.
+void build_dsm_plan(const CholFactor& f, int ctas, int warps_per_cta, size_t max_smem, DsmPlan& plan);
+
 // Factors K (vertex-indexed, n x n SPD).  ordering: 0 = AMD, 1 = nested
 // dissection (xyz required).  Throws Error(PDGB_ERR_NOT_SPD) if a pivot is
-// not positive.
-// bwd_chunk_rows: rows per backward block item (0: whole columns).
+// not positive.  bwd_chunk_rows: rows per backward block item (0: whole
+// columns).
 void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out,
                      int bwd_chunk_rows = kBwdChunkRows);
 

@@ -401,6 +401,143 @@ void launch_chol_solve_cluster(const CholArgs& a, int nbodies, cudaStream_t s) {
     if (nbodies > 0) k_chol_solve_cluster<<<nbodies * kClusterCtas, kClusterSolveThreads, 0, s>>>(a);
 }
 
+// ---- one body per cluster, everything in the cluster's shared memory.
+// Each CTA stages the M_s blocks and row lists of its supernodes (stored
+// back to back per CTA by the plan: one float4-wide copy each), and
+// holds the vector slots of vertices v with v % 8 == its rank.  The level
+// loops run the warp items of the CTA's supernodes; right-hand side, y and x
+// are read and updated in whichever CTA holds the vertex (distributed shared
+// memory, float atomics for the forward updates); a cluster barrier
+// separates levels.  Nothing but the staging and the final x touches global
+// memory.
+namespace {
+namespace cg = cooperative_groups;
+
+__device__ __forceinline__ float4* dsm_slot(cg::cluster_group& cl, float4* local, int v) {
+    return cl.map_shared_rank(local + (v >> 3), (unsigned)(v & (kClusterCtas - 1)));
+}
+
+__device__ __forceinline__ void dsm_add(float4* p, float x, float y, float z) {
+    atomicAdd(&p->x, x);
+    atomicAdd(&p->y, y);
+    atomicAdd(&p->z, z);
+}
+
+// cnt4 16-byte words from global to shared memory, the whole CTA at once
+__device__ __forceinline__ void dsm_copy16(void* dst, const void* src, int cnt4) {
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    for (int t = threadIdx.x; t < cnt4; t += blockDim.x) d4[t] = __ldg(s4 + t);
+}
+}  // namespace
+
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterSolveThreads)
+    k_chol_solve_dsm(CholArgs a, DsmArgs d) {
+    extern __shared__ float4 dsm_base[];
+    if (a.done && *a.done) return;  // the flag is fixed for the kernel: uniform over the cluster
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int kWarps = kClusterSolveThreads / 32;
+    const int S = d.slots;
+    float4* vr = dsm_base;
+    float4* vy = vr + S;
+    float4* vx = vy + S;
+    float4* stage = vx + S + warp * 32;
+    float* Ms = reinterpret_cast<float*>(dsm_base) + d.m_area;
+    int* Rs = reinterpret_cast<int*>(dsm_base) + d.r_area;
+    const int m0 = d.mcopy_ptr[rank], r0c = d.rcopy_ptr[rank];
+    dsm_copy16(Ms, d.mcopy + m0, (d.mcopy_ptr[rank + 1] - m0) >> 2);
+    dsm_copy16(Rs, d.rcopy + r0c, (d.rcopy_ptr[rank + 1] - r0c) >> 2);
+    for (int j = threadIdx.x; j < S; j += blockDim.x) {
+        const int v = j * kClusterCtas + rank;
+        vr[j] = v < d.n ? a.r[v] : make_float4(0.f, 0.f, 0.f, 0.f);
+        vy[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        vx[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    cl.sync();
+    // forward: y_s = L_ss^-1 r_s (pivot rows), r_O -= L_os L_ss^-1 r_s
+    for (int L = 0; L < d.nlevels; ++L) {
+        const int4 lv = d.lvl[rank * d.nlevels + L];
+        for (int it = lv.x + warp; it < lv.y; it += kWarps) {
+            const int* w = d.items + (size_t)kItemInts * it;
+            const int moff = w[0], m = w[2], k = w[3], r0 = w[4], c0 = w[5], c1 = w[6];
+            const int* rows = Rs + w[1];
+            const int row = r0 + lane;
+            const bool valid = row < m;
+            const int cend = !valid ? c0 : (row < k ? min(c1, row + 1) : c1);
+            const float* Mr = Ms + moff + row;
+            float ax = 0.f, ay = 0.f, az = 0.f;
+            for (int cb = c0; cb < c1; cb += 32) {
+                const int nc = min(32, c1 - cb);
+                __syncwarp();
+                if (lane < nc) stage[lane] = *dsm_slot(cl, vr, rows[cb + lane]);
+                __syncwarp();
+                for (int c = cb; c < cb + nc; ++c) {
+                    const float mv = c < cend ? Mr[(size_t)c * m] : 0.f;
+                    const float4 v = stage[c - cb];
+                    ax = fmaf(mv, v.x, ax);
+                    ay = fmaf(mv, v.y, ay);
+                    az = fmaf(mv, v.z, az);
+                }
+            }
+            if (valid) {
+                const int vid = rows[row];
+                if (row < k) dsm_add(dsm_slot(cl, vy, vid), ax, ay, az);
+                else dsm_add(dsm_slot(cl, vr, vid), -ax, -ay, -az);
+            }
+        }
+        cl.sync();
+    }
+    // backward: x_s = sum_{i >= c} M_s[i, c] z_i, z = [y_pivots ; -x_offdiag]
+    for (int L = d.nlevels - 1; L >= 0; --L) {
+        const int4 lv = d.lvl[rank * d.nlevels + L];
+        for (int it = lv.z + warp; it < lv.w; it += kWarps) {
+            const int* w = d.items + (size_t)kItemInts * it;
+            const int moff = w[0], m = w[2], k = w[3], c = w[4];
+            const int* rows = Rs + w[1];
+            const float* Mc = Ms + moff + (size_t)c * m;
+            float ax = 0.f, ay = 0.f, az = 0.f;
+            for (int i = c + lane; i < m; i += 32) {
+                const int vid = rows[i];
+                const float mv = Mc[i];
+                float4 z;
+                if (i < k) {
+                    z = *dsm_slot(cl, vy, vid);
+                } else {
+                    const float4 xv = *dsm_slot(cl, vx, vid);
+                    z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+                }
+                ax = fmaf(mv, z.x, ax);
+                ay = fmaf(mv, z.y, ay);
+                az = fmaf(mv, z.z, az);
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                ax += __shfl_xor_sync(0xffffffffu, ax, off);
+                ay += __shfl_xor_sync(0xffffffffu, ay, off);
+                az += __shfl_xor_sync(0xffffffffu, az, off);
+            }
+            if (lane == 0) *dsm_slot(cl, vx, rows[c]) = make_float4(ax, ay, az, 0.f);
+        }
+        cl.sync();
+    }
+    for (int j = threadIdx.x; j < S; j += blockDim.x) {
+        const int v = j * kClusterCtas + rank;
+        if (v < d.n) a.x[v] = vx[j];
+    }
+}
+
+void launch_chol_solve_dsm(const CholArgs& a, const DsmArgs& d, size_t smem_bytes, cudaStream_t s) {
+    static size_t allowed = 0;
+    if (smem_bytes > allowed) {
+        PDGB_CUDA_TRY(cudaFuncSetAttribute(k_chol_solve_dsm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem_bytes));
+        allowed = smem_bytes;
+    }
+    k_chol_solve_dsm<<<kClusterCtas, kClusterSolveThreads, smem_bytes, s>>>(a, d);
+}
+
 // Cholesky-path vertex kernel after each solve (new positions in sn, written
 // by the backward pass): resets b for the next local step (pinned vertices
 // get the pin RHS: computeDBCLocal overwrites b, pdUtil.cu:153-158), clears

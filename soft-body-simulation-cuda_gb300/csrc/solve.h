@@ -74,6 +74,24 @@ void launch_chol_solve_cta(const CholArgs& a, int nbodies, cudaStream_t s);
 // The whole solve of one body in one thread-block cluster of kClusterCtas
 // CTAs, levels separated by cluster barriers; one cluster per body.
 void launch_chol_solve_cluster(const CholArgs& a, int nbodies, cudaStream_t s);
+
+// Distributed-shared-memory solve of one body (DsmPlan): one 8-CTA cluster;
+// factor blocks, row lists and the three vectors stay on chip, levels are
+// separated by cluster barriers.
+struct DsmArgs {
+    const float* mcopy;    // each CTA's M_s blocks, as laid out in its shared memory
+    const int* mcopy_ptr;  // [kClusterCtas + 1], multiples of 4
+    const int* rcopy;      // each CTA's row lists
+    const int* rcopy_ptr;
+    const int* items;      // kItemInts per item
+    const int4* lvl;       // [kClusterCtas][nlevels]
+    int nlevels;
+    int n;
+    int slots;
+    int m_area;            // float index of the staged M area
+    int r_area;            // int index of the staged row area
+};
+void launch_chol_solve_dsm(const CholArgs& a, const DsmArgs& d, size_t smem_bytes, cudaStream_t s);
 // FP64-residual iterative refinement of the global solve:
 //   bsave = b (before the solve destroys it);
 //   r = bsave - K x0 in double (K: FP64 CSR over vertex ids), b = r, y = 0;

@@ -36,6 +36,7 @@ PDGB_SOLVE_AUTO = 0
 PDGB_SOLVE_CTA = 1
 PDGB_SOLVE_CLUSTER = 2
 PDGB_SOLVE_LEVELS = 3
+PDGB_SOLVE_DSM = 4
 PDGB_TIMING_OFF = 0
 PDGB_TIMING_STEPS = 1
 PDGB_TIMING_KERNELS = 2

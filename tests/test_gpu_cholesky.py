@@ -10,7 +10,7 @@ import pytest
 from conftest import GOLDEN_CASES, load_golden, rel_l2
 
 import oracle as O
-from pdgb import PdSolver, SolverParams, mesh
+from pdgb import PdgbError, PdSolver, SolverParams, mesh
 from pdgb import _native as N
 
 pytestmark = pytest.mark.gpu
@@ -129,11 +129,12 @@ def test_solve_timing_and_bytes():
     assert rel_l2(X, Xo) < TOL
 
 
-@pytest.mark.parametrize("mode", [N.PDGB_SOLVE_CTA, N.PDGB_SOLVE_CLUSTER, N.PDGB_SOLVE_LEVELS])
+@pytest.mark.parametrize("mode", [N.PDGB_SOLVE_CTA, N.PDGB_SOLVE_CLUSTER, N.PDGB_SOLVE_LEVELS, N.PDGB_SOLVE_DSM])
 def test_solve_schedules_agree(mode):
-    """The three schedules of the same factor (one CTA, one cluster, one
-    launch per level) give the FP64 oracle's positions; tol > 0 keeps the
-    early exit working in each."""
+    """The four schedules of the same factor (one CTA, one cluster, one
+    launch per level, one cluster with everything in distributed shared
+    memory) give the FP64 oracle's positions; tol > 0 keeps the early exit
+    working in each."""
     body = mesh.make_grid_body(9, 8, 7, jitter=0.1, seed=13, young=3e4)
     params = SolverParams(num_iterations=10, tol=1e-4, solver=1)
     with PdSolver(body, params) as e:
@@ -147,3 +148,27 @@ def test_solve_schedules_agree(mode):
     Xo, _, ito = O.simulate(body, params, 6, precision=64)
     assert rel_l2(X, Xo) < TOL
     assert np.abs(np.asarray(its) - ito).max() <= 1
+
+
+
+def test_dsm_solve_matches_cluster_and_refines():
+    """The on-chip solve of the 10^3 cube (the C1 system) against the
+    cluster schedule, with FP64-residual refinement steps in both."""
+    body = mesh.cube_c1()
+    out = {}
+    for mode in (N.PDGB_SOLVE_CLUSTER, N.PDGB_SOLVE_DSM):
+        params = SolverParams(num_iterations=10, solver=1, refine_steps=1)
+        with PdSolver(body, params) as e:
+            e.set_solve_mode(mode)
+            e.update(5)
+            assert e.solve_mode() == mode
+            out[mode] = e.download_state()[0]
+    assert rel_l2(out[N.PDGB_SOLVE_DSM], out[N.PDGB_SOLVE_CLUSTER]) < 1e-6
+
+
+def test_dsm_solve_refuses_a_factor_too_large():
+    body = mesh.make_grid_body(30, 30, 30)
+    with PdSolver(body, SolverParams(num_iterations=2, solver=1)) as e:
+        e.set_solve_mode(N.PDGB_SOLVE_DSM)
+        with pytest.raises(PdgbError):
+            e.update(1)
