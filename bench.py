@@ -40,7 +40,9 @@ WORKLOADS = {
         "workload": "pd_jacobi_cube64",
         "desc": "64^3 hex grid x5 tets (274625 v / 1310720 t), jitter 0.1 cell seed 2024, E=1e6 nu=0.45 rho=1000, "
                 "top face pinned, dt=1/120, Jacobi+Chebyshev rho=0.9995, 20 iterations/step",
-        "grid": 64, "iterations": 20, "rho": 0.9995, "solver": "jacobi",
+        "grid": 64, "iterations": 20, "rho": 0.9995, "solver": "jacobi", "episode_steps": 50,
+        "state": "50-step runs from rest, repeated: the rest state is restored on the device between runs, "
+                 "outside the step events (past ~25 steps this iteration diverges, in FP64 as in FP32)",
     },
     "c1": {
         "workload": "pd_cholesky_cube10",
@@ -509,8 +511,22 @@ def main():
     tune = None
     if not args.no_autotune:
         tune = eng.autotune(steps=3)  # set-up, outside the timed region; the state is restored
+    # Workloads timed as repeated runs of a fixed length from rest: the rest
+    # state is uploaded from device memory (one gather launch) at the start
+    # of every run, between step graphs.
+    episode = int(WORKLOAD.get("episode_steps", 0))
+    X0d = torch.from_numpy(np.ascontiguousarray(body.X, dtype=np.float32)).cuda()
+    V0d = torch.zeros_like(X0d)
+    torch.cuda.synchronize()
+
+    def start_episode(k):
+        if episode and k % episode == 0:
+            N.check(eng._lib.pdgb_upload_state(eng.handle, X0d.data_ptr(), V0d.data_ptr(), N.PDGB_MEM_DEVICE),
+                    "pdgb_upload_state")
+
     eng.enable_kernel_timing(N.PDGB_TIMING_STEPS)
     eng.prepare()
+    start_episode(0)
     for _ in range(args.warmup):
         eng.update(1)
         flush_l2()
@@ -523,11 +539,14 @@ def main():
     # between steps, outside the events.
     with ClockSampler(local) as clocks:
         for k in range(args.steps):
+            start_episode(k)
             eng.update(1)
             flush_l2()
         torch.cuda.synchronize()
     barrier(dist)
     tm = eng.read_timing()
+    Xt, _ = eng.download_state()
+    finite_timed = bool(np.isfinite(Xt).all())
     assert tm["steps"] == args.steps
     if collision is not None:
         _, _, cinfo = eng.collision()
@@ -539,9 +558,11 @@ def main():
     # roofline of the dominant kernel.
     eng.enable_kernel_timing(N.PDGB_TIMING_KERNELS)
     eng.prepare()
+    start_episode(0)
     eng.update(1)
     eng.read_timing()
     for k in range(args.steps):
+        start_episode(k)
         eng.update(1)
         flush_l2()
     eng.synchronize()
@@ -557,7 +578,8 @@ def main():
     eng.enable_kernel_timing(N.PDGB_TIMING_OFF)
     eng.prepare()
     nv = body.num_verts
-    Xh = torch.from_numpy(body.X.copy()).pin_memory()
+    X0h = torch.from_numpy(body.X.copy())
+    Xh = X0h.clone().pin_memory()
     Vh = torch.zeros((nv, 3), dtype=torch.float32).pin_memory()
     lib, h = eng._lib, eng.handle
     for _ in range(2):
@@ -565,7 +587,10 @@ def main():
         N.check(lib.pdgb_step(h, 1), "step")
         N.check(lib.pdgb_download_state(h, Xh.data_ptr(), Vh.data_ptr(), N.PDGB_MEM_HOST), "download")
     e2e_s = 0.0
-    for _ in range(args.steps):
+    for k in range(args.steps):
+        if k == 0 or (episode and k % episode == 0):
+            Xh.copy_(X0h)  # the caller starts a new run from rest
+            Vh.zero_()
         flush_l2()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -584,7 +609,17 @@ def main():
     # the local step alone, back to back (CUDA events around 200 launches on
     # the engine's stream, after the timed region): no event nodes between
     # launches inflate it, unlike the in-graph pairs above
-    local_b2b_ms = min(eng.time_local(200) for _ in range(3))
+    if episode:
+        # averaged over the states of one run from rest (the rotation's cost
+        # depends on the deformation)
+        start_episode(0)
+        b2b = []
+        for _ in range(episode):
+            b2b.append(eng.time_local(50))
+            eng.update(1)
+        local_b2b_ms = sum(b2b) / len(b2b)
+    else:
+        local_b2b_ms = min(eng.time_local(200) for _ in range(3))
     eng.close()
 
     if rank != 0:
@@ -601,6 +636,8 @@ def main():
                   "launches": local_launches,
                   "share_of_step": (local_ms / step_ms_kernel_pass) if step_ms_kernel_pass > 0 else None,
                   "back_to_back": {"avg_launch_us": local_b2b_ms * 1e3,
+                                   "sample": ("50 launches at each of the %d states of a run from rest, mean" % episode
+                                              if episode else "3 x 200 launches on the final state, min"),
                                    "achieved": bytes_per_launch / (local_b2b_ms / 1e3) / 1e9,
                                    "frac": bytes_per_launch / (local_b2b_ms / 1e3) / 1e9 / peak}}
     roofline, kernels = local_roof, {"local": local_roof}
@@ -626,7 +663,7 @@ def main():
     clk = clocks.summary()
     acc = None
     if not args.no_accuracy:
-        acc_steps = {"c1": 20, "c2": 2, "c3": 3, "c4": 5}[args.workload]
+        acc_steps = {"c1": 20, "c2": 20, "c3": 3, "c4": 5}[args.workload]
         acc = accuracy_vs_fp64(cpu_body, params, acc_steps, refine_sweep=args.workload == "c3")
         if bodies is not None:
             acc["sample"] = "first 16 bodies of the batch"
@@ -651,9 +688,10 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
                 "d2h_bytes_per_step": 2 * 3 * 4 * nv},
-        "gpu_launches": args.steps * launches_per_step(eng_info, params),
+        "gpu_launches": args.steps * launches_per_step(eng_info, params)
+                        + (-(-args.steps // episode) if episode else 0),  # + the rest-state upload of every run
         "clocks": clk,
-        "finite": finite,
+        "finite": finite and finite_timed,
         "accuracy": acc,
     }
     print(json.dumps(line), flush=True)
