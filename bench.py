@@ -354,6 +354,12 @@ def run_serving(args):
     for i in sample:
         rid, p, k = ids[i]
         results[i] = srv.result(rid)[0]
+    # every other result once: all finite (no request's iteration left the finite range)
+    nonfinite = sum(0 if np.isfinite(results[i]).all() else 1 for i in sample)
+    in_sample = set(sample)
+    for i, (rid, p, k) in enumerate(ids):
+        if i not in in_sample and not np.isfinite(srv.result(rid)[0]).all():
+            nonfinite += 1
     for i in sample:
         rid, p, k = ids[i]
         with PdSolver(pool[p], params) as e:
@@ -381,6 +387,7 @@ def run_serving(args):
                        "mean": float(np.mean(lat)) if len(lat) else None},
         "wall_s": wall, "completed": int(st["completed"] - base_completed), "failed": int(st["failed"]),
         "alone_vs_mix_max_rel_err": worst_alone, "alone_vs_mix_sample": len(sample),
+        "nonfinite_results": int(nonfinite),
         "accuracy": acc, "clocks": clocks.summary(),
         "busy_frac": float(st["busy_ms"] - base_busy) / 1e3 / wall,
         "server_ms": {"admit": st["admit_ms"], "step": st["step_ms"], "ticks": st["ticks"]},
