@@ -15,6 +15,18 @@
 
 namespace pdgb {
 
+// Programmatic dependent launch of the per-level kernels.  Each level kernel
+// lets the next launch be scheduled as soon as all of its own CTAs run
+// (launch_dependents); the next kernel reads its static item descriptors
+// and prefetches its factor blocks into L2 meanwhile, and reads nothing an
+// earlier kernel writes (r, y, x, z, the early-exit flag) before
+// griddepcontrol.wait, which returns once the previous grid has completed
+// and its writes are visible.  Every CTA waits before it can exit, so each
+// grid completes after its predecessor and the order holds along the chain.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // Forward warp item {moff, roff, m, k, r0, c0, c1}: lane = row r0 + lane of
 // M_s; sum over pivot columns c0..c1 of M_s[row, c] r[pivot c]; pivot rows
 // add the sum to y, off-diagonal rows subtract it from r (ancestor columns,
@@ -104,19 +116,23 @@ __device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, f
 // off-diagonal rows subtract from r (ancestor pivots, read at a later level).
 __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, int item0) {
     __shared__ float4 rs[kFwdBlockCols];
-    if (a.done && *a.done) return;
+    pdl_trigger();
     const int* w = a.fwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
     const int roff = h0.z, m = h0.w, k = h1.x, r0 = h1.y, c0 = h1.z, c1 = h1.w;
     const int* rows = a.rows + roff;
+    const int row = r0 + threadIdx.x;
+    const bool active = row < m && row < r0 + kFwdBlockRows;
+    const int cend = !active ? c0 : (row < k ? min(c1, row + 1) : c1);
+    const float* Mr = a.mval + moff + row;
+    for (int c = c0; c < cend; ++c) prefetch_l2(Mr + (size_t)c * m);
+    pdl_wait();
+    if (a.done && *a.done) return;
     for (int j = threadIdx.x; j < c1 - c0; j += kBlockThreads) rs[j] = a.r[__ldg(&rows[c0 + j])];
     __syncthreads();
-    const int row = r0 + threadIdx.x;
-    if (row >= m || row >= r0 + kFwdBlockRows) return;
-    const int cend = row < k ? min(c1, row + 1) : c1;
-    const float* Mr = a.mval + moff + row;
+    if (!active) return;
     float ax = 0.f, ay = 0.f, az = 0.f;
     int c = c0;
     for (; c + 8 <= cend; c += 8) {
@@ -150,10 +166,12 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
 // chunks, x at the pivot rows is cleared here: the backward blocks of the
 // level add their chunk sums into it.
 __global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, int item0) {
-    if (a.done && *a.done) return;
+    pdl_trigger();
     const int* w = a.zstage + (size_t)kItemInts * (item0 + blockIdx.x);
     const int roff = __ldg(w + 2), m = __ldg(w + 3), k = __ldg(w + 4), r0 = __ldg(w + 5), split = __ldg(w + 6),
               zoff = __ldg(w + 7);
+    pdl_wait();
+    if (a.done && *a.done) return;
     const int* rows = a.rows + roff;
     const int r1 = min(m, r0 + kStageRows);
     for (int i = r0 + threadIdx.x; i < r1; i += kStageThreads) {
@@ -177,7 +195,7 @@ __global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, i
 // (contiguous loads of M_s, one per column), then a warp reduction per
 // column whose sum is added into x.  Column c uses rows i >= c only.
 __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
-    if (a.done && *a.done) return;
+    pdl_trigger();
     const int* w = a.bwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
@@ -188,10 +206,18 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
     const float4* z = a.zbuf + zoff;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cw = c0 + kBwdWarpCols * warp;  // first column of this warp
-    if (cw >= c1) return;
     const int nc = min(kBwdWarpCols, c1 - cw);
-    if (cw >= rend) return;
     const float* Mc = a.mval + moff + (size_t)cw * m;
+    if (cw < c1 && cw < rend) {
+        // the warp's first 256 rows of each of its columns
+        const int i0 = max(cw, r0) + lane, i1 = min(rend, i0 + 256);
+        for (int j = 0; j < kBwdWarpCols; ++j)
+            if (j < nc)
+                for (int i = i0; i < i1; i += 32) prefetch_l2(Mc + (size_t)j * m + i);
+    }
+    pdl_wait();
+    if (a.done && *a.done) return;
+    if (cw >= c1 || cw >= rend) return;
     float acc[kBwdWarpCols][3];
 #pragma unroll
     for (int j = 0; j < kBwdWarpCols; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
@@ -230,6 +256,8 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
 // limited by the block kernels' registers and shared memory.
 __global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_small(CholArgs a, int item0, int nitems) {
     __shared__ float4 stage[kSmallThreads / 32][32];
+    pdl_trigger();
+    pdl_wait();
     if (a.done && *a.done) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int it = blockIdx.x * (kSmallThreads / 32) + warp;
@@ -237,6 +265,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_small(CholArgs a, in
 }
 
 __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_small(CholArgs a, int item0, int nitems) {
+    pdl_trigger();
+    pdl_wait();
     if (a.done && *a.done) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int it = blockIdx.x * (kSmallThreads / 32) + warp;
@@ -249,6 +279,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_small(CholArgs a, in
 // supernode writes them), off-diagonal rows subtract from r.  Backward:
 // x_c = sum_{i >= c} M[i, c] z_i over the supernode's rows.
 __global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_tiny(CholArgs a, int t0, int n) {
+    pdl_trigger();
+    pdl_wait();
     if (a.done && *a.done) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -280,6 +312,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_tiny(CholArgs a, int
 }
 
 __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int t0, int n) {
+    pdl_trigger();
+    pdl_wait();
     if (a.done && *a.done) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -316,23 +350,41 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int
         if (c < k) a.x[__ldg(&rows[c])] = make_float4(acc[c][0], acc[c][1], acc[c][2], 0.f);
 }
 
+namespace {
+// Launch with programmatic stream serialization (see pdl_wait).
+template <typename... P, typename... A>
+void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s, A... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PDGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kernel, args...));
+}
+}  // namespace
+
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
     constexpr int kWarps = kSmallThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
         const SolveLevel& v = levels[L];
         const int nb = v.fwdb_end - v.fwdb_begin, nw = v.fwdw_end - v.fwdw_begin, nt = v.tiny_end - v.tiny_begin;
-        if (nt > 0) k_chol_fwd_tiny<<<(nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s>>>(a, v.tiny_begin, nt);
-        if (nw > 0) k_chol_fwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.fwdw_begin, nw);
-        if (nb > 0) k_chol_fwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.fwdb_begin);
+        if (nt > 0) launch_pdl(k_chol_fwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, s, a, v.tiny_begin, nt);
+        if (nw > 0) launch_pdl(k_chol_fwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, s, a, v.fwdw_begin, nw);
+        if (nb > 0) launch_pdl(k_chol_fwd_block, nb, kBlockThreads, s, a, v.fwdb_begin);
     }
     for (size_t L = levels.size(); L-- > 0;) {
         const SolveLevel& v = levels[L];
         const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin, nt = v.tiny_end - v.tiny_begin;
         const int nz = v.zst_end - v.zst_begin;
-        if (nz > 0) k_chol_bwd_zstage<<<nz, kStageThreads, 0, s>>>(a, v.zst_begin);
-        if (nb > 0) k_chol_bwd_block<<<nb, kBlockThreads, 0, s>>>(a, v.bwdb_begin);
-        if (nw > 0) k_chol_bwd_small<<<(nw + kWarps - 1) / kWarps, kSmallThreads, 0, s>>>(a, v.bwdw_begin, nw);
-        if (nt > 0) k_chol_bwd_tiny<<<(nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s>>>(a, v.tiny_begin, nt);
+        if (nz > 0) launch_pdl(k_chol_bwd_zstage, nz, kStageThreads, s, a, v.zst_begin);
+        if (nb > 0) launch_pdl(k_chol_bwd_block, nb, kBlockThreads, s, a, v.bwdb_begin);
+        if (nw > 0) launch_pdl(k_chol_bwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, s, a, v.bwdw_begin, nw);
+        if (nt > 0) launch_pdl(k_chol_bwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, s, a, v.tiny_begin, nt);
     }
 }
 
