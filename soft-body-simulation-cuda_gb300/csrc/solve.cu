@@ -71,6 +71,20 @@ __device__ __forceinline__ void fwd_warp_item(const CholArgs& a, const int* w, f
     else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
 }
 
+// L2 prefetch of a forward warp item's static data (row ids and up to 16
+// columns of the lane's row of M_s), issued before the grid dependency wait.
+__device__ __forceinline__ void fwd_warp_prefetch(const CholArgs& a, const int* w, int lane) {
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
+    const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
+    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+    const int m = h0.w, k = h1.x, row = h1.y + lane, c0 = h1.z, c1 = h1.w;
+    if (row >= m) return;
+    const int cend = min(row < k ? min(c1, row + 1) : c1, c0 + 16);
+    const float* Mr = a.mval + moff + row;
+    for (int c = c0; c < cend; ++c) prefetch_l2(Mr + (size_t)c * m);
+    if (lane == 0) prefetch_l2(a.rows + h0.z + h1.y);
+}
+
 // Backward warp item {moff, roff, m, k, c}: x[pivot c] = sum_{i >= c}
 // M_s[i, c] z_i with z = [y_pivots ; -x_offdiag]; lanes stride over rows
 // (a coalesced column of M_s, 4 independent loads in flight per lane),
@@ -108,6 +122,17 @@ __device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, f
     if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
 }
 
+// L2 prefetch of a backward warp item's column of M_s and its row ids.
+__device__ __forceinline__ void bwd_warp_prefetch(const CholArgs& a, const int* w, int lane) {
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
+    const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
+    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+    const int m = h0.w, c = h1.y;
+    const float* Mc = a.mval + moff + (size_t)c * m;
+    for (int i = c + 32 * lane; i < m && i < c + 256; i += 32 * 32) prefetch_l2(Mc + i);
+    if (lane < 8 && c + 32 * lane < m) prefetch_l2(a.rows + h0.z + c + 32 * lane);
+}
+
 // ---- per-level launches with CTA block items.
 // Forward block {moff, roff, m, k, r0, c0, c1}: the pivot right-hand sides
 // r[c0 .. c1) are staged in shared memory once; thread t owns row r0 + t and
@@ -127,34 +152,28 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
     const bool active = row < m && row < r0 + kFwdBlockRows;
     const int cend = !active ? c0 : (row < k ? min(c1, row + 1) : c1);
     const float* Mr = a.mval + moff + row;
-    for (int c = c0; c < cend; ++c) prefetch_l2(Mr + (size_t)c * m);
+    // the thread's row of the item (at most kFwdBlockCols columns, zero past
+    // cend) and the staging indices are static: loaded before the wait
+    float mv[kFwdBlockCols];
+#pragma unroll
+    for (int q = 0; q < kFwdBlockCols; ++q) mv[q] = (c0 + q < cend) ? __ldg(Mr + (size_t)(c0 + q) * m) : 0.f;
+    const int vid = active ? __ldg(&rows[row]) : 0;
+    const int ncols = c1 - c0;
+    const int sv = (int)threadIdx.x < ncols ? __ldg(&rows[c0 + threadIdx.x]) : 0;
     pdl_wait();
     if (a.done && *a.done) return;
-    for (int j = threadIdx.x; j < c1 - c0; j += kBlockThreads) rs[j] = a.r[__ldg(&rows[c0 + j])];
+    if (threadIdx.x < kFwdBlockCols)
+        rs[threadIdx.x] = (int)threadIdx.x < ncols ? a.r[sv] : make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     if (!active) return;
     float ax = 0.f, ay = 0.f, az = 0.f;
-    int c = c0;
-    for (; c + 8 <= cend; c += 8) {
-        float mv[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) mv[q] = __ldg(Mr + (size_t)(c + q) * m);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const float4 v = rs[c + q - c0];
-            ax = fmaf(mv[q], v.x, ax);
-            ay = fmaf(mv[q], v.y, ay);
-            az = fmaf(mv[q], v.z, az);
-        }
+    for (int q = 0; q < kFwdBlockCols; ++q) {
+        const float4 v = rs[q];
+        ax = fmaf(mv[q], v.x, ax);
+        ay = fmaf(mv[q], v.y, ay);
+        az = fmaf(mv[q], v.z, az);
     }
-    for (; c < cend; ++c) {
-        const float mv = __ldg(Mr + (size_t)c * m);
-        const float4 v = rs[c - c0];
-        ax = fmaf(mv, v.x, ax);
-        ay = fmaf(mv, v.y, ay);
-        az = fmaf(mv, v.z, az);
-    }
-    const int vid = __ldg(&rows[row]);
     if (row < k) atomicAdd(&a.y[vid], make_float4(ax, ay, az, 0.f));
     else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
 }
@@ -170,12 +189,14 @@ __global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, i
     const int* w = a.zstage + (size_t)kItemInts * (item0 + blockIdx.x);
     const int roff = __ldg(w + 2), m = __ldg(w + 3), k = __ldg(w + 4), r0 = __ldg(w + 5), split = __ldg(w + 6),
               zoff = __ldg(w + 7);
-    pdl_wait();
-    if (a.done && *a.done) return;
     const int* rows = a.rows + roff;
     const int r1 = min(m, r0 + kStageRows);
-    for (int i = r0 + threadIdx.x; i < r1; i += kStageThreads) {
-        const int vid = __ldg(&rows[i]);
+    const int i0 = r0 + threadIdx.x;
+    const int vid0 = i0 < r1 ? __ldg(&rows[i0]) : 0;
+    pdl_wait();
+    if (a.done && *a.done) return;
+    for (int i = i0; i < r1; i += kStageThreads) {
+        const int vid = i == i0 ? vid0 : __ldg(&rows[i]);
         float4 z;
         if (i < k) {
             z = a.y[vid];
@@ -257,20 +278,31 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
 __global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_small(CholArgs a, int item0, int nitems) {
     __shared__ float4 stage[kSmallThreads / 32][32];
     pdl_trigger();
-    pdl_wait();
-    if (a.done && *a.done) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int it = blockIdx.x * (kSmallThreads / 32) + warp;
+    if (it < nitems) fwd_warp_prefetch(a, a.fwd_small + (size_t)kItemInts * (item0 + it), lane);
+    pdl_wait();
+    if (a.done && *a.done) return;
     if (it < nitems) fwd_warp_item(a, a.fwd_small + (size_t)kItemInts * (item0 + it), stage[warp], lane);
 }
 
 __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_small(CholArgs a, int item0, int nitems) {
     pdl_trigger();
-    pdl_wait();
-    if (a.done && *a.done) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int it = blockIdx.x * (kSmallThreads / 32) + warp;
+    if (it < nitems) bwd_warp_prefetch(a, a.bwd_small + (size_t)kItemInts * (item0 + it), lane);
+    pdl_wait();
+    if (a.done && *a.done) return;
     if (it < nitems) bwd_warp_item(a, a.bwd_small + (size_t)kItemInts * (item0 + it), nullptr, lane);
+}
+
+// L2 prefetch of a tiny supernode's columns of M_s and row ids.
+__device__ __forceinline__ void tiny_prefetch(const CholArgs& a, int item) {
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * item));
+    const float* M = a.mval + ((int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32));
+    const int m = h0.w, k = __ldg(a.tiny + (size_t)kItemInts * item + 4);
+    for (int i = 0; i < k * m; i += 32) prefetch_l2(M + i);
+    prefetch_l2(a.rows + h0.z);
 }
 
 // Tiny supernodes (at most kTinyCols pivots, kTinyRows rows): one thread
@@ -280,9 +312,10 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_small(CholArgs a, in
 // x_c = sum_{i >= c} M[i, c] z_i over the supernode's rows.
 __global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_tiny(CholArgs a, int t0, int n) {
     pdl_trigger();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) tiny_prefetch(a, t0 + t);
     pdl_wait();
     if (a.done && *a.done) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * (t0 + t)));
     const int k = __ldg(a.tiny + (size_t)kItemInts * (t0 + t) + 4);
@@ -313,9 +346,10 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_tiny(CholArgs a, int
 
 __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int t0, int n) {
     pdl_trigger();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) tiny_prefetch(a, t0 + t);
     pdl_wait();
     if (a.done && *a.done) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * (t0 + t)));
     const int k = __ldg(a.tiny + (size_t)kItemInts * (t0 + t) + 4);
