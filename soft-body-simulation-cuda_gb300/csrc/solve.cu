@@ -122,15 +122,72 @@ __device__ __forceinline__ void bwd_warp_item(const CholArgs& a, const int* w, f
     if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
 }
 
-// L2 prefetch of a backward warp item's column of M_s and its row ids.
-__device__ __forceinline__ void bwd_warp_prefetch(const CholArgs& a, const int* w, int lane) {
-    const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
-    const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
-    const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
-    const int m = h0.w, c = h1.y;
-    const float* Mc = a.mval + moff + (size_t)c * m;
-    for (int i = c + 32 * lane; i < m && i < c + 256; i += 32 * 32) prefetch_l2(Mc + i);
-    if (lane < 8 && c + 32 * lane < m) prefetch_l2(a.rows + h0.z + c + 32 * lane);
+// Backward warp item with its first 64 rows of M_s and row ids loaded
+// into registers before the grid dependency wait (the small supernodes of
+// the per-level kernels have fewer rows than that); same sums, same order
+// as bwd_warp_item.
+__device__ __forceinline__ void bwd_warp_item_pre(const CholArgs& a, const int* w, int lane, bool item) {
+    int m = 0, k = 0, c = 0;
+    const int* rows = a.rows;
+    const float* Mc = a.mval;
+    float mv[2] = {0.f, 0.f};
+    int vid[2] = {0, 0};
+    if (item) {
+        const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
+        const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
+        const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
+        m = h0.w;
+        k = h1.x;
+        c = h1.y;
+        rows = a.rows + h0.z;
+        Mc = a.mval + moff + (size_t)c * m;
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            const int i = c + lane + 32 * t;
+            if (i < m) {
+                mv[t] = __ldg(Mc + i);
+                vid[t] = __ldg(&rows[i]);
+            }
+        }
+    }
+    pdl_wait();
+    if ((a.done && *a.done) || !item) return;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const int i = c + lane + 32 * t;
+        if (i < m) {
+            float4 z;
+            if (i < k) z = a.y[vid[t]];
+            else {
+                const float4 xv = a.x[vid[t]];
+                z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+            }
+            ax = fmaf(mv[t], z.x, ax);
+            ay = fmaf(mv[t], z.y, ay);
+            az = fmaf(mv[t], z.z, az);
+        }
+    }
+    for (int i = c + lane + 64; i < m; i += 32) {
+        const int v = __ldg(&rows[i]);
+        const float mvi = __ldg(Mc + i);
+        float4 z;
+        if (i < k) z = a.y[v];
+        else {
+            const float4 xv = a.x[v];
+            z = make_float4(-xv.x, -xv.y, -xv.z, 0.f);
+        }
+        ax = fmaf(mvi, z.x, ax);
+        ay = fmaf(mvi, z.y, ay);
+        az = fmaf(mvi, z.z, az);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, off);
+        ay += __shfl_xor_sync(0xffffffffu, ay, off);
+        az += __shfl_xor_sync(0xffffffffu, az, off);
+    }
+    if (lane == 0) a.x[__ldg(&rows[c])] = make_float4(ax, ay, az, 0.f);
 }
 
 // ---- per-level launches with CTA block items.
@@ -229,21 +286,43 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
     const int cw = c0 + kBwdWarpCols * warp;  // first column of this warp
     const int nc = min(kBwdWarpCols, c1 - cw);
     const float* Mc = a.mval + moff + (size_t)cw * m;
-    if (cw < c1 && cw < rend) {
-        // the warp's first 256 rows of each of its columns
-        const int i0 = max(cw, r0) + lane, i1 = min(rend, i0 + 256);
+    // The warp's first 256 rows of each of its columns (a whole 256-row
+    // chunk) are loaded into registers before the wait; longer columns of
+    // whole-column items stream the rest afterwards.
+    constexpr int kPre = 8;
+    const bool live = cw < c1 && cw < rend;
+    const int ib = max(cw, r0) + lane;
+    float mpre[kPre][kBwdWarpCols];
+#pragma unroll
+    for (int t = 0; t < kPre; ++t) {
+        const int i = ib + 32 * t;
+#pragma unroll
         for (int j = 0; j < kBwdWarpCols; ++j)
-            if (j < nc)
-                for (int i = i0; i < i1; i += 32) prefetch_l2(Mc + (size_t)j * m + i);
+            mpre[t][j] = (live && j < nc && i < rend && i >= cw + j) ? __ldg(Mc + (size_t)j * m + i) : 0.f;
     }
     pdl_wait();
     if (a.done && *a.done) return;
-    if (cw >= c1 || cw >= rend) return;
+    if (!live) return;
     float acc[kBwdWarpCols][3];
 #pragma unroll
     for (int j = 0; j < kBwdWarpCols; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
+#pragma unroll
+    for (int t = 0; t < kPre; ++t) {
+        const int i = ib + 32 * t;
+        if (i < rend) {
+            const float4 zz = z[i];
+#pragma unroll
+            for (int j = 0; j < kBwdWarpCols; ++j) {
+                if (j < nc && i >= cw + j) {
+                    acc[j][0] = fmaf(mpre[t][j], zz.x, acc[j][0]);
+                    acc[j][1] = fmaf(mpre[t][j], zz.y, acc[j][1]);
+                    acc[j][2] = fmaf(mpre[t][j], zz.z, acc[j][2]);
+                }
+            }
+        }
+    }
 #pragma unroll 2
-    for (int i = max(cw, r0) + lane; i < rend; i += 32) {
+    for (int i = ib + 32 * kPre; i < rend; i += 32) {
         const float4 zz = z[i];
 #pragma unroll
         for (int j = 0; j < kBwdWarpCols; ++j) {
@@ -290,10 +369,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_small(CholArgs a, in
     pdl_trigger();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int it = blockIdx.x * (kSmallThreads / 32) + warp;
-    if (it < nitems) bwd_warp_prefetch(a, a.bwd_small + (size_t)kItemInts * (item0 + it), lane);
-    pdl_wait();
-    if (a.done && *a.done) return;
-    if (it < nitems) bwd_warp_item(a, a.bwd_small + (size_t)kItemInts * (item0 + it), nullptr, lane);
+    bwd_warp_item_pre(a, a.bwd_small + (size_t)kItemInts * (item0 + min(it, nitems - 1)), lane, it < nitems);
 }
 
 // L2 prefetch of a tiny supernode's columns of M_s and row ids.
