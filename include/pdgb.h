@@ -290,8 +290,8 @@ int pdgb_set_rotation(pdgb_engine* e, int rotation);
  * (distributed shared memory between the CTAs; PDGB_ERR_UNSUPPORTED at
  * prepare when it does not fit; on request only: with whole supernodes
  * per CTA and remote float atomics it measures slower than CLUSTER on the
- * bodies that fit).  AUTO picks by size: a batch uses CTA, a single system
- * CLUSTER up to 2^20 stored factor entries and LEVELS above;
+ * bodies that fit).  AUTO picks by size: LEVELS from 2^15 stored factor
+ * entries up, below that CLUSTER for a single system and CTA for a batch;
  * pdgb_autotune times CTA, CLUSTER and LEVELS.  Takes
  * effect at the next prepare; pdgb_get_solve_mode returns the schedule in
  * use (AUTO before the first prepare or on the Jacobi path). */

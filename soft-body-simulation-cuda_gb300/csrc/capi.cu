@@ -119,7 +119,7 @@ struct pdgb_engine {
 namespace {
 
 // Factors up to this many stored entries use the single-CTA solve.
-constexpr size_t kCtaSolveMaxEntries = 1u << 20;
+constexpr size_t kCtaSolveMaxEntries = 1u << 15;
 
 template <class F> int guarded(F&& f) {
     try {
@@ -386,18 +386,21 @@ SparseSym engine_system(const HostLayout& L) {
     return assemble_system(L.nv, L.nt, L.tets_int.data(), L.dminv_d.data(), L.coef_d.data(), mdt2);
 }
 
-// Solve schedule: the requested one, or by size.  A single CTA or one
-// cluster per body walks a body's whole tree when the factor is small (the
-// solve is then bound by the tree depth, not by bandwidth, and launches
-// would dominate); batches always run one CTA or cluster per body.
+// Solve schedule: the requested one, or by size.  The per-level launches
+// (programmatic dependent launch, factor blocks loaded before each wait)
+// are fastest from a single 10^3 body up (48 K stored entries: 59 us per
+// solve against 68 us for one cluster; 512 bodies: 0.82 ms against 2.4 ms
+// for one CTA per body); below 2^15 stored entries the chain of launches
+// dominates and one cluster (a single body) or one CTA per body (a batch)
+// walks the whole tree instead.
 int choose_solve_mode(const pdgb_engine* e) {
     const bool small = e->chol.mval.size() <= kCtaSolveMaxEntries;
     const int m = e->solve_req;
     if (m == PDGB_SOLVE_DSM && !e->dsm.ok)
         throw Error{PDGB_ERR_UNSUPPORTED, "the factor does not fit the shared memory of one cluster (DSM solve)"};
     if (m != PDGB_SOLVE_AUTO) return m;
-    if (e->nbodies > 1) return PDGB_SOLVE_CTA;
-    return small ? PDGB_SOLVE_CLUSTER : PDGB_SOLVE_LEVELS;
+    if (!small) return PDGB_SOLVE_LEVELS;
+    return e->nbodies > 1 ? PDGB_SOLVE_CTA : PDGB_SOLVE_CLUSTER;
 }
 
 void prepare_cholesky(pdgb_engine* e) {
@@ -466,9 +469,6 @@ void prepare_cholesky(pdgb_engine* e) {
             e->dsm_lvl.upload(e->dsm.lvl, s);
         }
     }
-    // A single CTA walks a body's whole tree when the factor is small (the
-    // solve is then bound by the tree depth, not by bandwidth, and launches
-    // would dominate); batches of bodies always run one CTA per body.
     e->solve_mode = choose_solve_mode(e);
     e->chol_ordering = e->ordering;
     e->chol_dt = e->prm.dt;
