@@ -9,6 +9,7 @@
 //   k_begin        step prologue: gravity, s_n, M/h^2 s_n (reference:
 //                  pdSolver.cu:154-163, computeSn pdUtil.cu:73-95)
 #include "engine.h"
+#include "pdl.cuh"
 #include "scene.cuh"
 #include "rotation.cuh"
 
@@ -30,6 +31,7 @@ namespace pdgb {
 // atomics; within a tile the sums are deterministic.
 template <bool kJacobiForm, int kRotation>
 __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4* slot, float4* pos) {
+    pdl_trigger();
     const int vb = a.tile_vptr[tile];
     const int np = a.tile_vptr[tile + 1] - vb;
     const int t0 = a.tile_tet_ptr[tile], t1 = a.tile_tet_ptr[tile + 1];
@@ -54,6 +56,9 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         GC[0] = __ldg(geo2 + t);
         S[0] = __ldg(reinterpret_cast<const uint2*>(a.inc_ent) + t);
     }
+    // the tile's layout and first geometry are in flight; positions, b and
+    // the early-exit flag come from earlier kernels of the step
+    pdl_wait();
     if (a.done && *a.done) return;
     // the first patch vertex of each thread keeps its id and slot run in
     // registers for the reduction phase
@@ -183,6 +188,10 @@ void launch_local_multi(const LocalArgs* req, const int2* list, const int* count
     if (grid > 0) k_local_multi<true><<<grid, kLocalThreads, kMaxPatch * sizeof(float4), s>>>(req, list, count);
 }
 
+// The plain form (Cholesky path) is launched with programmatic dependent
+// launch: its CTAs load their tile layout and first geometry while the
+// preceding kernel drains.  On the Jacobi path, local step and vertex update
+// alternate 20 times per step and plain launches measured faster.
 void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_form, int rotation, cudaStream_t s) {
     if (ntiles <= 0) return;
     if (max_patch < 1 || max_patch > kMaxPatch)
@@ -190,10 +199,10 @@ void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_for
     const size_t sm = (size_t)max_patch * sizeof(float4);
     if (rotation == PDGB_ROTATION_SVD) {
         if (jacobi_form) k_local<true, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, sm, s>>>(a);
-        else k_local<false, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, sm, s>>>(a);
+        else launch_pdl(k_local<false, PDGB_ROTATION_SVD>, ntiles, kLocalThreads, sm, s, a);
     } else {
         if (jacobi_form) k_local<true, PDGB_ROTATION_QUAT><<<ntiles, kLocalThreads, sm, s>>>(a);
-        else k_local<false, PDGB_ROTATION_QUAT><<<ntiles, kLocalThreads, sm, s>>>(a);
+        else launch_pdl(k_local<false, PDGB_ROTATION_QUAT>, ntiles, kLocalThreads, sm, s, a);
     }
 }
 
@@ -338,6 +347,7 @@ __device__ __forceinline__ void begin_vertex(const BeginArgs& a, int i) {
 }
 
 __global__ void __launch_bounds__(256) k_begin(BeginArgs a) {
+    pdl_trigger();  // the step's first local step may be scheduled meanwhile (Cholesky path)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         if (a.done) *a.done = 0;

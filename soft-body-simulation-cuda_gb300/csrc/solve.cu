@@ -9,23 +9,17 @@
 // hold engine vertex ids, so no permutation pass is needed.
 #include "engine.h"
 #include "solve.h"
+#include "pdl.cuh"
 #include "scene.cuh"
 
 #include <cooperative_groups.h>
 
 namespace pdgb {
 
-// Programmatic dependent launch of the per-level kernels.  Each level kernel
-// lets the next launch be scheduled as soon as all of its own CTAs run
-// (launch_dependents); the next kernel reads its static item descriptors
-// and prefetches its factor blocks into L2 meanwhile, and reads nothing an
-// earlier kernel writes (r, y, x, z, the early-exit flag) before
-// griddepcontrol.wait, which returns once the previous grid has completed
-// and its writes are visible.  Every CTA waits before it can exit, so each
-// grid completes after its predecessor and the order holds along the chain.
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+// The per-level kernels are launched with programmatic dependent launch
+// (pdl.cuh): each triggers its dependents at entry and, before its wait,
+// reads only its item descriptors, factor blocks and row ids -- never r, y,
+// x, z or the early-exit flag, which earlier kernels write.
 
 // Forward warp item {moff, roff, m, k, r0, c0, c1}: lane = row r0 + lane of
 // M_s; sum over pivot columns c0..c1 of M_s[row, c] r[pivot c]; pivot rows
@@ -460,41 +454,23 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int
         if (c < k) a.x[__ldg(&rows[c])] = make_float4(acc[c][0], acc[c][1], acc[c][2], 0.f);
 }
 
-namespace {
-// Launch with programmatic stream serialization (see pdl_wait).
-template <typename... P, typename... A>
-void launch_pdl(void (*kernel)(P...), int grid, int block, cudaStream_t s, A... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3((unsigned)block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    PDGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kernel, args...));
-}
-}  // namespace
-
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
     constexpr int kWarps = kSmallThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
         const SolveLevel& v = levels[L];
         const int nb = v.fwdb_end - v.fwdb_begin, nw = v.fwdw_end - v.fwdw_begin, nt = v.tiny_end - v.tiny_begin;
-        if (nt > 0) launch_pdl(k_chol_fwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, s, a, v.tiny_begin, nt);
-        if (nw > 0) launch_pdl(k_chol_fwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, s, a, v.fwdw_begin, nw);
-        if (nb > 0) launch_pdl(k_chol_fwd_block, nb, kBlockThreads, s, a, v.fwdb_begin);
+        if (nt > 0) launch_pdl(k_chol_fwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s, a, v.tiny_begin, nt);
+        if (nw > 0) launch_pdl(k_chol_fwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, 0, s, a, v.fwdw_begin, nw);
+        if (nb > 0) launch_pdl(k_chol_fwd_block, nb, kBlockThreads, 0, s, a, v.fwdb_begin);
     }
     for (size_t L = levels.size(); L-- > 0;) {
         const SolveLevel& v = levels[L];
         const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin, nt = v.tiny_end - v.tiny_begin;
         const int nz = v.zst_end - v.zst_begin;
-        if (nz > 0) launch_pdl(k_chol_bwd_zstage, nz, kStageThreads, s, a, v.zst_begin);
-        if (nb > 0) launch_pdl(k_chol_bwd_block, nb, kBlockThreads, s, a, v.bwdb_begin);
-        if (nw > 0) launch_pdl(k_chol_bwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, s, a, v.bwdw_begin, nw);
-        if (nt > 0) launch_pdl(k_chol_bwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, s, a, v.tiny_begin, nt);
+        if (nz > 0) launch_pdl(k_chol_bwd_zstage, nz, kStageThreads, 0, s, a, v.zst_begin);
+        if (nb > 0) launch_pdl(k_chol_bwd_block, nb, kBlockThreads, 0, s, a, v.bwdb_begin);
+        if (nw > 0) launch_pdl(k_chol_bwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, 0, s, a, v.bwdw_begin, nw);
+        if (nt > 0) launch_pdl(k_chol_bwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s, a, v.tiny_begin, nt);
     }
 }
 
