@@ -262,10 +262,11 @@ def run_reference_arm(args, body, params, scale=1.0):
     print(json.dumps(line), flush=True)
 
 
-def accuracy_vs_fp64(body, params, steps: int, refine_sweep: bool = False) -> dict:
+def accuracy_vs_fp64(body, params, steps: int, refine_sweep: bool = False, ref_gpu: bool = False) -> dict:
     """Engine vs the FP64 oracle from the rest state, `steps` steps of the
     workload (a bounded sample); relative L2 errors of positions and of
-    displacements.  With refine_sweep: one entry per refinement count 0..3."""
+    displacements.  With refine_sweep: one entry per refinement count 0..3.
+    With ref_gpu: the restated reference GPU path as well."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as O
     from pdgb import PdSolver
@@ -284,7 +285,52 @@ def accuracy_vs_fp64(body, params, steps: int, refine_sweep: bool = False) -> di
         key = f"refine{r}" if refine_sweep else "engine"
         out[key] = {"rel_err_x": float(np.linalg.norm(X - Xo) / np.linalg.norm(Xo)),
                     "rel_err_disp": float(np.linalg.norm(X - Xo) / max(np.linalg.norm(Xo - X0), 1e-30))}
+    if ref_gpu:
+        sys.path.insert(0, str(ROOT / "baseline"))
+        import refgpu
+
+        with refgpu.ReferenceGpuPath(body, params) as r:
+            r.step(steps)
+            X, _ = r.state()
+        X = X.astype(np.float64)
+        out["reference_gpu"] = {"rel_err_x": float(np.linalg.norm(X - Xo) / np.linalg.norm(Xo)),
+                                "rel_err_disp": float(np.linalg.norm(X - Xo) / max(np.linalg.norm(Xo - X0), 1e-30))}
     return out
+
+
+def reference_gpu(body, params, nsteps: int, episode: int, sample: str) -> dict:
+    """The reference's GPU PD step restated with cuSOLVER's FP32 sparse
+    Cholesky (baseline/refgpu.cu), timed on this GPU with CUDA events on the
+    default stream around `nsteps` steps (inputs resident, set-up and factor
+    outside); Jacobi workloads run from rest in runs of `episode` steps.  Its
+    Cholesky branch reads the error on the host every iteration, as the
+    reference does."""
+    sys.path.insert(0, str(ROOT / "baseline"))
+    import refgpu
+
+    t0 = time.perf_counter()
+    r = refgpu.ReferenceGpuPath(body, params)
+    setup_s = time.perf_counter() - t0
+    try:
+        r.step(3)  # warm-up
+        r.reset()
+        ms, its, done = 0.0, 0, 0
+        while done < nsteps:
+            k = min(nsteps - done, episode) if episode else nsteps - done
+            if episode:
+                r.reset()
+            m, i = r.step(k)
+            ms, its, done = ms + m, its + i, done + k
+        X, _ = r.state()
+        nnz = r.system_nnz()
+    finally:
+        r.close()
+    return {"value": body.num_tets * its / (ms / 1e3), "unit": UNIT, "kind": "port",
+            "what": "the reference's PdSolver::SolverStep kernels restated (per-tet threads, 12 float atomics per "
+                    "tet, 4-sweep SVD) with cuSOLVER's low-level FP32 sparse Cholesky (symamd ordering) on the "
+                    "3n x 3n system, or Jacobi + Chebyshev; legacy default stream, 128 threads per block",
+            "steps": nsteps, "iterations": its, "ms_per_step": ms / nsteps, "setup_s": setup_s,
+            "system_nnz": nnz, "finite": bool(np.isfinite(X).all()), "sample": sample}
 
 
 def run_serving(args):
@@ -437,6 +483,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-oracle error report")
     ap.add_argument("--window", type=float, default=20.0, help="arrival window of the serving workload, seconds")
     ap.add_argument("--rate", type=float, default=0.0, help="serving: mean arrivals per second (0 = the workload's)")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip the restated reference GPU path "
+                    "(cuSOLVER Cholesky / Jacobi) timed beside the engine")
     ap.add_argument("--collision", action="store_true", help="run continuous collision between bodies after every "
                     "step (inside the timed region)")
     args = ap.parse_args()
@@ -668,10 +716,18 @@ def main():
         if bodies is not None:
             cpu["sample"] += f"; the first 16 of the {len(bodies)} bodies"
     clk = clocks.summary()
+    ref_gpu = None
+    if not args.no_ref_gpu:
+        ref_steps = {"c1": 20, "c2": 50, "c3": 3, "c4": 5}[args.workload]
+        ref_sample = (f"{ref_steps} steps of the workload" if bodies is None else
+                      f"{ref_steps} steps of the first 16 of the {len(bodies)} bodies concatenated into one system "
+                      "(the reference's multi-body mode)")
+        ref_gpu = reference_gpu(cpu_body, params, ref_steps, episode, ref_sample)
     acc = None
     if not args.no_accuracy:
         acc_steps = {"c1": 20, "c2": 20, "c3": 3, "c4": 5}[args.workload]
-        acc = accuracy_vs_fp64(cpu_body, params, acc_steps, refine_sweep=args.workload == "c3")
+        acc = accuracy_vs_fp64(cpu_body, params, acc_steps, refine_sweep=args.workload == "c3",
+                               ref_gpu=not args.no_ref_gpu)
         if bodies is not None:
             acc["sample"] = "first 16 bodies of the batch"
     line = {
@@ -693,6 +749,7 @@ def main():
         "autotune": tune,
         "collision": collision,
         "cpu_baseline": cpu,
+        "reference_gpu": ref_gpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
                 "d2h_bytes_per_step": 2 * 3 * 4 * nv},
         "gpu_launches": args.steps * launches_per_step(eng_info, params)

@@ -5,6 +5,9 @@
 - ``oracle/liboracle.so``: the CPU oracle (test infrastructure), g++.
 - ``oracle/_ref/libref_pd.so``: the reference's own PD kernels compiled as
   C++ (only where the reference sources are present; test infrastructure).
+- ``baseline/_build/librefgpu.so``: the reference's GPU PD step restated with
+  cuSOLVER's sparse Cholesky, timed beside the engine (a baseline, not part
+  of the engine).
 
 Nothing here downloads anything; the only tools used are nvcc and g++.
 """
@@ -23,6 +26,8 @@ LIB_DIR = PKG_DIR / "_lib"
 LIB_PATH = LIB_DIR / "libpdgb.so"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "_build" / "liboracle.so"
+BASELINE_DIR = ROOT / "baseline"
+REFGPU_LIB = BASELINE_DIR / "_build" / "librefgpu.so"
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -108,9 +113,23 @@ def build_reference_harness(force: bool = False) -> Path | None:
     return out if out.exists() else None
 
 
+def build_refgpu(force: bool = False) -> Path:
+    src = BASELINE_DIR / "refgpu.cu"
+    deps = [src, CSRC / "rotation.cuh", Path(__file__)]
+    if not force and not _stale(REFGPU_LIB, deps):
+        return REFGPU_LIB
+    REFGPU_LIB.parent.mkdir(parents=True, exist_ok=True)
+    tmp = REFGPU_LIB.with_suffix(".so.tmp")
+    _run([_nvcc()] + ARCH_FLAGS + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                                   "-Wno-deprecated-declarations", "-I", str(CSRC), "-shared", str(src), "-o",
+                                   str(tmp), "-lcusolver", "-lcusparse"])
+    os.replace(tmp, REFGPU_LIB)
+    return REFGPU_LIB
+
+
 def build_all(force: bool = False) -> None:
-    with _cf.ThreadPoolExecutor(max_workers=3) as ex:
+    with _cf.ThreadPoolExecutor(max_workers=4) as ex:
         futs = [ex.submit(build_engine, force), ex.submit(build_oracle, force),
-                ex.submit(build_reference_harness, force)]
+                ex.submit(build_reference_harness, force), ex.submit(build_refgpu, force)]
         for f in futs:
             f.result()
