@@ -333,6 +333,43 @@ def reference_gpu(body, params, nsteps: int, episode: int, sample: str) -> dict:
             "system_nnz": nnz, "finite": bool(np.isfinite(X).all()), "sample": sample}
 
 
+def plain_drop_in(bodies, params, steps: int, flush) -> dict:
+    """The plain drop-in on the batch's bodies: one engine per body, run one
+    body at a time (the engine as a single-scene PdSolver replacement), the
+    same step timing as the batch (CUDA events around every step graph, L2
+    flushed between steps outside the events)."""
+    from pdgb import PdSolver
+    from pdgb import _native as N
+
+    import torch
+
+    tet_iters, ms = 0.0, 0.0
+    for b in bodies:
+        with PdSolver(b, params) as e:
+            stream = torch.cuda.ExternalStream(e._lib.pdgb_stream(e.handle))
+
+            def flush_l2():
+                with torch.cuda.stream(stream):
+                    flush.add_(1.0)
+
+            e.enable_kernel_timing(N.PDGB_TIMING_STEPS)
+            e.prepare()
+            for _ in range(3):
+                e.update(1)
+            e.synchronize()
+            e.read_timing()
+            for _ in range(steps):
+                e.update(1)
+                flush_l2()
+            e.synchronize()
+            tm = e.read_timing()
+        ms += tm["step_ms"]
+        tet_iters += float(b.num_tets * params.num_iterations * steps)
+    return {"value": tet_iters / (ms / 1e3), "unit": UNIT, "bodies": len(bodies), "steps": steps,
+            "ms_per_body_step": ms / (len(bodies) * steps),
+            "sample": f"every 8th body of the batch ({len(bodies)} bodies), one engine each, run one after another"}
+
+
 def run_serving(args):
     """Serving workload: wall-clock request arrivals into the server."""
     import math
@@ -483,6 +520,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64-oracle error report")
     ap.add_argument("--window", type=float, default=20.0, help="arrival window of the serving workload, seconds")
     ap.add_argument("--rate", type=float, default=0.0, help="serving: mean arrivals per second (0 = the workload's)")
+    ap.add_argument("--no-plain", action="store_true", help="batch workload: skip the plain drop-in leg (the same "
+                    "bodies one engine each, one at a time)")
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip the restated reference GPU path "
                     "(cuSOLVER Cholesky / Jacobi) timed beside the engine")
     ap.add_argument("--collision", action="store_true", help="run continuous collision between bodies after every "
@@ -655,6 +694,9 @@ def main():
         e2e_s += time.perf_counter() - t0
     e2e_max = reduce_max(dist, e2e_s)
     e2e_value = tet_iters / e2e_max
+    plain = None
+    if bodies is not None and not args.no_plain:
+        plain = plain_drop_in(bodies[::8], params, 10, flush)
     finite = bool(torch.isfinite(Xh).all().item())
     eng_info = eng.get_performance_data()
     eng_info["levels"] = eng.solve_levels() if params.solver == 1 else 0
@@ -750,6 +792,7 @@ def main():
         "collision": collision,
         "cpu_baseline": cpu,
         "reference_gpu": ref_gpu,
+        "plain_drop_in": plain,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
                 "d2h_bytes_per_step": 2 * 3 * 4 * nv},
         "gpu_launches": args.steps * launches_per_step(eng_info, params)
