@@ -276,12 +276,15 @@ def accuracy_vs_fp64(body, params, steps: int, refine_sweep: bool = False, ref_g
     X0 = body.X.astype(np.float64)
     out = {"steps": steps, "oracle": "fp64"}
     counts = range(4) if refine_sweep else [params.refine_steps]
+    X_engine = None
     for r in counts:
         p = SolverParams(**{**params.__dict__, "refine_steps": r})
         with PdSolver(body, p) as e:
             e.update(steps)
             X, _ = e.download_state()
         X = X.astype(np.float64)
+        if X_engine is None:
+            X_engine = X
         key = f"refine{r}" if refine_sweep else "engine"
         out[key] = {"rel_err_x": float(np.linalg.norm(X - Xo) / np.linalg.norm(Xo)),
                     "rel_err_disp": float(np.linalg.norm(X - Xo) / max(np.linalg.norm(Xo - X0), 1e-30))}
@@ -295,6 +298,10 @@ def accuracy_vs_fp64(body, params, steps: int, refine_sweep: bool = False, ref_g
         X = X.astype(np.float64)
         out["reference_gpu"] = {"rel_err_x": float(np.linalg.norm(X - Xo) / np.linalg.norm(Xo)),
                                 "rel_err_disp": float(np.linalg.norm(X - Xo) / max(np.linalg.norm(Xo - X0), 1e-30))}
+        # the engine (first entry above) against the reference GPU path itself
+        out["engine_vs_reference_gpu"] = {
+            "rel_err_x": float(np.linalg.norm(X_engine - X) / np.linalg.norm(X)),
+            "rel_err_disp": float(np.linalg.norm(X_engine - X) / max(np.linalg.norm(X - X0), 1e-30))}
     return out
 
 
