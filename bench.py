@@ -54,8 +54,9 @@ WORKLOADS = {
         "workload": "pd_cholesky_batch512",
         "desc": "512 independent hex-grid bodies, dims uniform 4..24 per axis (seed 4), cells 1/16 m, E log-uniform "
                 "1e4..1e7, nu U[0.3,0.45], rho U[800,1200], top faces pinned, dt=1/120, per-body prefactored sparse "
-                "Cholesky (AMD), 10 iterations/step, one engine: 1 local launch + 1 solve launch (one CTA per body) "
-                "+ 1 vertex launch per iteration, CUDA graph per step",
+                "Cholesky (AMD), 10 iterations/step, one engine: per iteration 1 local launch over every body's tiles, "
+                "the solve (autotuned schedule: per-level launches over all bodies, or one CTA per body) and 1 "
+                "vertex launch, CUDA graph per step",
         "nbodies": 512, "iterations": 10, "solver": "cholesky",
     },
     "c5": {
