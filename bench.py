@@ -255,7 +255,7 @@ def run_reference_arm(args, body, params, scale=1.0):
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": WORKLOAD,
+        "config": dict(WORKLOAD, parallelism=f"replicas{world}" if world > 1 else "single"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1 if use_ref else cores, "kind": kind,
                          "sample": sample, "seconds": t_total},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

@@ -212,6 +212,14 @@ int pdgb_last_step_iterations(pdgb_engine* e, int* iterations);
 /* Waits for the engine's stream. */
 int pdgb_synchronize(pdgb_engine* e);
 
+/* Status of the steps run since the state was last set (pdgb_create,
+ * pdgb_upload_state, pdgb_reset): PDGB_ERR_NONFINITE once any step has ended
+ * with a non-finite position or velocity (the iteration left the finite
+ * range), else PDGB_OK.  The step epilogue sets a device word; this call
+ * waits for the stream and reads it.  The reference reports nothing here
+ * (SolverStep returns true unconditionally, pdSolver.cu:207). */
+int pdgb_last_step_status(pdgb_engine* e);
+
 /* Device timing for benchmarks (mode, default OFF):
  *   PDGB_TIMING_STEPS: pdgb_step brackets every step-graph launch with a
  *     pair of CUDA events on the engine's stream and does not wait;
@@ -521,15 +529,20 @@ int pdgb_render_surface(pdgb_engine* e, const uint32_t* tris, int num_tris, floa
  * fixed device array of about 8 MB inside this library, held by every GPU
  * that loads it until the process exits.
  *   - Limits: num_verts <= 32768 and num_tets <= 131072, else
- *     PDGB_ERR_UNSUPPORTED.  A tet with an out-of-range index or zero rest
- *     volume gives PDGB_ERR_BAD_MESH.
+ *     PDGB_ERR_UNSUPPORTED.  The mesh is checked on the device before the
+ *     first step: a tet with an out-of-range index, a zero or nearly zero
+ *     rest volume (a DmInv that float cannot hold) or a negative or
+ *     non-finite weight gives PDGB_ERR_BAD_MESH, and X and V are left as
+ *     they were.
  *   - All calls share that scratch array: calls that overlap on the GPU
  *     (other streams, other host threads) race; serialise them.  Each call
  *     recomputes or clears everything it reads from the scratch.
  *   - The first call on a device looks up the scratch's device address for
- *     that device; make it before any stream capture.
- *   - The call waits for its stream before returning (it reports mesh
- *     errors found on the device). */
+ *     that device; make it before any stream capture.  The address is kept
+ *     until the process exits: a cudaDeviceReset between calls is not
+ *     supported.
+ *   - The call waits for its stream twice: after the mesh check and before
+ *     returning. */
 typedef struct pdgb_noalloc_mesh {
     int num_verts;
     int num_tets;

@@ -7,11 +7,20 @@
 # drag selection, see below).  Test infrastructure only; reads the reference
 # sources where they lie and writes nothing outside oracle/_ref/.
 #
-# usage: build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# usage: build_ref.sh [REFERENCE_ROOT]
+#   The reference root is the argument, else $PDGB_REFERENCE_ROOT, else the
+#   place this container mounts it (/root/reference).  Where none of these
+#   exists (the GPU machines) the script builds nothing and exits 0.  The root
+#   used is recorded in oracle/_ref/REFERENCE_ROOT for the tests that read the
+#   reference's own asset files.
 set -euo pipefail
-R="${1:-/root/reference}"
+R="${1:-${PDGB_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
+if [ ! -d "$R/src/simulation/solver/projective" ]; then
+    echo "build_ref.sh: no reference sources at $R; oracle/_ref not built" >&2
+    exit 0
+fi
 mkdir -p "$OUT"
 CXX=(g++ -std=c++17 -O2 -ffp-contract=off -fPIC -w)
 INC=(-I"$HERE/refshim/include" -I"$R/src" -I"$R/src/simulation" -I"$R/src/simulation/solver"
@@ -80,3 +89,4 @@ fn_text() {  # fn_text FILE NAME: one template function definition, its template
 g++ -shared -fopenmp -o "$OUT/libref_pd.so.tmp" "$OUT/pdUtil.o" "$OUT/ref_harness.o" "$OUT/pd_oracle.o" \
     "$OUT/ref_scene.o" "$OUT/rigid.o" "$OUT/ref_ccd.o"
 mv "$OUT/libref_pd.so.tmp" "$OUT/libref_pd.so"
+printf "%s\n" "$(cd "$R" && pwd)" > "$OUT/REFERENCE_ROOT"

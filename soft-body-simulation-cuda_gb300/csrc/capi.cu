@@ -193,7 +193,13 @@ SceneArgs scene_args(pdgb_engine* e) {
     sc.mu_t = e->mu_t;
     sc.mu_n = e->mu_n;
     sc.ccd = e->ccd_on ? 1 : 0;
+    sc.nonfinite = e->st.p ? &e->st.p->nonfinite : nullptr;
     return sc;
+}
+
+// Clears the sticky non-finite status (the state was set again).
+void clear_nonfinite(pdgb_engine* e) {
+    PDGB_CUDA_TRY(cudaMemsetAsync(&e->st.p->nonfinite, 0, sizeof(int), e->stream));
 }
 
 // Collision detection + response after a step (PdSolver::Update,
@@ -951,6 +957,7 @@ int pdgb_upload_state(pdgb_engine* e, const float* X, const float* V, int memory
             throw Error{PDGB_ERR_INVALID_ARGUMENT, "bad memory kind"};
         }
         if (e->xt.p) launch_copy_state(e->nv, e->x.p, e->xt.p, e->stream);  // XTilde = X
+        clear_nonfinite(e);
         PDGB_CUDA_TRY(cudaGetLastError());
     });
 }
@@ -984,6 +991,7 @@ int pdgb_reset(pdgb_engine* e) {
         if (e->drag_w.p) PDGB_CUDA_TRY(cudaMemsetAsync(e->drag_w.p, 0, (size_t)e->nv * sizeof(float), e->stream));
         e->drag_on = false;
         PDGB_CUDA_TRY(cudaMemsetAsync(e->prev.p, 0, (size_t)e->nv * sizeof(float4), e->stream));
+        clear_nonfinite(e);
         PDGB_CUDA_TRY(cudaGetLastError());
         e->prepared = false;
         e->steps_run = 0;
@@ -1289,6 +1297,21 @@ int pdgb_last_step_iterations(pdgb_engine* e, int* iterations) {
 int pdgb_synchronize(pdgb_engine* e) {
     if (!e) return PDGB_ERR_INVALID_ARGUMENT;
     return guarded([&] { PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream)); });
+}
+
+int pdgb_last_step_status(pdgb_engine* e) {
+    if (!e) return PDGB_ERR_INVALID_ARGUMENT;
+    int flag = 0;
+    const int st = guarded([&] {
+        PDGB_CUDA_TRY(cudaMemcpyAsync(&flag, &e->st.p->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    });
+    if (st != PDGB_OK) return st;
+    if (flag) {
+        set_last_error(PDGB_ERR_NONFINITE, "a step ended with a non-finite position or velocity");
+        return PDGB_ERR_NONFINITE;
+    }
+    return PDGB_OK;
 }
 
 int pdgb_enable_kernel_timing(pdgb_engine* e, int mode) {

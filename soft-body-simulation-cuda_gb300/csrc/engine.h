@@ -172,6 +172,8 @@ struct SceneArgs {
     float mu_t, mu_n;
     int ccd;                  // collision handling on: the step writes XTilde only; X and the
                               // fixed-body correction follow the collision response
+    int* nonfinite;           // set to 1 when a vertex ends a step with a non-finite position or
+                              // velocity (sticky until the state is set again); may be null
 };
 
 struct VertexArgs {

@@ -11,6 +11,7 @@
 #include "engine.h"
 #include "pdl.cuh"
 #include "scene.cuh"
+#include "relax.cuh"
 #include "rotation.cuh"
 
 namespace pdgb {
@@ -207,15 +208,7 @@ void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_for
 }
 
 // ------------------------------------------------------- vertex kernels
-// 0.9 is a double literal in the reference's Chebyshev kernel (pdUtil.cu:221),
-// so 0.9*(x - s) + s is evaluated in double there.  Splitting 0.9 into a
-// float head and tail keeps the product exact to ~1e-15 without FP64 math.
-__device__ __forceinline__ float relax09(float nx, float s) {
-    const float d = nx - s;
-    constexpr float kHi = 0.9f;
-    constexpr float kLo = (float)(0.9 - (double)0.9f);
-    return fmaf(kHi, d, fmaf(kLo, d, s));
-}
+// (relax09: the 0.9 under-relaxation of pdUtil.cu:221, relax.cuh)
 
 template <int kMode>
 __device__ __forceinline__ void jacobi_vertex(const VertexArgs& a, int i, float omega) {

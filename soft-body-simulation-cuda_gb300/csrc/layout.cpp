@@ -252,6 +252,9 @@ void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const f
         for (int k = 0; k < 9; ++k) {
             L.dminv_d[9 * (size_t)i + k] = inv[k];
             const float v = (float)(g * inv[k]);
+            // a nearly flat tet has a finite double inverse that overflows float
+            if (!std::isfinite(inv[k]) || !std::isfinite(v))
+                throw Error{PDGB_ERR_BAD_MESH, "tet " + std::to_string(t) + " is too flat (its DmInv overflows float)"};
             if (k < 4) L.geo[4 * (size_t)i + k] = v;
             else if (k < 8) L.geo[np4 + 4 * (size_t)i + (k - 4)] = v;
             else L.geo[2 * np4 + 2 * (size_t)i] = v;

@@ -24,12 +24,18 @@
 //     needs is recomputed or cleared by that call;
 //   - the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) once for that device; make that first call
-//     before any stream capture.
+//     before any stream capture.  The address is kept for the life of the
+//     process, so a cudaDeviceReset between calls is not supported;
+//   - the mesh is checked on the device (tet indices, rest volumes, weights)
+//     before any step: a bad mesh returns PDGB_ERR_BAD_MESH with X and V
+//     untouched.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <mutex>
 
 #include "../../include/pdgb.h"
+#include "relax.cuh"
 #include "rotation.cuh"
 
 namespace pdgb {
@@ -60,7 +66,9 @@ struct NaScratch {
     float4* base;
     float4* coef;
     float* diag;
-    int* bad;       // set when a tet has an out-of-range index or zero volume
+    int* bad;       // set when a tet has an out-of-range index, no float-representable
+                    // DmInv (zero or nearly zero rest volume) or a negative or
+                    // non-finite weight
 };
 
 NaScratch carve(unsigned char* base) {
@@ -94,7 +102,8 @@ __global__ void na_tets(int nv, int nt, const uint32_t* __restrict__ tets, const
         for (int r = 0; r < 3; ++r) D[r][c] = (double)X0[3 * id[c] + r] - (double)X0[3 * i0 + r];
     const double det = D[0][0] * (D[1][1] * D[2][2] - D[1][2] * D[2][1]) - D[0][1] * (D[1][0] * D[2][2] - D[1][2] * D[2][0]) +
                        D[0][2] * (D[1][0] * D[2][1] - D[1][1] * D[2][0]);
-    if (det == 0.0) {
+    const float w = mu[t];
+    if (!(det != 0.0) || !isfinite(det) || !(w >= 0.f) || !isfinite(w)) {
         atomicExch(s.bad, 1);
         return;
     }
@@ -108,7 +117,15 @@ __global__ void na_tets(int nv, int nt, const uint32_t* __restrict__ tets, const
     inv[6] = (D[1][0] * D[2][1] - D[1][1] * D[2][0]) / det;
     inv[7] = (D[0][1] * D[2][0] - D[0][0] * D[2][1]) / det;
     inv[8] = (D[0][0] * D[1][1] - D[0][1] * D[1][0]) / det;
-    const double coef = fabs(det) / 6.0 * (double)mu[t];
+    const double coef = fabs(det) / 6.0 * (double)w;
+    // a nearly flat tet has a finite double inverse that overflows float:
+    // rejected like a flat one (the layout of pdgb_create does the same)
+    bool finite = isfinite((float)coef);
+    for (int k = 0; k < 9; ++k) finite = finite && isfinite((float)inv[k]);
+    if (!finite) {
+        atomicExch(s.bad, 1);
+        return;
+    }
     for (int k = 0; k < 9; ++k) s.geo[(size_t)k * kNaMaxTets + t] = (float)inv[k];
     s.geo[(size_t)9 * kNaMaxTets + t] = (float)coef;
     const uint32_t corner[4] = {i0, i1, i2, i3};
@@ -202,10 +219,7 @@ __global__ void na_vertex(int nv, const float* __restrict__ X0, float wpin, floa
     const float den = cf.x + cf.y;
     float n[3];
     const float sv[3] = {sn.x, sn.y, sn.z}, bv[3] = {bb.x, bb.y, bb.z};
-    for (int d = 0; d < 3; ++d) {
-        const float j = (bv[d] - cf.x * sv[d]) / den + sv[d];
-        n[d] = (float)(0.9 * (double)(j - sv[d]) + (double)sv[d]);
-    }
+    for (int d = 0; d < 3; ++d) n[d] = relax09((bv[d] - cf.x * sv[d]) / den + sv[d], sv[d]);
     if (read_prev) {
         const float4 p = s.prev[i];
         n[0] = (n[0] - p.x) * omega + p.x;
@@ -259,6 +273,13 @@ extern "C" int pdgb_step_noalloc(const pdgb_noalloc_mesh* mesh, const pdgb_param
     na_clear<<<vb, 256, 0, st>>>(nv, s);
     na_tets<<<tb, 256, 0, st>>>(nv, nt, mesh->tets, mesh->X0, mesh->mu, s);
     na_vertex_coef<<<vb, 256, 0, st>>>(nv, mesh->mass, mesh->dbc, p->dt, p->positional_weight, s);
+    // The mesh check is read back before the first step, so that a bad mesh
+    // leaves the caller's X and V untouched.
+    int hbad = 0;
+    if (cudaGetLastError() != cudaSuccess) return PDGB_ERR_CUDA;
+    if (cudaMemcpyAsync(&hbad, s.bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDGB_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return PDGB_ERR_CUDA;
+    if (hbad) return PDGB_ERR_BAD_MESH;
     const float dt_inv = 1.0f / p->dt;
     const float wpin = p->positional_weight * (dt_inv * dt_inv);
     const int n = p->num_iterations;
@@ -275,8 +296,6 @@ extern "C" int pdgb_step_noalloc(const pdgb_noalloc_mesh* mesh, const pdgb_param
         }
     }
     if (cudaGetLastError() != cudaSuccess) return PDGB_ERR_CUDA;
-    int hbad = 0;
-    if (cudaMemcpyAsync(&hbad, s.bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return PDGB_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return PDGB_ERR_CUDA;
-    return hbad ? PDGB_ERR_BAD_MESH : PDGB_OK;
+    return PDGB_OK;
 }

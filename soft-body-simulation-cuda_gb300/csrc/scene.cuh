@@ -78,6 +78,12 @@ __device__ __forceinline__ void finish_vertex(const SceneArgs& sc, int i, float4
     const float4 xo = sc.xt ? sc.xt[i] : x[i];
     float3 V = make_float3((q.x - xo.x) * dt_inv, (q.y - xo.y) * dt_inv, (q.z - xo.z) * dt_inv);
     if (drag_weight(sc, i) > 0.f) V = make_float3(0.f, 0.f, 0.f);
+    // The reference has no such check (SolverStep returns true, pdSolver.cu:207);
+    // a diverged step is reported through the engine's status word instead of
+    // leaving the caller with silent NaN / inf positions.
+    if (sc.nonfinite && !(isfinite(q.x) && isfinite(q.y) && isfinite(q.z) && isfinite(V.x) && isfinite(V.y) &&
+                          isfinite(V.z)))
+        *sc.nonfinite = 1;
     if (sc.ccd) {
         sc.xt[i] = make_float4(q.x, q.y, q.z, 0.f);
         v[i] = make_float4(V.x, V.y, V.z, 0.f);

@@ -46,6 +46,7 @@ struct StepState {
     int iterations;      // iterations run in the current step
     unsigned count;      // blocks that added their partial error sum
     float err_acc;       // sum of squared changes (float, as the reference)
+    int nonfinite;       // a step ended with a non-finite position or velocity (sticky)
 };
 
 struct CholVertexArgs {

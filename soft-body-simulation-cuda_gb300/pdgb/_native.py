@@ -234,6 +234,7 @@ SIGNATURES = {
     "pdgb_get_perf": (C.c_int, [C.c_void_p, C.POINTER(pdgb_perf)]),
     "pdgb_last_step_iterations": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "pdgb_synchronize": (C.c_int, [C.c_void_p]),
+    "pdgb_last_step_status": (C.c_int, [C.c_void_p]),
     "pdgb_enable_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_read_timing": (C.c_int, [C.c_void_p, C.POINTER(pdgb_timing)]),
     "pdgb_local_step_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),

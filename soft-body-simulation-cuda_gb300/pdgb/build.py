@@ -100,17 +100,36 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_reference_harness(force: bool = False) -> Path | None:
-    """Builds oracle/_ref from the reference's sources when they are present."""
+    """Builds oracle/_ref from the reference's sources when they are present
+    (the recipe oracle/build_ref.sh finds them: its argument,
+    $PDGB_REFERENCE_ROOT, or where this project's build container mounts
+    them; elsewhere it builds nothing)."""
     script = ORACLE_DIR / "build_ref.sh"
-    ref_root = Path(os.environ.get("PDGB_REFERENCE_ROOT", "/root/reference"))
-    if not ref_root.exists() or not script.exists():
+    if not script.exists():
         return None
     out = ORACLE_DIR / "_ref" / "libref_pd.so"
     deps = [script, ORACLE_DIR / "pd_oracle.cpp"] + sorted((ORACLE_DIR / "refshim").glob("*.*"))
     if not force and not _stale(out, [d for d in deps if d.exists()]):
         return out
-    _run(["bash", str(script), str(ref_root)], cwd=ORACLE_DIR)
+    args = ["bash", str(script)]
+    if os.environ.get("PDGB_REFERENCE_ROOT"):
+        args.append(os.environ["PDGB_REFERENCE_ROOT"])
+    _run(args, cwd=ORACLE_DIR)
     return out if out.exists() else None
+
+
+def reference_root() -> Path | None:
+    """Root of the reference's sources this checkout's oracle/_ref was built
+    from ($PDGB_REFERENCE_ROOT first), or None where they are absent."""
+    env = os.environ.get("PDGB_REFERENCE_ROOT")
+    if env and Path(env).is_dir():
+        return Path(env)
+    rec = ORACLE_DIR / "_ref" / "REFERENCE_ROOT"
+    if rec.exists():
+        p = Path(rec.read_text().strip())
+        if p.is_dir():
+            return p
+    return None
 
 
 def build_refgpu(force: bool = False) -> Path:

@@ -115,6 +115,18 @@ class PdSolver:
     def synchronize(self) -> None:
         N.check(self._lib.pdgb_synchronize(self._h), "pdgb_synchronize")
 
+    def step_status(self) -> int:
+        """PDGB_OK, or PDGB_ERR_NONFINITE once a step since the state was last
+        set ended with a non-finite position or velocity (waits for the GPU)."""
+        st = int(self._lib.pdgb_last_step_status(self._h))
+        if st not in (N.PDGB_OK, N.PDGB_ERR_NONFINITE):
+            N.check(st, "pdgb_last_step_status")
+        return st
+
+    def check_finite(self) -> None:
+        """Raises PdgbError(PDGB_ERR_NONFINITE) if the iteration left the finite range."""
+        N.check(self._lib.pdgb_last_step_status(self._h), "pdgb_last_step_status")
+
     # -- state
     def upload_state(self, X: np.ndarray, V: np.ndarray | None = None) -> None:
         X = np.ascontiguousarray(X, dtype=np.float32)

@@ -12,8 +12,13 @@ import numpy as np
 import pytest
 
 from pdgb import PdgbError, mesh, meshio
+from pdgb.build import reference_root
 
-REF_ASSETS = Path("/root/reference/assets")
+# the reference's asset files, where its sources are present (the root that
+# oracle/_ref was built from, or $PDGB_REFERENCE_ROOT); the tests that read
+# them skip elsewhere
+_REF = reference_root()
+REF_ASSETS = (_REF / "assets") if _REF is not None else Path("reference-assets-absent")
 
 
 def write_tetgen(tmp: Path, body, start=1, faces=None, comments=False):
