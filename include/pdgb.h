@@ -349,13 +349,35 @@ typedef struct pdgb_factor_info {
     int fwd_items;          /* GPU work items, forward pass                   */
     int bwd_items;          /* GPU work items, backward pass                  */
     double flops;           /* factorisation flops (approx.)                  */
-    double factor_ms;       /* host time of ordering + factorisation         */
+    double factor_ms;       /* wall time of ordering + symbolic analysis +    */
+                            /* numeric factorisation                          */
     int solve_launches;     /* kernel launches of one solve, current schedule */
-    int reserved;
+    int numeric_device;     /* where the numeric factorisation ran:           */
+                            /* PDGB_FACTOR_GPU or PDGB_FACTOR_HOST            */
+    double numeric_ms;      /* device time of the GPU numeric factorisation   */
+    long long pool_bytes;   /* FP64 front pool of the GPU factorisation       */
 } pdgb_factor_info;
 /* Factor statistics of a prepared engine on the Cholesky path (zeros
  * otherwise). */
 int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info);
+
+/* Where the one-time numeric factorisation of the system runs.  The
+ * reference factors on the GPU in FP32 (cusolverSpScsrcholFactor,
+ * cholesky.cu:152-157).  PDGB_FACTOR_GPU (default): FP64 supernodal
+ * multifrontal factorisation with the engine's own kernels, level by level
+ * of the elimination tree; PDGB_FACTOR_HOST: the same factorisation in FP64
+ * on the host (OpenMP).  The ordering and symbolic analysis run on the host
+ * in both.  The distributed-shared-memory solve (PDGB_SOLVE_DSM) stages the
+ * factor from host memory and always uses the host factorisation.  Takes
+ * effect at the next prepare. */
+#define PDGB_FACTOR_GPU 0
+#define PDGB_FACTOR_HOST 1
+int pdgb_set_factor_device(pdgb_engine* e, int device);
+
+/* Copies the FP32 M_s blocks of the prepared factor (m_entries floats, see
+ * pdgb_factor_info) to host memory; capacity in floats.  Waits for the
+ * stream. */
+int pdgb_get_factor_blocks(pdgb_engine* e, float* out, long long capacity);
 
 int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params, int ordering, const double* b,
                            double* x, pdgb_factor_info* info);

@@ -72,7 +72,10 @@ struct pdgb_engine {
     DBuf<float4> bsave, dx;
     int solve_req = PDGB_SOLVE_AUTO;  // requested solve schedule
     int solve_mode = PDGB_SOLVE_LEVELS;  // schedule in use (decided at prepare)
-    double factor_ms = 0.0;
+    int factor_req = PDGB_FACTOR_GPU;    // where the numeric factorisation runs
+    int factor_dev = PDGB_FACTOR_GPU;    // where it ran for the current factor
+    double factor_ms = 0.0, numeric_ms = 0.0;
+    long long pool_bytes = 0;
     // scene terms: drag and fixed rigid bodies
     bool drag_on = false;
     DBuf<float> drag_w;
@@ -400,7 +403,7 @@ SparseSym engine_system(const HostLayout& L) {
 // dominates and one cluster (a single body) or one CTA per body (a batch)
 // walks the whole tree instead.
 int choose_solve_mode(const pdgb_engine* e) {
-    const bool small = e->chol.mval.size() <= kCtaSolveMaxEntries;
+    const bool small = (size_t)e->chol.mval_size <= kCtaSolveMaxEntries;
     const int m = e->solve_req;
     if (m == PDGB_SOLVE_DSM && !e->dsm.ok)
         throw Error{PDGB_ERR_UNSUPPORTED, "the factor does not fit the shared memory of one cluster (DSM solve)"};
@@ -410,11 +413,14 @@ int choose_solve_mode(const pdgb_engine* e) {
 }
 
 void prepare_cholesky(pdgb_engine* e) {
+    // the distributed-shared-memory solve stages the factor from host memory
+    const int dev = e->solve_req == PDGB_SOLVE_DSM ? PDGB_FACTOR_HOST : e->factor_req;
     if (e->chol_ordering == e->ordering && e->chol_dt == e->prm.dt && e->chol_pw == e->prm.positional_weight &&
-        e->chol.n == e->nv) {
+        e->chol.n == e->nv && e->factor_dev == dev) {
         e->solve_mode = choose_solve_mode(e);
         return;  // the system matrix depends only on the mesh, dt and the pin weight
     }
+    const bool gpu = dev == PDGB_FACTOR_GPU;
     auto t0 = std::chrono::steady_clock::now();
     SparseSym K;
     if (e->nbodies == 1) K = engine_system(e->L);
@@ -428,13 +434,26 @@ void prepare_cholesky(pdgb_engine* e) {
         std::vector<double> mdt2(e->nv);
         for (int i = 0; i < e->nv; ++i) mdt2[i] = (double)e->L.coef[i].x;
         cholesky_factor_bodies(e->nbodies, e->L.body_ivstart, e->L.body_itstart, e->L.tets_int.data(),
-                               e->L.dminv_d.data(), e->L.coef_d.data(), mdt2, e->ordering, xyz.data(), e->chol);
+                               e->L.dminv_d.data(), e->L.coef_d.data(), mdt2, e->ordering, xyz.data(), e->chol,
+                               gpu);
     } else {
-        cholesky_factor(K, e->ordering, xyz.data(), e->chol);
+        cholesky_factor(K, e->ordering, xyz.data(), e->chol, kBwdChunkRows, gpu);
     }
-    e->factor_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     cudaStream_t s = e->stream;
     const CholFactor& f = e->chol;
+    e->numeric_ms = 0.0;
+    e->pool_bytes = 0;
+    if (gpu) {
+        // FP64 numeric factorisation on the GPU, straight into the M_s blocks
+        e->ch_mval.alloc((size_t)std::max<int64_t>(f.mval_size, 1));
+        e->numeric_ms = gpu_factor(f, e->ch_mval.p, s);
+        e->pool_bytes = (long long)f.fp.pool * (long long)sizeof(double);
+        e->chol.fp = FrontPlan();  // the plan is not needed after the factorisation
+    } else {
+        e->ch_mval.upload(f.mval, s);
+    }
+    e->factor_dev = dev;
+    e->factor_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     e->ch_fwd.upload(f.fwd_items, s);
     e->ch_bwd.upload(f.bwd_items, s);
     e->ch_fwdb.upload(f.fwd_blocks, s);
@@ -445,7 +464,6 @@ void prepare_cholesky(pdgb_engine* e) {
     e->ch_zstage.upload(f.zstage, s);
     e->ch_zbuf.alloc((size_t)std::max<int64_t>(f.zrows, 1));
     e->ch_rows.upload(f.rows, s);
-    e->ch_mval.upload(f.mval, s);
     std::vector<int4> lv(f.levels.size());
     for (size_t i = 0; i < lv.size(); ++i)
         lv[i] = make_int4(f.levels[i].fwd_begin, f.levels[i].fwd_end, f.levels[i].bwd_begin, f.levels[i].bwd_end);
@@ -1448,7 +1466,7 @@ int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info) {
     if (e->prm.solver != PDGB_SOLVER_CHOLESKY || e->chol.n != e->nv) return PDGB_OK;
     const CholFactor& f = e->chol;
     info->nnz_L = f.nnz_L;
-    info->m_entries = (long long)f.mval.size();
+    info->m_entries = (long long)f.mval_size;
     info->num_supernodes = f.nsuper;
     info->num_levels = f.nlevels;
     info->fwd_items = (int)(f.fwd_items.size() / kItemInts);
@@ -1456,7 +1474,34 @@ int pdgb_get_factor_info(pdgb_engine* e, pdgb_factor_info* info) {
     info->flops = f.flops;
     info->factor_ms = e->factor_ms;
     info->solve_launches = solve_launches(e);
+    info->numeric_device = e->factor_dev;
+    info->numeric_ms = e->numeric_ms;
+    info->pool_bytes = e->pool_bytes;
     return PDGB_OK;
+}
+
+int pdgb_set_factor_device(pdgb_engine* e, int device) {
+    if (!e || (device != PDGB_FACTOR_GPU && device != PDGB_FACTOR_HOST)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or factor device");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (device != e->factor_req) {
+        e->factor_req = device;
+        e->prepared = false;
+    }
+    return PDGB_OK;
+}
+
+int pdgb_get_factor_blocks(pdgb_engine* e, float* out, long long capacity) {
+    if (!e || !out || capacity < 0) return PDGB_ERR_INVALID_ARGUMENT;
+    return guarded([&] {
+        if (e->prm.solver != PDGB_SOLVER_CHOLESKY || e->chol.n != e->nv || !e->ch_mval.p)
+            throw Error{PDGB_ERR_INVALID_ARGUMENT, "no prepared Cholesky factor"};
+        const long long n = (long long)e->chol.mval_size;
+        if (capacity < n) throw Error{PDGB_ERR_INVALID_ARGUMENT, "capacity below the factor's m_entries"};
+        PDGB_CUDA_TRY(cudaMemcpyAsync(out, e->ch_mval.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+        PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
+    });
 }
 
 int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params, int ordering, const double* b,
@@ -1483,7 +1528,7 @@ int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params
         const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         if (info) {
             info->nnz_L = f.nnz_L;
-            info->m_entries = (long long)f.mval.size();
+            info->m_entries = (long long)f.mval_size;
             info->num_supernodes = f.nsuper;
             info->num_levels = f.nlevels;
             info->fwd_items = (int)(f.fwd_items.size() / kItemInts);
@@ -1491,7 +1536,9 @@ int pdgb_host_factor_check(const pdgb_mesh_desc* mesh, const pdgb_params* params
             info->flops = f.flops;
             info->factor_ms = ms;
             info->solve_launches = 0;
-            info->reserved = 0;
+            info->numeric_device = PDGB_FACTOR_HOST;
+            info->numeric_ms = 0.0;
+            info->pool_bytes = 0;
         }
         if (b && x) {
             const int nv = L.nv;

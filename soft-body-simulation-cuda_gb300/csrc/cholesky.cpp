@@ -6,7 +6,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <numeric>
+#include <set>
 #include <string>
 
 #include "engine.h"
@@ -407,7 +409,8 @@ bool partial_cholesky(double* F, int m, int k) {
 
 }  // namespace
 
-void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out, int bwd_chunk_rows) {
+void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out, int bwd_chunk_rows,
+                     bool gpu_numeric, bool finish_plan) {
     const int n = K.n;
     out = CholFactor();
     out.n = n;
@@ -556,15 +559,56 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
     }
     out.moff[ns] = mtot;
     out.roff[ns] = (int)rtot;
-    out.mval.assign(mtot, 0.f);
+    out.mval_size = mtot;
     out.rows.resize(rtot);
     for (int s = 0; s < ns; ++s)
         for (int q = 0; q < out.sm[s]; ++q) out.rows[out.roff[s] + q] = perm[sstruct[s][q]];
-    std::vector<std::vector<double>> upd(ns);  // update matrices (lower, column major)
     std::vector<int> relpos(n, -1);
     double flops = 0.0;
+    if (gpu_numeric) {
+        // The numeric factorisation is left to the GPU (factor.cu): record
+        // where every entry of K lands in its supernode's front and where
+        // every row of a child's Schur complement lands in its parent's.
+        FrontPlan& P = out.fp;
+        P.on = true;
+        P.parent = sparent;
+        P.kptr.assign(ns + 1, 0);
+        P.rel_ptr.assign(ns + 1, 0);
+        for (int s = 0; s < ns; ++s) {
+            const int k = out.sk[s], m = out.sm[s], f = sfirst[s];
+            if ((int64_t)m * m > (int64_t)INT32_MAX)
+                throw Error{PDGB_ERR_UNSUPPORTED, "supernode front too large for the GPU factorisation"};
+            const std::vector<int>& st = sstruct[s];
+            for (int q = 0; q < m; ++q) relpos[st[q]] = q;
+            for (int jj = 0; jj < k; ++jj) {
+                const int v = perm[f + jj];
+                for (int64_t e = K.p[v]; e < K.p[v + 1]; ++e) {
+                    const int i = iperm[K.i[e]];
+                    if (i < f + jj) continue;
+                    P.kpos.push_back(jj * m + relpos[i]);
+                    P.kval.push_back(K.x[e]);
+                }
+            }
+            P.kptr[s + 1] = (int)P.kpos.size();
+            for (int jj = 0; jj < k; ++jj) flops += (double)(m - jj) * (m - jj);
+            for (int q = 0; q < m; ++q) relpos[st[q]] = -1;
+        }
+        for (int s = 0; s < ns; ++s) {
+            const int p = sparent[s];
+            if (p >= 0) {
+                const std::vector<int>& sp = sstruct[p];
+                for (int q = 0; q < out.sm[p]; ++q) relpos[sp[q]] = q;
+                for (int q = out.sk[s]; q < out.sm[s]; ++q) P.rel.push_back(relpos[sstruct[s][q]]);
+                for (int q = 0; q < out.sm[p]; ++q) relpos[sp[q]] = -1;
+            }
+            P.rel_ptr[s + 1] = (int)P.rel.size();
+        }
+    } else {
+        out.mval.assign(mtot, 0.f);
+    }
+    std::vector<std::vector<double>> upd(ns);  // update matrices (lower, column major)
     std::vector<double> F, Linv;
-    for (int s = 0; s < ns; ++s) {
+    for (int s = 0; s < ns && !gpu_numeric; ++s) {
         const int k = out.sk[s], m = out.sm[s], f = sfirst[s];
         const std::vector<int>& st = sstruct[s];
         for (int q = 0; q < m; ++q) relpos[st[q]] = q;
@@ -711,11 +755,116 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
     out.body_level = {0, nl};
     out.body_order = {0};
     out.step_levels = out.levels;
+    if (gpu_numeric && finish_plan) finish_front_plan(out);
+}
+
+int64_t front_doubles(const CholFactor& f, int s) {
+    const int64_t m = f.sm[s], k = f.sk[s];
+    return m * m + m * k;
+}
+
+void finish_front_plan(CholFactor& out) {
+    FrontPlan& P = out.fp;
+    const int ns = out.nsuper;
+    // children of each supernode, in supernode order
+    P.child_ptr.assign(ns + 1, 0);
+    for (int s = 0; s < ns; ++s)
+        if (P.parent[s] >= 0) P.child_ptr[P.parent[s] + 1]++;
+    for (int s = 0; s < ns; ++s) P.child_ptr[s + 1] += P.child_ptr[s];
+    P.child.assign(P.child_ptr[ns], 0);
+    {
+        std::vector<int> fill(P.child_ptr.begin(), P.child_ptr.end() - 1);
+        for (int s = 0; s < ns; ++s)
+            if (P.parent[s] >= 0) P.child[fill[P.parent[s]]++] = s;
+    }
+    // supernodes by level (levels from the leaves; a batch's bodies together)
+    int nl = 0;
+    for (int s = 0; s < ns; ++s) nl = std::max(nl, out.level[s] + 1);
+    P.lvl_ptr.assign(nl + 1, 0);
+    for (int s = 0; s < ns; ++s) P.lvl_ptr[out.level[s] + 1]++;
+    for (int L = 0; L < nl; ++L) P.lvl_ptr[L + 1] += P.lvl_ptr[L];
+    P.lvl_sn.assign(ns, 0);
+    {
+        std::vector<int> fill(P.lvl_ptr.begin(), P.lvl_ptr.end() - 1);
+        for (int s = 0; s < ns; ++s) P.lvl_sn[fill[out.level[s]]++] = s;
+    }
+    // Front pool, best fit: the fronts of level L are placed while their
+    // children's fronts still hold the Schur complements they pass up; the
+    // children's memory is released once level L is placed.
+    P.foff.assign(ns, 0);
+    P.max_m = 0;
+    std::set<std::pair<int64_t, int64_t>> by_size;  // (size, offset) of the free blocks
+    std::map<int64_t, int64_t> by_off;              // offset -> size of a free block
+    int64_t top = 0;
+    auto take = [&](int64_t need) -> int64_t {
+        auto it = by_size.lower_bound({need, INT64_MIN});
+        if (it == by_size.end()) {
+            const int64_t o = top;
+            top += need;
+            return o;
+        }
+        const int64_t size = it->first, o = it->second;
+        by_size.erase(it);
+        by_off.erase(o);
+        if (size > need) {
+            by_size.emplace(size - need, o + need);
+            by_off.emplace(o + need, size - need);
+        }
+        return o;
+    };
+    auto give = [&](int64_t o, int64_t size) {
+        auto next = by_off.lower_bound(o);
+        if (next != by_off.end() && next->first == o + size) {  // merge with the following block
+            by_size.erase({next->second, next->first});
+            size += next->second;
+            next = by_off.erase(next);
+        }
+        if (next != by_off.begin()) {  // merge with the preceding block
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == o) {
+                by_size.erase({prev->second, prev->first});
+                o = prev->first;
+                size += prev->second;
+                by_off.erase(prev);
+            }
+        }
+        if (o + size == top) {  // the block ends the pool: shrink it
+            top = o;
+            return;
+        }
+        by_off.emplace(o, size);
+        by_size.emplace(size, o);
+    };
+    int64_t peak = 0;
+    for (int L = 0; L < nl; ++L) {
+        for (int q = P.lvl_ptr[L]; q < P.lvl_ptr[L + 1]; ++q) {
+            const int s = P.lvl_sn[q];
+            const int64_t m = out.sm[s];
+            P.max_m = std::max(P.max_m, (int)m);
+            P.foff[s] = take(front_doubles(out, s));
+        }
+        peak = std::max(peak, top);
+        // level L is assembled: its children's fronts are consumed, and its
+        // roots need their fronts only during this level
+        for (int q = P.lvl_ptr[L]; q < P.lvl_ptr[L + 1]; ++q) {
+            const int s = P.lvl_sn[q];
+            for (int c = P.child_ptr[s]; c < P.child_ptr[s + 1]; ++c) {
+                const int ch = P.child[c];
+                give(P.foff[ch], front_doubles(out, ch));
+            }
+        }
+        for (int q = P.lvl_ptr[L]; q < P.lvl_ptr[L + 1]; ++q) {
+            const int s = P.lvl_sn[q];
+            if (P.parent[s] < 0) give(P.foff[s], front_doubles(out, s));
+        }
+    }
+    P.pool = peak;
 }
 
 void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const std::vector<int>& tstart,
                             const uint32_t* tets4, const double* dminv, const double* coef,
-                            const std::vector<double>& mdt2, int ordering, const float* xyz, CholFactor& out) {
+                            const std::vector<double>& mdt2, int ordering, const float* xyz, CholFactor& out,
+                            bool gpu_numeric) {
     std::vector<CholFactor> fs(nbodies);
     std::vector<int> order(nbodies);
     std::iota(order.begin(), order.end(), 0);
@@ -732,7 +881,7 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
             for (size_t i = 0; i < lt.size(); ++i) lt[i] = tets4[4 * (size_t)t0 + i] - (uint32_t)v0;
             std::vector<double> md(mdt2.begin() + v0, mdt2.begin() + v0 + nvb);
             SparseSym Kb = assemble_system(nvb, ntb, lt.data(), dminv + 9 * (size_t)t0, coef + t0, md);
-            cholesky_factor(Kb, ordering, xyz ? xyz + 3 * (size_t)v0 : nullptr, fs[b], 0);
+            cholesky_factor(Kb, ordering, xyz ? xyz + 3 * (size_t)v0 : nullptr, fs[b], 0, gpu_numeric, false);
         } catch (const Error& e) {
             failed[b] = e.status;
         } catch (...) {
@@ -766,6 +915,23 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         }
         out.nsuper += f.nsuper;
         out.mval.insert(out.mval.end(), f.mval.begin(), f.mval.end());
+        if (gpu_numeric) {
+            FrontPlan& P = out.fp;
+            const FrontPlan& Q = f.fp;
+            if (P.kptr.empty()) {
+                P.kptr.assign(1, 0);
+                P.rel_ptr.assign(1, 0);
+            }
+            const int kb = (int)P.kpos.size(), rb = (int)P.rel.size();
+            for (int s = 0; s < f.nsuper; ++s) {
+                P.parent.push_back(Q.parent[s] >= 0 ? Q.parent[s] + sbase : -1);
+                P.kptr.push_back(Q.kptr[s + 1] + kb);
+                P.rel_ptr.push_back(Q.rel_ptr[s + 1] + rb);
+            }
+            P.kpos.insert(P.kpos.end(), Q.kpos.begin(), Q.kpos.end());
+            P.kval.insert(P.kval.end(), Q.kval.begin(), Q.kval.end());
+            P.rel.insert(P.rel.end(), Q.rel.begin(), Q.rel.end());
+        }
         for (int r : f.rows) out.rows.push_back(r + v0);
         auto shift = [&](std::vector<int>& dst, const std::vector<int>& src, bool zfield = false) {
             const int base_item = (int)(dst.size() / kItemInts);
@@ -801,7 +967,7 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
             shift(bbw[L], slice(f.bwd_small, lv.bwdw_begin, lv.bwdw_end));
         }
         out.body_level.push_back((int)out.levels.size());
-        mbase += (int64_t)f.mval.size();
+        mbase += f.mval_size;
         rbase += (int64_t)f.rows.size();
         zbase += f.zrows;
         out.zrows += f.zrows;
@@ -809,7 +975,11 @@ void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const s
         out.K.n = 0;  // per-body systems are not kept
         f = CholFactor();  // release the per-body copy
     }
-    (void)sbase;
+    out.mval_size = mbase;
+    if (gpu_numeric) {
+        out.fp.on = true;
+        finish_front_plan(out);
+    }
     for (size_t L = 0; L < bfb.size(); ++L) {
         SolveLevel lv{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         auto put = [&](std::vector<int>& dst, std::vector<int>& src, int& b0, int& b1) {

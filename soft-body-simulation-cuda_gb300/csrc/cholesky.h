@@ -109,6 +109,29 @@ constexpr int kStageRows = 128;
 constexpr int kBwdChunkRows = PDGB_BWD_CHUNK_ROWS;
 constexpr int kBlockMinRows = PDGB_BLOCK_MIN_ROWS;
 
+// Numeric factorisation on the GPU (factor.cu): everything the device needs
+// beyond the symbolic structure of CholFactor.  Each supernode s has a dense
+// front F_s (m_s x m_s, column major, FP64) in one pool, followed by an
+// m_s x k_s FP64 block for M_s; F_s receives the entries of K in its pivot
+// columns and the Schur complements of its children (extend-add), is
+// factored over its first k_s columns, and its own Schur complement
+// F_s[k_s:, k_s:] is then added into its parent's front.  Fronts live from
+// their level until their parent's level is assembled, and the pool reuses
+// the memory of the fronts that are done.
+struct FrontPlan {
+    bool on = false;                   // mval is left to the GPU
+    int64_t pool = 0;                  // doubles in the front pool
+    int max_m = 0;                     // largest front
+    std::vector<int64_t> foff;         // [nsuper] front offset in the pool
+    std::vector<int> parent;           // [nsuper] parent supernode, -1 for a root
+    std::vector<int> child_ptr, child; // children of each supernode ([nsuper + 1] / [nsuper])
+    std::vector<int> rel_ptr, rel;     // rows of s past its pivots, as positions in its parent's row list
+    std::vector<int> kptr;             // [nsuper + 1] entries of K in the pivot columns of s
+    std::vector<int> kpos;             // position of the entry in F_s (column * m_s + row)
+    std::vector<double> kval;
+    std::vector<int> lvl_ptr, lvl_sn;  // supernodes by level (from the leaves, all bodies together)
+};
+
 struct CholFactor {
     int n = 0;
     long long nnz_L = 0;             // nnz of the scalar factor (incl. diagonal)
@@ -142,6 +165,8 @@ struct CholFactor {
     long long zeros = 0;             // explicit zeros stored by amalgamated supernodes
     // FP64 copy of K for refinement residuals (CSR over vertex ids)
     SparseSym K;
+    int64_t mval_size = 0;           // FP32 entries of the M_s blocks (= mval.size() when factored on the host)
+    FrontPlan fp;                    // numeric factorisation left to the GPU (fp.on)
 };
 
 // Plan of the distributed-shared-memory solve of a single body: an 8-CTA
@@ -176,8 +201,12 @@ void build_dsm_plan(const CholFactor& f, int ctas, int warps_per_cta, size_t max
 // dissection (xyz required).  Throws Error(PDGB_ERR_NOT_SPD) if a pivot is
 // not positive.  bwd_chunk_rows: rows per backward block item (0: whole
 // columns).
+// gpu_numeric: stop after the symbolic analysis and fill out.fp for the
+// GPU factorisation (factor.cu) instead of computing mval on the host;
+// finish_plan: complete it (finish_front_plan) -- a batch completes the
+// combined plan of its bodies instead.
 void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out,
-                     int bwd_chunk_rows = kBwdChunkRows);
+                     int bwd_chunk_rows = kBwdChunkRows, bool gpu_numeric = false, bool finish_plan = true);
 
 // Factors the block-diagonal system of independent bodies, one block per
 // body (vertex range vstart[b]..vstart[b+1], tets tstart[b]..tstart[b+1] in
@@ -186,7 +215,22 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
 // per body.
 void cholesky_factor_bodies(int nbodies, const std::vector<int>& vstart, const std::vector<int>& tstart,
                             const uint32_t* tets4, const double* dminv, const double* coef,
-                            const std::vector<double>& mdt2, int ordering, const float* xyz, CholFactor& out);
+                            const std::vector<double>& mdt2, int ordering, const float* xyz, CholFactor& out,
+                            bool gpu_numeric = false);
+
+// Doubles of the pool that supernode s takes: its front and its M_s block.
+int64_t front_doubles(const CholFactor& f, int s);
+
+// Numeric factorisation of the plan f.fp on the GPU (factor.cu): writes the
+// FP32 M_s blocks (f.mval_size floats, device memory) and returns the device
+// time in ms.  Waits for the stream.  Throws Error(PDGB_ERR_NOT_SPD) when a
+// pivot is not positive.
+double gpu_factor(const CholFactor& f, float* mval, void* stream);
+
+// Completes out.fp once the supernodes of all bodies are in place: children
+// lists, supernodes by level, and the front pool (best-fit reuse of the
+// fronts whose parents are assembled).
+void finish_front_plan(CholFactor& out);
 
 // Applies the factor on the host exactly as the GPU work items do
 // (forward by levels with M_s, backward by levels), in double: x = K^-1 b

@@ -37,6 +37,8 @@ PDGB_SOLVE_CTA = 1
 PDGB_SOLVE_CLUSTER = 2
 PDGB_SOLVE_LEVELS = 3
 PDGB_SOLVE_DSM = 4
+PDGB_FACTOR_GPU = 0
+PDGB_FACTOR_HOST = 1
 PDGB_TIMING_OFF = 0
 PDGB_TIMING_STEPS = 1
 PDGB_TIMING_KERNELS = 2
@@ -146,7 +148,9 @@ class pdgb_factor_info(C.Structure):
         ("flops", C.c_double),
         ("factor_ms", C.c_double),
         ("solve_launches", C.c_int),
-        ("reserved", C.c_int),
+        ("numeric_device", C.c_int),
+        ("numeric_ms", C.c_double),
+        ("pool_bytes", C.c_longlong),
     ]
 
 
@@ -252,6 +256,8 @@ SIGNATURES = {
     "pdgb_version": (C.c_char_p, []),
     "pdgb_set_ordering": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_get_factor_info": (C.c_int, [C.c_void_p, C.POINTER(pdgb_factor_info)]),
+    "pdgb_set_factor_device": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_get_factor_blocks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
     "pdgb_set_rotation": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_host_factor_check": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_params), C.c_int, C.c_void_p,
                                          C.c_void_p, C.POINTER(pdgb_factor_info)]),

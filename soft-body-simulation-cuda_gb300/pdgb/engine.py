@@ -222,6 +222,18 @@ class PdSolver:
         N.check(self._lib.pdgb_get_factor_info(self._h, C.byref(f)), "pdgb_get_factor_info")
         return {k: getattr(f, k) for k, _ in f._fields_}
 
+    def set_factor_device(self, device: int) -> None:
+        """PDGB_FACTOR_GPU (default) or PDGB_FACTOR_HOST: where the one-time FP64
+        numeric factorisation of the Cholesky path runs."""
+        N.check(self._lib.pdgb_set_factor_device(self._h, int(device)), "pdgb_set_factor_device")
+
+    def factor_blocks(self) -> np.ndarray:
+        """The FP32 M_s blocks of the prepared factor (host copy)."""
+        n = self.factor_info()["m_entries"]
+        out = np.empty(max(int(n), 1), np.float32)
+        N.check(self._lib.pdgb_get_factor_blocks(self._h, out.ctypes.data, int(out.size)), "pdgb_get_factor_blocks")
+        return out[: int(n)]
+
     def last_step_iterations(self) -> int:
         it = C.c_int()
         N.check(self._lib.pdgb_last_step_iterations(self._h, C.byref(it)), "pdgb_last_step_iterations")

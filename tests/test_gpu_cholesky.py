@@ -172,3 +172,45 @@ def test_dsm_solve_refuses_a_factor_too_large():
         e.set_solve_mode(N.PDGB_SOLVE_DSM)
         with pytest.raises(PdgbError):
             e.update(1)
+
+
+@pytest.mark.parametrize("case", ["c1", "hetero14", "batch"])
+def test_gpu_factor_matches_host_factor(case):
+    """The one-time FP64 numeric factorisation on the GPU (default) and on the
+    host give the same M_s blocks (both FP64, rounded to FP32: a few entries
+    may differ in their last float bit) and the same steps."""
+    if case == "c1":
+        body = mesh.make_grid_body(10, 10, 10, young=1e5, poisson=0.4)
+    elif case == "hetero14":
+        body = mesh.cube_c3(n=14, seed=5)
+    else:
+        body = mesh.batch_c4(nbodies=9, seed=11, lo=2, hi=9)
+    params = SolverParams(num_iterations=10, solver=1)
+    out = {}
+    for dev in (N.PDGB_FACTOR_GPU, N.PDGB_FACTOR_HOST):
+        with PdSolver(body, params) as e:
+            e.set_factor_device(dev)
+            e.update(3)
+            info = e.factor_info()
+            assert info["numeric_device"] == dev
+            out[dev] = (e.factor_blocks(), e.download_state()[0], info)
+    Mg, Xg, ig = out[N.PDGB_FACTOR_GPU]
+    Mh, Xh, ih = out[N.PDGB_FACTOR_HOST]
+    assert Mg.shape == Mh.shape and ig["m_entries"] == ih["m_entries"]
+    assert ig["numeric_ms"] > 0 and ig["pool_bytes"] > 0
+    assert np.isfinite(Mg).all()
+    scale = np.abs(Mh).max()
+    assert np.abs(Mg - Mh).max() <= 1e-6 * scale, np.abs(Mg - Mh).max() / scale
+    rel = np.abs(Mg.astype(np.float64) - Mh) / np.maximum(np.abs(Mh), 1e-30 * scale)
+    assert (rel > 2.5e-7).mean() < 1e-3
+    assert rel_l2(Xg, Xh) < 1e-6
+
+
+def test_gpu_factor_reports_not_positive_definite():
+    body = mesh.make_grid_body(2, 2, 2)
+    body.mass = -np.abs(body.mass) * 1e9  # negative inertia term dominates
+    params = SolverParams(num_iterations=4, solver=1)
+    with PdSolver(body, params) as e:
+        with pytest.raises(PdgbError) as err:
+            e.update(1)
+        assert err.value.status == N.PDGB_ERR_NOT_SPD
