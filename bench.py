@@ -63,9 +63,10 @@ WORKLOADS = {
         "workload": "pd_serving_poisson200",
         "desc": "request stream: Poisson arrivals 200 req/s over the arrival window, each a near-cubic hex-grid body "
                 "with tets log-uniform 1e3..3e5 (drawn from a seeded pool of 48 bodies), material as the batch "
-                "workload, K steps uniform 10..200, dt=1/120, 10 Jacobi+Chebyshev iterations; continuous batching, "
-                "admission by an 8 GiB HBM budget",
-        "rate": 200.0, "iterations": 10, "solver": "jacobi",
+                "workload, K steps uniform 10..200, dt=1/120, 10 iterations of the prefactored sparse Cholesky solve "
+                "(each request's FP64 factor computed on the GPU at admission and resident with its mesh and state); "
+                "continuous batching, admission by an 8 GiB HBM budget",
+        "rate": 200.0, "iterations": 10, "solver": "cholesky",
     },
     "c3": {
         "workload": "pd_cholesky_hetero40",
@@ -378,7 +379,8 @@ def plain_drop_in(bodies, params, steps: int, flush) -> dict:
             "sample": f"every 8th body of the batch ({len(bodies)} bodies), one engine each, run one after another"}
 
 
-def run_serving(args):
+def run_serving(args, window: float, rate: float = 0.0, solver: str = "", cache: bool = True,
+                print_line: bool = True) -> dict:
     """Serving workload: wall-clock request arrivals into the server."""
     import math
 
@@ -390,25 +392,37 @@ def run_serving(args):
 
     torch.cuda.set_device(local)
     wl = dict(WORKLOADS["c5"])
-    if args.rate > 0:
-        wl["rate"] = args.rate
-        wl["workload"] += f"_rate{args.rate:g}"
-        wl["desc"] = wl["desc"].replace("200 req/s", f"{args.rate:g} req/s", 1)
+    if rate > 0 and rate != wl["rate"]:
+        wl["rate"] = rate
+        wl["workload"] += f"_rate{rate:g}"
+        wl["desc"] = wl["desc"].replace("200 req/s", f"{rate:g} req/s", 1)
+    if solver and solver != wl["solver"]:
+        wl["solver"] = solver
+        wl["workload"] += f"_{solver}"
+        wl["desc"] = wl["desc"].replace(
+            "10 iterations of the prefactored sparse Cholesky solve (each request's FP64 factor computed on the GPU "
+            "at admission and resident with its mesh and state)", "10 Jacobi+Chebyshev iterations (rho=0.9995)")
+    if not cache:
+        wl["workload"] += "_nocache"
+        wl["cache"] = "off: every request builds its layout and factor"
+    else:
+        wl["cache"] = "layouts and factors of the 48 pool meshes kept after their first request"
     rng = np.random.default_rng(5)
     pool = [mesh.request_body(math.exp(rng.uniform(math.log(1e3), math.log(3e5))), rng) for _ in range(48)]
-    window = args.window
     n_req = int(rng.poisson(wl["rate"] * window))
     arrivals = np.sort(rng.uniform(0.0, window, size=n_req))
     picks = rng.integers(0, len(pool), size=n_req)
     ksteps = rng.integers(10, 201, size=n_req)
-    params = SolverParams(num_iterations=wl["iterations"], rho=0.9995, solver=0)
+    params = SolverParams(num_iterations=wl["iterations"], rho=0.9995, solver=1 if wl["solver"] == "cholesky" else 0)
     offered = float(sum(pool[p].num_tets * int(k) for p, k in zip(picks, ksteps)) * params.num_iterations / window)
-    srv = PdServer(params, hbm_budget_bytes=8 << 30)
+    srv = PdServer(params, hbm_budget_bytes=8 << 30, cache_entries=0 if cache else -1)
     # warm-up: a few requests through the server (graph capture, pool growth)
     for p in range(4):
         srv.submit(pool[p], 2)
-    while srv.stats()["completed"] < 4:
-        srv.tick()
+    deadline = time.monotonic() + 300.0
+    while srv.stats()["completed"] + srv.stats()["failed"] < 4 and time.monotonic() < deadline:
+        if srv.tick()[0] == 0:
+            time.sleep(0.002)
     base_completed = srv.stats()["completed"]
     base_ti = srv.stats()["tet_iterations"]
     base_busy = srv.stats()["busy_ms"]
@@ -438,35 +452,47 @@ def run_serving(args):
     st = srv.stats()
     lat = srv.latencies_ms()[base_completed:]
     value = (st["tet_iterations"] - base_ti) / wall
-    # same alone vs in the mix, on a 1 % sample (the smallest sampled bodies first)
-    sample = sorted(range(len(ids)), key=lambda i: pool[ids[i][1]].num_tets)[: max(1, len(ids) // 100)]
-    worst_alone = 0.0
+    # Same alone vs in the mix on a 1 % seeded sample across sizes, plus the
+    # largest and a mid-size request of the stream.
+    from pdgb import PdgbError
+
+    srng = np.random.default_rng(11)
+    by_size = sorted(range(len(ids)), key=lambda i: pool[ids[i][1]].num_tets)
+    sample = sorted(set(srng.choice(len(ids), size=max(1, len(ids) // 100), replace=False).tolist()
+                        + [by_size[-1], by_size[len(by_size) // 2]])) if ids else []
     results = {}
-    for i in sample:
-        rid, p, k = ids[i]
-        results[i] = srv.result(rid)[0]
-    # every other result once: all finite (no request's iteration left the finite range)
-    nonfinite = sum(0 if np.isfinite(results[i]).all() else 1 for i in sample)
-    in_sample = set(sample)
+    failed_results = 0
     for i, (rid, p, k) in enumerate(ids):
-        if i not in in_sample and not np.isfinite(srv.result(rid)[0]).all():
-            nonfinite += 1
+        try:
+            X = srv.result(rid)[0]
+        except PdgbError:
+            failed_results += 1
+            continue
+        if i in sample:
+            results[i] = X
+    worst_alone, alone_sizes = 0.0, []
     for i in sample:
+        if i not in results:
+            continue
         rid, p, k = ids[i]
         with PdSolver(pool[p], params) as e:
             e.update(k)
             Xa, _ = e.download_state()
         worst_alone = max(worst_alone, float(np.linalg.norm(results[i] - Xa) / np.linalg.norm(Xa)))
+        alone_sizes.append(pool[p].num_tets)
     acc = None
-    if not args.no_accuracy:
+    if not args.no_accuracy and results:
         sys.path.insert(0, str(ROOT / "oracle"))
         import oracle as O
 
-        i = sample[0]
-        rid, p, k = ids[i]
-        Xo, _, _ = O.simulate(pool[p], params, k, precision=64, nthreads=os.cpu_count() or 1)
-        acc = {"request_tets": pool[p].num_tets, "steps": k,
-               "rel_err_x_vs_fp64": float(np.linalg.norm(results[i] - Xo) / np.linalg.norm(Xo))}
+        acc = []
+        for i in [by_size[len(by_size) // 2]] + [j for j in sample if pool[ids[j][1]].num_tets < 2e4][:2]:
+            if i not in results:
+                continue
+            rid, p, k = ids[i]
+            Xo, _, _ = O.simulate(pool[p], params, k, precision=64, nthreads=os.cpu_count() or 1)
+            acc.append({"request_tets": pool[p].num_tets, "steps": k,
+                        "rel_err_x_vs_fp64": float(np.linalg.norm(results[i] - Xo) / np.linalg.norm(Xo))})
     srv.close()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": int(ksteps.sum()),
@@ -477,12 +503,17 @@ def run_serving(args):
                        "p99": float(np.percentile(lat, 99)) if len(lat) else None,
                        "mean": float(np.mean(lat)) if len(lat) else None},
         "wall_s": wall, "completed": int(st["completed"] - base_completed), "failed": int(st["failed"]),
-        "alone_vs_mix_max_rel_err": worst_alone, "alone_vs_mix_sample": len(sample),
-        "nonfinite_results": int(nonfinite),
+        "failed_results": failed_results,
+        "alone_vs_mix_max_rel_err": worst_alone, "alone_vs_mix_sample": len(alone_sizes),
+        "alone_vs_mix_tets": {"min": min(alone_sizes) if alone_sizes else None,
+                              "max": max(alone_sizes) if alone_sizes else None},
+        "nonfinite_results": int(st["nonfinite"]),
         "accuracy": acc, "clocks": clocks.summary(),
         "busy_frac": float(st["busy_ms"] - base_busy) / 1e3 / wall,
         "server_ms": {"admit": st["admit_ms"], "step": st["step_ms"], "ticks": st["ticks"]},
         "layout_cache_hits": st["layout_cache_hits"],
+        "factors": {"gpu_factorisations": int(st["factors"]), "cache_hits": int(st["factor_cache_hits"]),
+                    "gpu_ms": float(st["factor_ms"])} if params.solver == 1 else None,
         "queue_trace": {"fields": ["t_s", "active", "waiting", "ready", "completed"], "rows": trace[::5]},
         "e2e": {"value": value, "unit": UNIT,
                 "h2d_bytes_per_request": float(np.mean([48 * pool[p].num_verts + 28 * pool[p].num_tets
@@ -490,8 +521,9 @@ def run_serving(args):
                 "d2h_bytes_per_request": float(np.mean([24 * pool[p].num_verts for _, p, _ in ids])) if ids else 0.0,
                 "note": "requests enter as host meshes and leave as host arrays: the serving value is end to end"},
     }
-    if rank == 0:
+    if rank == 0 and print_line:
         print(json.dumps(line), flush=True)
+    return line
 
 
 def launches_per_step(info, params) -> int:

@@ -122,18 +122,27 @@ int pdgb_download_body(pdgb_engine* e, int body, float* X, float* V, int memory)
  * Serving: a request loop with continuous batching (no counterpart in the
  * reference, which advances one scene per frame).  Requests are soft bodies
  * with a step count, submitted at any time.  Host threads prepare each
- * request's layout; pdgb_server_tick admits ready requests in arrival order
- * while their device memory fits hbm_budget_bytes (and max_active), runs ONE
- * PD step (Jacobi + Chebyshev, the shared params) for every active request
- * with one set of launches, and retires finished requests (state copied to
- * host memory, device memory returned to the server's pool).  A request's
- * arithmetic is that of a single engine, so its result does not depend on
- * the other requests in the mix. */
+ * request's layout (and, on the Cholesky path, the ordering and symbolic
+ * analysis of its system); pdgb_server_tick admits ready requests in
+ * arrival order while their device memory fits hbm_budget_bytes (and
+ * max_active), runs ONE PD step (the shared params: Jacobi + Chebyshev, or
+ * the prefactored Cholesky solve with num_iterations iterations) for every
+ * active request with one set of launches, and retires finished requests
+ * (state copied to host memory, device memory returned to the server).  On
+ * the Cholesky path every request's FP64 factor is computed on the GPU at
+ * admission and stays resident with its mesh and state; the per-level solve
+ * launches cover level L of every active request's elimination tree.  A
+ * request's arithmetic is that of a single engine, so its result does not
+ * depend on the other requests in the mix.  A request whose state leaves the
+ * finite range fails (PDGB_ERR_NONFINITE from pdgb_server_result). */
 typedef struct pdgb_server_config {
-    pdgb_params params;       /* shared solver parameters (Jacobi path)       */
+    pdgb_params params;       /* shared solver parameters                     */
     size_t hbm_budget_bytes;  /* device bytes of resident requests           */
     int max_active;           /* slot limit, 0 = budget only                  */
     int host_threads;         /* layout workers, 0 = half the host cores      */
+    int cache_entries;        /* meshes whose layout (and factor) are kept    */
+                              /* for resubmission: 0 = 256, < 0 = no cache    */
+    int reserved;
 } pdgb_server_config;
 
 #define PDGB_REQ_QUEUED 0
@@ -156,14 +165,19 @@ typedef struct pdgb_server_stats {
     long long ticks;          /* ticks that ran a step                        */
     int ready;                /* prepared, waiting for admission              */
     int layout_cache_hits;    /* requests that reused a cached host layout    */
+    long long nonfinite;      /* failed requests whose state became non-finite */
+    long long factors;        /* numeric factorisations run on the GPU         */
+    long long factor_cache_hits; /* admissions that reused a cached factor     */
+    double factor_ms;         /* device time of those factorisations           */
 } pdgb_server_stats;
 
 typedef struct pdgb_server pdgb_server;
 void pdgb_server_default_config(pdgb_server_config* cfg);
 int pdgb_server_create(const pdgb_server_config* cfg, void* stream, pdgb_server** out);
-/* Copies the host mesh; returns the request id.  Host layouts are cached
- * by mesh content (the last 256 distinct meshes): a mesh submitted again
- * skips the layout build. */
+/* Copies the host mesh; returns the request id.  Host layouts (and, on the
+ * Cholesky path, the symbolic and numeric factors) are cached by mesh
+ * content (the last cache_entries distinct meshes): a mesh submitted again
+ * skips the layout build and the factorisation. */
 int pdgb_server_submit(pdgb_server* s, const pdgb_mesh_desc* mesh, int nsteps, long long* request_id);
 /* Admission + one step of every active request + retirement (waits for the
  * step).  active / completed (nullable): requests resident after the tick,

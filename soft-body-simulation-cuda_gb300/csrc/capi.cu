@@ -389,11 +389,7 @@ void upload_mesh(pdgb_engine* e) {
 
 // Scalar system K of the engine's vertex order, from the float coefficients
 // the kernels use (M/h^2 incl. the pin weight) and the double geometry.
-SparseSym engine_system(const HostLayout& L) {
-    std::vector<double> mdt2(L.nv);
-    for (int i = 0; i < L.nv; ++i) mdt2[i] = (double)L.coef[i].x;
-    return assemble_system(L.nv, L.nt, L.tets_int.data(), L.dminv_d.data(), L.coef_d.data(), mdt2);
-}
+SparseSym engine_system(const HostLayout& L) { return layout_system(L); }
 
 // Solve schedule: the requested one, or by size.  The per-level launches
 // (programmatic dependent launch, factor blocks loaded before each wait)

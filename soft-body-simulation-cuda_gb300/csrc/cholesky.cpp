@@ -71,6 +71,22 @@ SparseSym assemble_system(int nv, int nt, const uint32_t* tets4, const double* d
     return K;
 }
 
+SparseSym layout_system(const HostLayout& L) {
+    std::vector<double> mdt2(L.nv);
+    for (int i = 0; i < L.nv; ++i) mdt2[i] = (double)L.coef[i].x;
+    return assemble_system(L.nv, L.nt, L.tets_int.data(), L.dminv_d.data(), L.coef_d.data(), mdt2);
+}
+
+std::vector<float> layout_xyz(const HostLayout& L) {
+    std::vector<float> xyz(3 * (size_t)L.nv);
+    for (int i = 0; i < L.nv; ++i) {
+        xyz[3 * (size_t)i] = L.x0[i].x;
+        xyz[3 * (size_t)i + 1] = L.x0[i].y;
+        xyz[3 * (size_t)i + 2] = L.x0[i].z;
+    }
+    return xyz;
+}
+
 // ------------------------------------------------------------------ AMD
 std::vector<int> amd_order(const SparseSym& A) {
     const int n = A.n;

@@ -242,4 +242,14 @@ void cholesky_solve_host(const CholFactor& f, const double* b3, double* x3);
 SparseSym assemble_system(int nv, int nt, const uint32_t* tets4, const double* dminv, const double* coef,
                           const std::vector<double>& mdt2);
 
+// The scalar system K of a single body's layout, in its internal vertex
+// order: M/h^2 from the float coefficients the kernels use (pin weight
+// included) and the double geometry.
+struct HostLayout;
+SparseSym layout_system(const HostLayout& L);
+
+// Rest positions of a layout as 3 floats per vertex (the nested-dissection
+// ordering's coordinates).
+std::vector<float> layout_xyz(const HostLayout& L);
+
 }  // namespace pdgb

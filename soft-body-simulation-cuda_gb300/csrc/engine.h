@@ -217,7 +217,8 @@ void launch_begin(const BeginArgs& a, cudaStream_t s);
 // Multi-request forms (serving): one launch covers the work lists of all
 // active requests; entries are {request index, tile or first vertex}.
 void launch_begin_multi(const BeginArgs* req, const int2* list, const int* count, int grid, cudaStream_t s);
-void launch_local_multi(const LocalArgs* req, const int2* list, const int* count, int grid, cudaStream_t s);
+void launch_local_multi(const LocalArgs* req, const int2* list, const int* count, int grid, cudaStream_t s,
+                        bool jacobi_form = true);
 void launch_jacobi_vertex_multi(const VertexArgs* req, const int2* list, const int* count, int grid, int mode,
                                 float omega, cudaStream_t s);
 void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_form, int rotation, cudaStream_t s);

@@ -185,8 +185,11 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_multi(const LocalArgs* 
     local_tile<kJacobiForm, PDGB_ROTATION_QUAT>(req[w.x], w.y, slot, pos);
 }
 
-void launch_local_multi(const LocalArgs* req, const int2* list, const int* count, int grid, cudaStream_t s) {
-    if (grid > 0) k_local_multi<true><<<grid, kLocalThreads, kMaxPatch * sizeof(float4), s>>>(req, list, count);
+void launch_local_multi(const LocalArgs* req, const int2* list, const int* count, int grid, cudaStream_t s,
+                        bool jacobi_form) {
+    if (grid <= 0) return;
+    if (jacobi_form) k_local_multi<true><<<grid, kLocalThreads, kMaxPatch * sizeof(float4), s>>>(req, list, count);
+    else k_local_multi<false><<<grid, kLocalThreads, kMaxPatch * sizeof(float4), s>>>(req, list, count);
 }
 
 // The plain form (Cholesky path) is launched with programmatic dependent

@@ -728,6 +728,43 @@ __global__ void __launch_bounds__(256) k_chol_vertex(CholVertexArgs a) {
     }
 }
 
+// Multi-request forms (serving, fixed iteration count): CTA i takes 256
+// vertices of request list[i].x from list[i].y.
+__global__ void __launch_bounds__(256) k_chol_vertex_multi(const CholVertexArgs* __restrict__ req,
+                                                           const int2* __restrict__ list,
+                                                           const int* __restrict__ count) {
+    if ((int)blockIdx.x >= *count) return;
+    const int2 w = list[blockIdx.x];
+    const CholVertexArgs& a = req[w.x];
+    const int i = w.y + threadIdx.x;
+    if (i >= a.nv) return;
+    a.y[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 cf = __ldg(&a.coef[i]);
+    a.b[i] = cf.z != 0.f ? __ldg(&a.pin_rhs[i]) : __ldg(&a.base[i]);
+}
+
+__global__ void __launch_bounds__(256) k_chol_finish_multi(const CholVertexArgs* __restrict__ req,
+                                                           const int2* __restrict__ list,
+                                                           const int* __restrict__ count) {
+    if ((int)blockIdx.x >= *count) return;
+    const int2 w = list[blockIdx.x];
+    const CholVertexArgs& a = req[w.x];
+    const int i = w.y + threadIdx.x;
+    if (i >= a.nv) return;
+    finish_vertex(a.sc, i, a.sn[i], a.dt_inv, a.x, a.v);
+    a.y[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+void launch_chol_vertex_multi(const CholVertexArgs* req, const int2* list, const int* count, int grid,
+                              cudaStream_t s) {
+    if (grid > 0) k_chol_vertex_multi<<<grid, 256, 0, s>>>(req, list, count);
+}
+
+void launch_chol_finish_multi(const CholVertexArgs* req, const int2* list, const int* count, int grid,
+                              cudaStream_t s) {
+    if (grid > 0) k_chol_finish_multi<<<grid, 256, 0, s>>>(req, list, count);
+}
+
 // After the iterations: velocity / position update (updateVelPos,
 // pdUtil.cu:180-193), X <- XTilde (pdSolver.cu:227) and the fixed-body
 // correction of XTilde and V (pdSolver.cu:228-231).

@@ -116,5 +116,10 @@ void launch_refine_update(const RefineArgs& a, cudaStream_t s);
 
 void launch_chol_vertex(const CholVertexArgs& a, cudaStream_t s);
 void launch_chol_finish(const CholVertexArgs& a, cudaStream_t s);
+// Multi-request forms (serving; no early exit): entries {request, first vertex}.
+void launch_chol_vertex_multi(const CholVertexArgs* req, const int2* list, const int* count, int grid,
+                              cudaStream_t s);
+void launch_chol_finish_multi(const CholVertexArgs* req, const int2* list, const int* count, int grid,
+                              cudaStream_t s);
 
 }  // namespace pdgb

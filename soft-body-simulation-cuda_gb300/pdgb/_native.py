@@ -114,6 +114,8 @@ class pdgb_server_config(C.Structure):
         ("hbm_budget_bytes", C.c_size_t),
         ("max_active", C.c_int),
         ("host_threads", C.c_int),
+        ("cache_entries", C.c_int),
+        ("reserved", C.c_int),
     ]
 
 
@@ -131,6 +133,10 @@ class pdgb_server_stats(C.Structure):
         ("ticks", C.c_longlong),
         ("ready", C.c_int),
         ("layout_cache_hits", C.c_int),
+        ("nonfinite", C.c_longlong),
+        ("factors", C.c_longlong),
+        ("factor_cache_hits", C.c_longlong),
+        ("factor_ms", C.c_double),
     ]
 
 

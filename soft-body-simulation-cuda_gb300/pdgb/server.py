@@ -15,7 +15,11 @@ class PdServer:
     tick() to advance every resident request by one step."""
 
     def __init__(self, params: SolverParams, hbm_budget_bytes: int = 8 << 30, max_active: int = 0,
-                 host_threads: int = 0, stream: int | None = None):
+                 host_threads: int = 0, stream: int | None = None, cache_entries: int = 0):
+        """params.solver selects the global solve of every request (Jacobi +
+        Chebyshev, or the Cholesky factor computed on the GPU at admission);
+        cache_entries: meshes whose layout and factor are kept (0 = 256, < 0 =
+        none)."""
         self._lib = N.lib()
         cfg = N.pdgb_server_config()
         self._lib.pdgb_server_default_config(C.byref(cfg))
@@ -23,6 +27,7 @@ class PdServer:
         cfg.hbm_budget_bytes = int(hbm_budget_bytes)
         cfg.max_active = int(max_active)
         cfg.host_threads = int(host_threads)
+        cfg.cache_entries = int(cache_entries)
         h = C.c_void_p()
         N.check(self._lib.pdgb_server_create(C.byref(cfg), stream, C.byref(h)), "pdgb_server_create")
         self._h = h

@@ -13,7 +13,9 @@ Each workload of the bench is asserted at its own size here, with the same
     bodies, the largest among them, against the same body alone and against
     the oracle;
   - served requests of mid and large size (3e4 and 3e5 tets) next to small
-    ones: each result equals the body run alone and matches the oracle.
+    ones, with the Jacobi and with the Cholesky global solve (factors
+    computed on the GPU at admission, resident while the request runs): each
+    result equals the body run alone and matches the oracle.
 
 Reference iteration: PdSolver::SolverStep, pdSolver.cu:141-208.
 """
@@ -101,8 +103,9 @@ def test_c4_batch_sample_vs_alone_and_oracle():
     assert sizes[largest] >= 5 * 20 ** 3
 
 
-def test_c5_mid_and_large_requests_alone_vs_mix():
-    params = SolverParams(num_iterations=10, rho=0.9995, solver=0)
+@pytest.mark.parametrize("solver", [0, 1])
+def test_c5_mid_and_large_requests_alone_vs_mix(solver):
+    params = SolverParams(num_iterations=10, rho=0.9995, solver=solver)
     rng = np.random.default_rng(8)
     big = [mesh.request_body(3e4, rng), mesh.request_body(3e5, rng)]
     small = [mesh.request_body(math.exp(rng.uniform(math.log(1e3), math.log(1e4))), rng) for _ in range(6)]

@@ -35,11 +35,16 @@ def _alone(body, steps):
         return e.download_state()
 
 
-def _drain(srv, ids, max_ticks=1000):
-    for _ in range(max_ticks):
+def _drain(srv, ids, timeout_s=120.0):
+    """Ticks until every request is done or failed (layouts and factors are
+    prepared by host workers meanwhile), bounded in time."""
+    deadline = time.monotonic() + timeout_s
+    while time.monotonic() < deadline:
         if all(srv.poll(i)[0] in (N.PDGB_REQ_DONE, N.PDGB_REQ_FAILED) for i in ids):
             return
-        srv.tick()
+        active, _ = srv.tick()
+        if active == 0:
+            time.sleep(0.002)
     raise AssertionError("requests did not finish")
 
 
@@ -132,4 +137,83 @@ def test_layout_cache_reuse():
         for rid, b, s in zip([first] + ids, [body, body, body, other], [3, 2, 5, 4]):
             X, _ = srv.result(rid)
             Xa, _ = _alone(b, s)
+            assert rel_l2(X, Xa) < 1e-5
+
+
+CHOL = SolverParams(num_iterations=10, solver=1)
+
+
+def _alone_with(body, steps, params):
+    with PdSolver(body, params) as e:
+        e.update(steps)
+        return e.download_state()
+
+
+def test_cholesky_requests_equal_alone_and_oracle():
+    """Cholesky requests: each request's FP64 factor is computed on the GPU at
+    admission and stays resident; the per-level solve launches cover every
+    active request.  Results equal the engine alone and the FP64 oracle."""
+    reqs = _bodies()
+    with PdServer(CHOL) as srv:
+        ids = [srv.submit(b, s) for b, s in reqs[:3]]
+        srv.tick()
+        ids += [srv.submit(b, s) for b, s in reqs[3:]]  # join while the others run
+        _drain(srv, ids)
+        for (body, steps), rid in zip(reqs, ids):
+            assert srv.poll(rid) == (N.PDGB_REQ_DONE, steps)
+            X, V = srv.result(rid)
+            Xa, _ = _alone_with(body, steps, CHOL)
+            assert rel_l2(X, Xa) < 1e-5
+            Xo, _, _ = O.simulate(body, CHOL, steps, precision=64)
+            assert rel_l2(X, Xo) < 1e-4
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["active"] == 0 and st["bytes_in_use"] == 0
+        assert st["factors"] == len(reqs) and st["factor_ms"] > 0
+
+
+def test_cholesky_factor_cache_and_no_cache():
+    """A mesh submitted again reuses its cached layout and numeric factor
+    (uploaded, not recomputed); with the cache off every request factors."""
+    body, _ = _bodies()[1]
+    other, _ = _bodies()[4]
+    for cache in (0, -1):
+        with PdServer(CHOL, cache_entries=cache) as srv:
+            first = srv.submit(body, 3)
+            _drain(srv, [first])
+            ids = [srv.submit(body, s) for s in (2, 5)] + [srv.submit(other, 4)]
+            _drain(srv, ids)
+            st = srv.stats()
+            if cache == 0:
+                assert st["factor_cache_hits"] >= 2 and st["factors"] == 2 and st["layout_cache_hits"] >= 2
+            else:
+                assert st["factor_cache_hits"] == 0 and st["factors"] == 4 and st["layout_cache_hits"] == 0
+            for rid, b, s in zip([first] + ids, [body, body, body, other], [3, 2, 5, 4]):
+                X, _ = srv.result(rid)
+                Xa, _ = _alone_with(b, s, CHOL)
+                assert rel_l2(X, Xa) < 1e-5
+
+
+@pytest.mark.parametrize("solver", [0, 1])
+def test_nonfinite_request_fails(solver):
+    """A request whose state leaves the finite range (here a NaN initial
+    velocity) fails with PDGB_ERR_NONFINITE instead of returning NaN; the
+    requests beside it are unaffected."""
+    params = PARAMS if solver == 0 else CHOL
+    reqs = _bodies()[:3]
+    bad, _ = _bodies()[3]
+    bad.V = np.zeros_like(bad.X)
+    bad.V[5, 1] = np.nan
+    with PdServer(params) as srv:
+        ids = [srv.submit(b, s) for b, s in reqs]
+        bad_id = srv.submit(bad, 3)
+        _drain(srv, ids + [bad_id])
+        assert srv.poll(bad_id)[0] == N.PDGB_REQ_FAILED
+        with pytest.raises(Exception) as err:
+            srv.result(bad_id)
+        assert getattr(err.value, "status", None) == N.PDGB_ERR_NONFINITE
+        st = srv.stats()
+        assert st["nonfinite"] == 1 and st["failed"] == 1 and st["completed"] == len(reqs)
+        for (body, steps), rid in zip(reqs, ids):
+            X, _ = srv.result(rid)
+            Xa, _ = _alone_with(body, steps, params)
             assert rel_l2(X, Xa) < 1e-5
