@@ -13,6 +13,13 @@ step.  One bench step = one PD time step = 20 iterations over all tets.
   roofline  local-step kernel: algorithmic bytes per launch / average launch
          time (CUDA events around every launch inside the step graph).
 
+The default run (no --workload) adds, under "workloads", a leg for each of
+the other workloads, each with its own step count: the 10^3 Cholesky cube
+(c1), the 40^3 heterogeneous Cholesky cube with its factor times and the
+refinement sweep (c3), the batch of 512 bodies with the plain drop-in on the
+same bodies and their ratio (c4), and an 8-second window of the Cholesky
+request stream with p50/p99 latency (c5).  --workload X runs X alone.
+
 `--impl reference` times the CPU implementation of the same iteration (the
 reference's kernels compiled for the CPU when present, else the project's
 float restatement) on all host cores, one PD step of the workload per bench
@@ -566,36 +573,82 @@ def main():
                     "(cuSOLVER Cholesky / Jacobi) timed beside the engine")
     ap.add_argument("--collision", action="store_true", help="run continuous collision between bodies after every "
                     "step (inside the timed region)")
+    ap.add_argument("--no-legs", action="store_true", help="default run: report the 64^3 Jacobi workload only, "
+                    "without the legs of the other workloads")
+    ap.add_argument("--solver", default="", choices=["", "jacobi", "cholesky"],
+                    help="serving workload: global solve of the requests (default: the workload's, Cholesky)")
+    ap.add_argument("--no-cache", action="store_true", help="serving workload: no mesh cache (every request builds "
+                    "its layout and factor)")
     args = ap.parse_args()
+    explicit = "--workload" in sys.argv[1:] or any(a.startswith("--workload=") for a in sys.argv[1:])
     if args.warmup < 3 and args.impl == "pdgb":
         args.warmup = 3
     if args.steps <= 0:
         args.steps = DEFAULT_STEPS.get(args.workload, 20) if args.impl == "pdgb" else 2
 
+    if args.workload == "c5" and args.impl != "reference":
+        run_serving(args, args.window, args.rate, args.solver, not args.no_cache)
+        return
+    if args.impl == "reference":
+        run_engine(args, args.workload, args.steps, args.warmup)
+        return
+    rank, world, _ = dist_info()
+    line = run_engine(args, args.workload, args.steps, args.warmup)
+    if line is None:
+        return
+    if not explicit and not args.no_legs and world == 1:
+        # The default run also reports the other workloads of the benchmark,
+        # each with its own (shorter) step count: the plain Cholesky cube, the
+        # heterogeneous Cholesky cube, the batch of 512 bodies (with the plain
+        # drop-in on the same bodies) and the Cholesky request stream.
+        legs = {}
+        for wl, steps in (("c1", 200), ("c3", 30), ("c4", 20)):
+            legs[wl] = compact_leg(run_engine(args, wl, steps, 3, leg=True))
+        legs["c5"] = compact_serving(run_serving(args, 8.0, 0.0, "", True, print_line=False))
+        line["workloads"] = legs
+    print(json.dumps(line), flush=True)
+
+
+def compact_leg(line: dict) -> dict:
+    """The fields of a workload's line that the default run reports as a leg."""
+    keep = ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config", "e2e", "roofline", "kernels",
+            "accuracy", "reference_gpu", "plain_drop_in", "batched_vs_plain", "factor", "cpu_baseline",
+            "gpu_launches", "clocks", "finite", "autotune")
+    return {k: line[k] for k in keep if k in line}
+
+
+def compact_serving(line: dict) -> dict:
+    keep = ("metric", "value", "unit", "config", "latency_ms", "wall_s", "completed", "failed", "failed_results",
+            "nonfinite_results", "alone_vs_mix_max_rel_err", "alone_vs_mix_sample", "alone_vs_mix_tets", "accuracy",
+            "busy_frac", "layout_cache_hits", "factors", "clocks", "e2e")
+    return {k: line[k] for k in keep if k in line}
+
+
+def run_engine(args, workload_name: str, nsteps: int, nwarmup: int, leg: bool = False):
+    """One engine workload (c1-c4): the timed steps, the kernel pass, the
+    end-to-end pass and the reports.  Returns the JSON line (rank 0), or
+    None on other ranks and for the reference arm (which prints its own)."""
     from pdgb import mesh
     from pdgb.engine import SolverParams
 
-    if args.workload == "c5" and args.impl != "reference":
-        run_serving(args)
-        return
     global WORKLOAD
-    WORKLOAD = dict(WORKLOADS[args.workload])
+    WORKLOAD = dict(WORKLOADS[workload_name])
     WORKLOAD["l2"] = "flushed between timed steps (256 MB write)"
-    if args.grid:
+    if args.grid and not leg:
         WORKLOAD["grid"] = args.grid
         WORKLOAD["workload"] += f"_grid{args.grid}"
     n = WORKLOAD.get("grid", 0)
     bodies = None
-    if args.workload == "c4":
-        bodies = mesh.batch_c4(nbodies=args.bodies or WORKLOAD["nbodies"])
+    if workload_name == "c4":
+        bodies = mesh.batch_c4(nbodies=(args.bodies if not leg else 0) or WORKLOAD["nbodies"])
         WORKLOAD["nbodies"] = len(bodies)
         body = mesh.concat(bodies)
         WORKLOAD["tets"], WORKLOAD["verts"] = body.num_tets, body.num_verts
         params = SolverParams(num_iterations=WORKLOAD["iterations"], solver=1)
-    elif args.workload == "c2":
+    elif workload_name == "c2":
         body = mesh.cube_c2(n=n)
         params = SolverParams(num_iterations=WORKLOAD["iterations"], rho=WORKLOAD["rho"], solver=0)
-    elif args.workload == "c1":
+    elif workload_name == "c1":
         body = mesh.make_grid_body(n, n, n, young=1e5, poisson=0.4, density=1000.0)
         params = SolverParams(num_iterations=WORKLOAD["iterations"], solver=1)
     else:
@@ -605,13 +658,13 @@ def main():
     cpu_body = body if bodies is None else mesh.concat(bodies[:16])  # bounded CPU sample of the batch
     if args.impl == "reference":
         run_reference_arm(args, cpu_body, params, scale=1.0)
-        return
+        return None
 
     rank, world, local = dist_info()
     import torch
 
     torch.cuda.set_device(local)
-    dist = init_dist(world)
+    dist = init_dist(world) if not leg else None
     from pdgb import PdSolver
 
     from pdgb import _native as N
@@ -661,7 +714,7 @@ def main():
     eng.enable_kernel_timing(N.PDGB_TIMING_STEPS)
     eng.prepare()
     start_episode(0)
-    for _ in range(args.warmup):
+    for _ in range(nwarmup):
         eng.update(1)
         flush_l2()
     eng.synchronize()
@@ -672,7 +725,7 @@ def main():
     # the engine's stream (no host wait between steps); the L2 flush runs
     # between steps, outside the events.
     with ClockSampler(local) as clocks:
-        for k in range(args.steps):
+        for k in range(nsteps):
             start_episode(k)
             eng.update(1)
             flush_l2()
@@ -681,7 +734,7 @@ def main():
     tm = eng.read_timing()
     Xt, _ = eng.download_state()
     finite_timed = bool(np.isfinite(Xt).all())
-    assert tm["steps"] == args.steps
+    assert tm["steps"] == nsteps
     if collision is not None:
         _, _, cinfo = eng.collision()
         collision.update(candidate_pairs=cinfo["candidate_pairs"], vertices_hit=cinfo["vertices_hit"],
@@ -695,7 +748,7 @@ def main():
     start_episode(0)
     eng.update(1)
     eng.read_timing()
-    for k in range(args.steps):
+    for k in range(nsteps):
         start_episode(k)
         eng.update(1)
         flush_l2()
@@ -705,7 +758,7 @@ def main():
     solve_ms, solves = tk["solve_ms"], tk["solves"]
     step_ms_kernel_pass = tk["step_ms"]
     t_max = reduce_max(dist, t_local)
-    tet_iters = reduce_sum(dist, float(body.num_tets * params.num_iterations * args.steps))
+    tet_iters = reduce_sum(dist, float(body.num_tets * params.num_iterations * nsteps))
     value = tet_iters / t_max
 
     # ---- e2e through the C ABI with pinned host buffers
@@ -721,7 +774,7 @@ def main():
         N.check(lib.pdgb_step(h, 1), "step")
         N.check(lib.pdgb_download_state(h, Xh.data_ptr(), Vh.data_ptr(), N.PDGB_MEM_HOST), "download")
     e2e_s = 0.0
-    for k in range(args.steps):
+    for k in range(nsteps):
         if k == 0 or (episode and k % episode == 0):
             Xh.copy_(X0h)  # the caller starts a new run from rest
             Vh.zero_()
@@ -742,6 +795,15 @@ def main():
     eng_info["levels"] = eng.solve_levels() if params.solver == 1 else 0
     eng_info["solve_mode"] = eng.solve_mode() if params.solver == 1 else 0
     eng_info["solve_launches"] = eng.factor_info()["solve_launches"] if params.solver == 1 else 0
+    factor = None
+    if params.solver == 1:
+        fi = eng.factor_info()
+        factor = {"numeric_device": "gpu" if fi["numeric_device"] == N.PDGB_FACTOR_GPU else "host",
+                  "numeric_ms": fi["numeric_ms"], "total_ms": fi["factor_ms"], "flops": fi["flops"],
+                  "nnz_L": fi["nnz_L"], "m_entries": fi["m_entries"], "pool_bytes": fi["pool_bytes"],
+                  "levels": fi["num_levels"],
+                  "what": "total_ms: ordering + symbolic analysis (host) + FP64 numeric factorisation "
+                          "(numeric_ms, device time on the GPU), once per system matrix"}
     solve_bytes = eng.solve_bytes()
     # the local step alone, back to back (CUDA events around 200 launches on
     # the engine's stream, after the timed region): no event nodes between
@@ -760,7 +822,7 @@ def main():
     eng.close()
 
     if rank != 0:
-        return
+        return None
     peak, peak_kind = measured_peak_hbm()
     bytes_per_launch = 56.0 * body.num_tets + 36.0 * body.num_verts
     avg_local_s = (local_ms / 1e3) / max(local_launches, 1)
@@ -794,21 +856,21 @@ def main():
             roofline = solve_roof  # the dominant kernel of the Cholesky step
     cpu = None
     if not args.no_cpu_baseline:
-        cpu = cpu_baseline(cpu_body, params, args.cpu_steps)
+        cpu = cpu_baseline(cpu_body, params, 1 if leg else args.cpu_steps)
         if bodies is not None:
             cpu["sample"] += f"; the first 16 of the {len(bodies)} bodies"
     clk = clocks.summary()
     ref_gpu = None
     if not args.no_ref_gpu:
-        ref_steps = {"c1": 20, "c2": 50, "c3": 3, "c4": 5}[args.workload]
+        ref_steps = {"c1": 20, "c2": 50, "c3": 3, "c4": 5}[workload_name]
         ref_sample = (f"{ref_steps} steps of the workload" if bodies is None else
                       f"{ref_steps} steps of the first 16 of the {len(bodies)} bodies concatenated into one system "
                       "(the reference's multi-body mode)")
         ref_gpu = reference_gpu(cpu_body, params, ref_steps, episode, ref_sample)
     acc = None
     if not args.no_accuracy:
-        acc_steps = {"c1": 20, "c2": 20, "c3": 3, "c4": 5}[args.workload]
-        acc = accuracy_vs_fp64(cpu_body, params, acc_steps, refine_sweep=args.workload == "c3",
+        acc_steps = {"c1": 20, "c2": 20, "c3": 3, "c4": 5}[workload_name]
+        acc = accuracy_vs_fp64(cpu_body, params, acc_steps, refine_sweep=workload_name == "c3",
                                ref_gpu=not args.no_ref_gpu)
         if bodies is not None:
             acc["sample"] = "first 16 bodies of the batch"
@@ -817,9 +879,9 @@ def main():
         "value": value,
         "unit": UNIT,
         "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": t_max * 1e3 / args.steps,
+        "steps": nsteps,
+        "warmup": nwarmup,
+        "ms_per_step": t_max * 1e3 / nsteps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -835,13 +897,17 @@ def main():
         "plain_drop_in": plain,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 3 * 4 * nv,
                 "d2h_bytes_per_step": 2 * 3 * 4 * nv},
-        "gpu_launches": args.steps * launches_per_step(eng_info, params)
-                        + (-(-args.steps // episode) if episode else 0),  # + the rest-state upload of every run
+        "gpu_launches": nsteps * launches_per_step(eng_info, params)
+                        + (-(-nsteps // episode) if episode else 0),  # + the rest-state upload of every run
         "clocks": clk,
         "finite": finite and finite_timed,
         "accuracy": acc,
+        "factor": factor,
     }
-    print(json.dumps(line), flush=True)
+    if plain is not None:
+        line["batched_vs_plain"] = {"ratio": value / plain["value"], "target": 5.0,
+                                    "what": "batched value over the plain drop-in's on the same bodies"}
+    return line
 
 
 if __name__ == "__main__":
