@@ -431,6 +431,9 @@ def run_serving(args, window: float, rate: float = 0.0, solver: str = "", cache:
         if srv.tick()[0] == 0:
             time.sleep(0.002)
     base_completed = srv.stats()["completed"]
+    base_failed = srv.stats()["failed"]
+    base_lat = len(srv.latencies_ms())
+    give_up_s = 20.0 * window + 600.0
     base_ti = srv.stats()["tet_iterations"]
     base_busy = srv.stats()["busy_ms"]
     ids = []
@@ -449,15 +452,17 @@ def run_serving(args, window: float, rate: float = 0.0, solver: str = "", cache:
                 ids.append((srv.submit(pool[picks[nxt]], int(ksteps[nxt])), int(picks[nxt]), int(ksteps[nxt])))
                 nxt += 1
             st = srv.stats()
-            if nxt >= n_req and st["completed"] - base_completed >= n_req:
+            if nxt >= n_req and st["completed"] + st["failed"] - base_completed - base_failed >= n_req:
                 break
-            if st["active"] == 0 and st["waiting"] == 0:
+            if now > give_up_s:
+                raise RuntimeError(f"serving: requests unfinished after {give_up_s:.0f} s")
+            if st["active"] == 0 and st["waiting"] == 0 and st["finishing"] == 0:
                 time.sleep(0.0005)
                 continue
-            srv.tick()
+            srv.tick()  # a tick hands out the requests the previous tick's step finished
         wall = time.perf_counter() - t0
     st = srv.stats()
-    lat = srv.latencies_ms()[base_completed:]
+    lat = srv.latencies_ms()[base_lat:]
     value = (st["tet_iterations"] - base_ti) / wall
     # Same alone vs in the mix on a 1 % seeded sample across sizes, plus the
     # largest and a mid-size request of the stream.
@@ -509,7 +514,7 @@ def run_serving(args, window: float, rate: float = 0.0, solver: str = "", cache:
         "latency_ms": {"p50": float(np.percentile(lat, 50)) if len(lat) else None,
                        "p99": float(np.percentile(lat, 99)) if len(lat) else None,
                        "mean": float(np.mean(lat)) if len(lat) else None},
-        "wall_s": wall, "completed": int(st["completed"] - base_completed), "failed": int(st["failed"]),
+        "wall_s": wall, "completed": int(st["completed"] - base_completed), "failed": int(st["failed"] - base_failed),
         "failed_results": failed_results,
         "alone_vs_mix_max_rel_err": worst_alone, "alone_vs_mix_sample": len(alone_sizes),
         "alone_vs_mix_tets": {"min": min(alone_sizes) if alone_sizes else None,
@@ -620,7 +625,7 @@ def compact_leg(line: dict) -> dict:
 def compact_serving(line: dict) -> dict:
     keep = ("metric", "value", "unit", "config", "latency_ms", "wall_s", "completed", "failed", "failed_results",
             "nonfinite_results", "alone_vs_mix_max_rel_err", "alone_vs_mix_sample", "alone_vs_mix_tets", "accuracy",
-            "busy_frac", "layout_cache_hits", "factors", "clocks", "e2e")
+            "busy_frac", "server_ms", "layout_cache_hits", "factors", "clocks", "e2e")
     return {k: line[k] for k in keep if k in line}
 
 
@@ -846,7 +851,8 @@ def run_engine(args, workload_name: str, nsteps: int, nwarmup: int, leg: bool = 
         solve_roof = {"bound": "hbm", "achieved": s_ach, "peak": peak, "unit": "GB/s", "frac": s_ach / peak,
                       "traffic": None, "peak_kind": peak_kind,
                       "kernel": {1: "k_chol_solve_cta", 2: "k_chol_solve_cluster", 4: "k_chol_solve_dsm",
-                                 3: "k_chol_fwd_level + k_chol_bwd_level"}.get(eng_info.get("solve_mode"), "solve"),
+                                 3: "k_chol_fwd_level + k_chol_bwd_level",
+                                 5: "k_chol_solve_persistent"}.get(eng_info.get("solve_mode"), "solve"),
                       "bytes_per_launch": solve_bytes, "avg_launch_us": avg_solve_s * 1e6, "launches": solves,
                       "share_of_step": solve_ms / step_ms_kernel_pass if step_ms_kernel_pass > 0 else None,
                       "note": "one solve = forward + backward over the supernodal tree; bytes per the scalar "

@@ -169,6 +169,9 @@ typedef struct pdgb_server_stats {
     long long factors;        /* numeric factorisations run on the GPU         */
     long long factor_cache_hits; /* admissions that reused a cached factor     */
     double factor_ms;         /* device time of those factorisations           */
+    int finishing;            /* stepped to their count, results handed out   */
+                              /* by the next tick                              */
+    int reserved;
 } pdgb_server_stats;
 
 typedef struct pdgb_server pdgb_server;
@@ -179,9 +182,13 @@ int pdgb_server_create(const pdgb_server_config* cfg, void* stream, pdgb_server*
  * content (the last cache_entries distinct meshes): a mesh submitted again
  * skips the layout build and the factorisation. */
 int pdgb_server_submit(pdgb_server* s, const pdgb_mesh_desc* mesh, int nsteps, long long* request_id);
-/* Admission + one step of every active request + retirement (waits for the
- * step).  active / completed (nullable): requests resident after the tick,
- * requests finished by it. */
+/* One tick: waits for the step launched by the previous tick and hands out
+ * the requests it finished, admits ready requests, launches one step of
+ * every active request and, while it runs, admits more and prepares the
+ * next step's work lists; it returns without waiting for its step.  active
+ * / completed (nullable): requests resident after the tick, requests handed
+ * out by it.  Keep calling it while requests are active, waiting or
+ * finishing (pdgb_server_stats). */
 int pdgb_server_tick(pdgb_server* s, int* active, int* completed);
 int pdgb_server_poll(pdgb_server* s, long long request_id, int* state, int* steps_done);
 /* Final state of a finished request (caller layout); releases the request. */
@@ -231,8 +238,19 @@ int pdgb_synchronize(pdgb_engine* e);
  * with a non-finite position or velocity (the iteration left the finite
  * range), else PDGB_OK.  The step epilogue sets a device word; this call
  * waits for the stream and reads it.  The reference reports nothing here
- * (SolverStep returns true unconditionally, pdSolver.cu:207). */
+ * (SolverStep returns true unconditionally, pdSolver.cu:207).  With the
+ * PERSISTENT solve schedule, PDGB_ERR_TIMEOUT when a grid-barrier wait ran
+ * out of its bound (the steps since then are invalid). */
 int pdgb_last_step_status(pdgb_engine* e);
+
+/* Check of the persistent solve's grid barrier on its own (no counterpart
+ * in the reference): one cooperative launch of `ctas` CTAs (0: the solve's
+ * grid) passes `rounds` barriers, each waiting for `missing` more arrivals
+ * than there are CTAs.  With missing = 0 every barrier completes (PDGB_OK);
+ * with missing > 0 no barrier can complete and every wait gives up after
+ * spin_limit polls (PDGB_ERR_TIMEOUT) -- the kernel returns, the context
+ * stays usable.  Waits for the GPU. */
+int pdgb_grid_sync_check(int ctas, int rounds, int missing, long long spin_limit);
 
 /* Device timing for benchmarks (mode, default OFF):
  *   PDGB_TIMING_STEPS: pdgb_step brackets every step-graph launch with a
@@ -312,9 +330,13 @@ int pdgb_set_rotation(pdgb_engine* e, int rotation);
  * (distributed shared memory between the CTAs; PDGB_ERR_UNSUPPORTED at
  * prepare when it does not fit; on request only: with whole supernodes
  * per CTA and remote float atomics it measures slower than CLUSTER on the
- * bodies that fit).  AUTO picks by size: LEVELS from 2^15 stored factor
- * entries up, below that CLUSTER for a single system and CTA for a batch;
- * pdgb_autotune times CTA, CLUSTER and LEVELS.  Takes
+ * bodies that fit); PERSISTENT: the whole solve (every body of a batch) in
+ * one cooperative launch over the GPU, the levels of LEVELS separated by a
+ * grid-wide barrier whose waits are bounded (a wait that runs out sets a
+ * status word: pdgb_last_step_status then returns PDGB_ERR_TIMEOUT).  AUTO
+ * picks by size: LEVELS from 2^15 stored factor entries up, below that
+ * CLUSTER for a single system and CTA for a batch; pdgb_autotune times CTA,
+ * CLUSTER, LEVELS and PERSISTENT.  Takes
  * effect at the next prepare; pdgb_get_solve_mode returns the schedule in
  * use (AUTO before the first prepare or on the Jacobi path). */
 #define PDGB_SOLVE_AUTO 0
@@ -322,6 +344,7 @@ int pdgb_set_rotation(pdgb_engine* e, int rotation);
 #define PDGB_SOLVE_CLUSTER 2
 #define PDGB_SOLVE_LEVELS 3
 #define PDGB_SOLVE_DSM 4
+#define PDGB_SOLVE_PERSISTENT 5
 int pdgb_set_solve_mode(pdgb_engine* e, int mode);
 int pdgb_get_solve_mode(pdgb_engine* e, int* mode);
 

@@ -62,6 +62,7 @@ struct pdgb_engine {
         ch_zstage;
     DBuf<float4> ch_zbuf;
     DBuf<int4> ch_levels;
+    DBuf<SolveLevel> ch_step_lv;  // per-level item ranges on the device (persistent solve)
     // distributed-shared-memory solve of a single body (when it fits)
     DsmPlan dsm;
     DBuf<float> dsm_mcopy;
@@ -200,9 +201,11 @@ SceneArgs scene_args(pdgb_engine* e) {
     return sc;
 }
 
-// Clears the sticky non-finite status (the state was set again).
+// Clears the sticky step status words (the state was set again): the
+// non-finite flag and the persistent solve's barrier state.
 void clear_nonfinite(pdgb_engine* e) {
     PDGB_CUDA_TRY(cudaMemsetAsync(&e->st.p->nonfinite, 0, sizeof(int), e->stream));
+    PDGB_CUDA_TRY(cudaMemsetAsync(&e->st.p->bar, 0, sizeof(GridSync), e->stream));
 }
 
 // Collision detection + response after a step (PdSolver::Update,
@@ -314,6 +317,9 @@ void record_chol_step(pdgb_engine* e) {
         if (e->solve_mode == PDGB_SOLVE_CTA) launch_chol_solve_cta(args, e->nbodies, s);
         else if (e->solve_mode == PDGB_SOLVE_CLUSTER) launch_chol_solve_cluster(args, e->nbodies, s);
         else if (e->solve_mode == PDGB_SOLVE_DSM) launch_chol_solve_dsm(args, dsm_args(e), e->dsm.smem_bytes, s);
+        else if (e->solve_mode == PDGB_SOLVE_PERSISTENT)
+            launch_chol_solve_persistent(args, e->ch_step_lv.p, (int)e->chol.step_levels.size(), &st->bar,
+                                         kPersistSpinLimit, s);
         else launch_chol_solve_levels(args, e->chol.step_levels, s);
     };
     for (int i = 0; i < n; ++i) {
@@ -464,6 +470,7 @@ void prepare_cholesky(pdgb_engine* e) {
     for (size_t i = 0; i < lv.size(); ++i)
         lv[i] = make_int4(f.levels[i].fwd_begin, f.levels[i].fwd_end, f.levels[i].bwd_begin, f.levels[i].bwd_end);
     e->ch_levels.upload(lv, s);
+    e->ch_step_lv.upload(f.step_levels, s);
     if (f.K.n == e->nv) {  // FP64 copy of K for refinement residuals (single body)
         std::vector<int> rp(f.K.p.begin(), f.K.p.end());
         e->k_rowptr.upload(rp, s);
@@ -900,7 +907,7 @@ int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
         std::vector<int> caps = {kTileTets, kTileTets / 2, kTileTets / 4, kTileTets / 8};
         std::vector<int> modes = {e->solve_req};
         if (e->prm.solver == PDGB_SOLVER_CHOLESKY) {
-            modes = {PDGB_SOLVE_CTA, PDGB_SOLVE_CLUSTER, PDGB_SOLVE_LEVELS};
+            modes = {PDGB_SOLVE_CTA, PDGB_SOLVE_CLUSTER, PDGB_SOLVE_LEVELS, PDGB_SOLVE_PERSISTENT};
         }
         double best = t0;
         int best_cap = cap0, best_mode = req0, tried = 1;
@@ -937,7 +944,7 @@ int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
 }
 
 int pdgb_set_solve_mode(pdgb_engine* e, int mode) {
-    if (!e || mode < PDGB_SOLVE_AUTO || mode > PDGB_SOLVE_DSM) {
+    if (!e || mode < PDGB_SOLVE_AUTO || mode > PDGB_SOLVE_PERSISTENT) {
         set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or solve mode");
         return PDGB_ERR_INVALID_ARGUMENT;
     }
@@ -1316,11 +1323,17 @@ int pdgb_synchronize(pdgb_engine* e) {
 int pdgb_last_step_status(pdgb_engine* e) {
     if (!e) return PDGB_ERR_INVALID_ARGUMENT;
     int flag = 0;
+    GridSync bar{};
     const int st = guarded([&] {
         PDGB_CUDA_TRY(cudaMemcpyAsync(&flag, &e->st.p->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(&bar, &e->st.p->bar, sizeof(GridSync), cudaMemcpyDeviceToHost, e->stream));
         PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
     });
     if (st != PDGB_OK) return st;
+    if (bar.timeout) {
+        set_last_error(PDGB_ERR_TIMEOUT, "a grid-barrier wait of the persistent solve ran out of its bound");
+        return PDGB_ERR_TIMEOUT;
+    }
     if (flag) {
         set_last_error(PDGB_ERR_NONFINITE, "a step ended with a non-finite position or velocity");
         return PDGB_ERR_NONFINITE;
@@ -1446,7 +1459,7 @@ int pdgb_inspect_layout(const pdgb_mesh_desc* mesh, pdgb_layout_info* info, int*
 namespace {
 // Kernel launches of one solve in the schedule in use.
 int solve_launches(const pdgb_engine* e) {
-    if (e->solve_mode != PDGB_SOLVE_LEVELS) return 1;
+    if (e->solve_mode != PDGB_SOLVE_LEVELS) return 1;  // PERSISTENT: one launch (and a barrier reset)
     int n = 0;
     for (const SolveLevel& v : e->chol.step_levels)
         n += (v.fwdb_end > v.fwdb_begin) + (v.fwdw_end > v.fwdw_begin) + (v.bwdb_end > v.bwdb_begin) +
@@ -1563,6 +1576,27 @@ int pdgb_closest_rotations(int n, const float* F, float* R, int rotation) {
         PDGB_CUDA_TRY(cudaGetLastError());
         PDGB_CUDA_TRY(cudaMemcpy(R, dR.p, 9 * (size_t)n * sizeof(float), cudaMemcpyDeviceToHost));
     });
+}
+
+int pdgb_grid_sync_check(int ctas, int rounds, int missing, long long spin_limit) {
+    if (ctas < 0 || rounds < 1 || rounds > 1000 || missing < 0 || spin_limit < 1) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad barrier check arguments");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    GridSync h{};
+    const int st = guarded([&] {
+        DBuf<GridSync> bar;
+        bar.alloc(1);
+        launch_grid_sync_check(bar.p, ctas ? ctas : persistent_grid(), rounds, missing, spin_limit, nullptr);
+        PDGB_CUDA_TRY(cudaGetLastError());
+        PDGB_CUDA_TRY(cudaMemcpy(&h, bar.p, sizeof(GridSync), cudaMemcpyDeviceToHost));
+    });
+    if (st != PDGB_OK) return st;
+    if (h.timeout) {
+        set_last_error(PDGB_ERR_TIMEOUT, "grid barrier wait ran out of its bound");
+        return PDGB_ERR_TIMEOUT;
+    }
+    return PDGB_OK;
 }
 
 const char* pdgb_version(void) { return "pdgb 0.2 (sm_103a)"; }

@@ -19,9 +19,20 @@
 //      while the set of requests stays the same;
 //   3. retires the requests that reached their step count: state copied to
 //      host memory, memory returned to the pool and arenas.
+// The tick does not wait for its step: while the step runs, it admits the
+// next requests and prepares the next step's work lists (their uploads are
+// ordered after the step on the stream), and the next tick waits for the
+// step before it hands out the results of the requests it finished.
 // Requests join and leave between steps, their work shares every launch,
 // and a request's arithmetic is the single engine's (same kernels, own
 // arrays), so its result does not depend on the mix.
+//
+// Uploads come from page-locked images kept with the cached mesh: the tile
+// layout as laid out in a request's block, and (Cholesky) the row lists,
+// the solve's work items and, once computed, the numeric factor.  A
+// request's work items stay in a device arena with its offsets applied on
+// the device; the combined per-level lists of a step are gathered from them
+// by a kernel, so the host only writes a table of segments per step.
 //
 // Memory.  Jacobi requests keep everything in their block.  Cholesky
 // requests keep the vectors the solve reaches through its row lists (the
@@ -59,14 +70,41 @@ enum : int { kQueued = 0, kPreparing = 1, kReady = 2, kRunning = 3, kDone = 4, k
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Page-locked host buffer (asynchronous uploads).
+template <class T> struct Pinned {
+    T* p = nullptr;
+    size_t n = 0;
+    Pinned() = default;
+    Pinned(const Pinned&) = delete;
+    Pinned& operator=(const Pinned&) = delete;
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+    void reserve(size_t count) {
+        if (count <= n && p) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        PDGB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&p), std::max<size_t>(count, 1) * sizeof(T)));
+        n = std::max<size_t>(count, 1);
+    }
+};
+
+constexpr int kItemKinds = 6;  // fwd blocks, bwd blocks, fwd small, bwd small, tiny, z staging
+
 // What the workers prepare for a mesh, shared by the requests that submit
-// the same mesh (cache by content).
+// the same mesh (cache by content).  The images are built by the tick
+// thread at the mesh's first admission and used by it only.
 struct MeshEntry {
     std::shared_ptr<const HostLayout> L;
     std::shared_ptr<CholFactor> f;  // symbolic factor + front plan (Cholesky servers)
-    // numeric factor: host copy of the M_s blocks once the GPU has computed
-    // them (written and read by the tick thread only)
-    std::vector<float> mval;
+    bool images = false;
+    size_t layout_bytes = 0;        // tile layout part of a request's block
+    Pinned<unsigned char> layout;   // that part, as laid out in the block
+    Pinned<int> rows;               // row lists (mesh vertex ids)
+    Pinned<int> items;              // work items of the 6 kinds, back to back (mesh offsets)
+    int64_t kbase[kItemKinds + 1] = {0};  // ints: start of each kind in items
+    Pinned<float> mval;             // numeric factor once computed
     bool numeric = false;
 };
 
@@ -167,7 +205,7 @@ struct Request {
     int* flag = nullptr;                  // non-finite state (device)
     int flag_host = 0;
     // arena ranges of a Cholesky request
-    int64_t v0 = 0, m0 = 0, r0 = 0, z0 = 0;
+    int64_t v0 = 0, m0 = 0, r0 = 0, z0 = 0, io = 0;
     float4 *x = nullptr, *v = nullptr, *prev = nullptr, *base = nullptr;
     const float4 *coef = nullptr, *pin = nullptr;
     std::vector<float> X_out, V_out;
@@ -175,6 +213,19 @@ struct Request {
 };
 
 template <class T> size_t bytes_of(const std::vector<T>& v) { return align256(v.size() * sizeof(T)); }
+
+int64_t item_ints(const CholFactor& f) {
+    return (int64_t)(f.fwd_blocks.size() + f.bwd_blocks.size() + f.fwd_small.size() + f.bwd_small.size() +
+                     f.tiny.size() + f.zstage.size());
+}
+
+// Arena bytes of a Cholesky request: 3 solve vectors, rows, M_s, backward
+// staging and work items.
+size_t arena_bytes(const Request& r) {
+    const CholFactor& f = *r.me->f;
+    return 3 * (size_t)r.nv * sizeof(float4) + f.rows.size() * sizeof(int) + (size_t)f.mval_size * sizeof(float) +
+           (size_t)f.zrows * sizeof(float4) + (size_t)item_ints(f) * sizeof(int);
+}
 
 // Device bytes of a prepared request: its block (layout arrays, the state
 // vectors it owns, staging for the state transfers, the status word) and,
@@ -187,12 +238,58 @@ size_t request_bytes(const Request& r, bool chol) {
     b += (chol ? 4 : 6) * align256((size_t)r.nv * sizeof(float4));  // x, v, prev, base (+ sn, b)
     b += align256(6 * (size_t)r.nv * sizeof(float));                // staging
     b += 256;                                                         // status word
-    if (chol) {
-        const CholFactor& f = *r.me->f;
-        b += 3 * (size_t)r.nv * sizeof(float4) + f.rows.size() * sizeof(int) + (size_t)f.mval_size * sizeof(float) +
-             (size_t)f.zrows * sizeof(float4);
-    }
+    if (chol) b += arena_bytes(r);
     return b;
+}
+
+// A run of work items copied into a step's combined list: cnt ints from
+// items[src] to comb[kind][dst].
+struct ItemSeg {
+    long long src;
+    int cnt;
+    int dst;
+    int kind;
+    int pad;
+};
+
+struct CombPtrs {
+    int* p[kItemKinds];
+};
+
+__global__ void __launch_bounds__(256) k_gather_items(const int* __restrict__ items,
+                                                      const ItemSeg* __restrict__ seg, CombPtrs comb) {
+    const ItemSeg g = seg[blockIdx.x];
+    int* dst = comb.p[g.kind] + g.dst;
+    const int* src = items + g.src;
+    for (int i = threadIdx.x; i < g.cnt; i += blockDim.x) dst[i] = __ldg(src + i);
+}
+
+__global__ void k_add_offset(int* a, int64_t n, int off) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] += off;
+}
+
+// A request's work items (kinds back to back, kb[k] = first item of kind k)
+// moved to its arena ranges: factor offset m0 into the 64-bit field of
+// ints 0-1, row-list offset r0 into int 2, backward staging offset z0 into
+// int 7 of the backward blocks (kind 1) and staging items (kind 5).
+struct ItemShift {
+    long long m0;
+    int r0, z0;
+    long long kb[kItemKinds + 1];
+};
+
+__global__ void k_shift_items(int* items, ItemShift sh) {
+    const long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= sh.kb[kItemKinds]) return;
+    int kind = 0;
+    while (kind + 1 < kItemKinds && it >= sh.kb[kind + 1]) ++kind;
+    int* w = items + it * kItemInts;
+    const long long mo = ((long long)(uint32_t)w[0] | ((long long)w[1] << 32)) + sh.m0;
+    w[0] = (int)(mo & 0xffffffff);
+    w[1] = (int)(mo >> 32);
+    w[2] += sh.r0;
+    if (kind == 1 || kind == 5) w[7] += sh.z0;
 }
 
 }  // namespace
@@ -235,8 +332,15 @@ struct pdgb_server {
     Arena<float> ar_mval;
     Arena<int> ar_rows;
     Arena<float4> ar_zbuf;
-    DBuf<int> d_fwdb, d_bwdb, d_fwds, d_bwds, d_tiny, d_zst;
+    Arena<int> ar_items;               // every request's work items, its offsets applied
+    DBuf<int> d_comb[kItemKinds];       // the step's combined per-level lists, by kind
+    Pinned<ItemSeg> h_seg;              // segments gathered into them
+    DBuf<ItemSeg> d_seg;
     std::vector<SolveLevel> step_levels;
+    // pipelining: the step launched by the last tick and the requests it finishes
+    bool inflight = false;
+    bool rebuilt = false;               // lists rebuilt since the last wait for the stream
+    std::vector<Request*> retiring;
     // stats
     long long completed = 0, failed = 0, nonfinite = 0;
     double tet_iterations = 0.0;
@@ -472,19 +576,60 @@ void set_args(pdgb_server* S, Request* r) {
     }
 }
 
-// Uploads a prepared request into its device block (and arenas).
+// The page-locked images of a mesh, built at its first admission: the tile
+// layout as carved into a block, and (Cholesky) row lists and work items.
+void build_images(pdgb_server* S, MeshEntry& me) {
+    if (me.images) return;
+    const HostLayout& L = *me.L;
+    auto sz = [](size_t bytes) { return align256(bytes); };
+    const size_t lb = sz(L.inc_ent.size() * 2) + sz(L.inc_end.size() * 2) + sz(L.geo.size() * 4) +
+                      sz(L.tile_tet_ptr.size() * 4) + sz(L.tile_vptr.size() * 4) + sz(L.tile_verts.size() * 4) +
+                      sz(L.vperm.size() * 4) + sz(L.coef.size() * 16) + sz(L.pin_rhs.size() * 16);
+    me.layout.reserve(lb);
+    std::memset(me.layout.p, 0, lb);
+    unsigned char* q = me.layout.p;
+    auto copy = [&](const void* src, size_t bytes) {
+        if (bytes) std::memcpy(q, src, bytes);
+        q += sz(bytes);
+    };
+    copy(L.inc_ent.data(), L.inc_ent.size() * 2);
+    copy(L.inc_end.data(), L.inc_end.size() * 2);
+    copy(L.geo.data(), L.geo.size() * 4);
+    copy(L.tile_tet_ptr.data(), L.tile_tet_ptr.size() * 4);
+    copy(L.tile_vptr.data(), L.tile_vptr.size() * 4);
+    copy(L.tile_verts.data(), L.tile_verts.size() * 4);
+    copy(L.vperm.data(), L.vperm.size() * 4);
+    copy(L.coef.data(), L.coef.size() * 16);
+    copy(L.pin_rhs.data(), L.pin_rhs.size() * 16);
+    me.layout_bytes = lb;
+    if (S->chol) {
+        const CholFactor& f = *me.f;
+        me.rows.reserve(f.rows.size());
+        if (!f.rows.empty()) std::memcpy(me.rows.p, f.rows.data(), f.rows.size() * sizeof(int));
+        const std::vector<int>* kinds[kItemKinds] = {&f.fwd_blocks, &f.bwd_blocks, &f.fwd_small,
+                                                     &f.bwd_small,  &f.tiny,       &f.zstage};
+        me.kbase[0] = 0;
+        for (int k = 0; k < kItemKinds; ++k) me.kbase[k + 1] = me.kbase[k] + (int64_t)kinds[k]->size();
+        me.items.reserve((size_t)me.kbase[kItemKinds]);
+        for (int k = 0; k < kItemKinds; ++k)
+            if (!kinds[k]->empty())
+                std::memcpy(me.items.p + me.kbase[k], kinds[k]->data(), kinds[k]->size() * sizeof(int));
+    }
+    me.images = true;
+}
+
+// Uploads a prepared request into its device block (and arenas).  The
+// copies are ordered on the stream after any step in flight.
 void admit(pdgb_server* S, Request* r) {
     cudaStream_t s = S->stream;
+    MeshEntry& me = *r->me;
+    build_images(S, me);
     const HostLayout& L = *r->L;
     const int nv = r->nv;
     const bool chol = S->chol;
-    size_t block_bytes = r->bytes;
-    if (chol) {  // the arena part of r->bytes is not in the block
-        const CholFactor& f = *r->me->f;
-        block_bytes -= 3 * (size_t)nv * sizeof(float4) + f.rows.size() * sizeof(int) +
-                       (size_t)f.mval_size * sizeof(float) + (size_t)f.zrows * sizeof(float4);
-    }
+    const size_t block_bytes = r->bytes - (chol ? arena_bytes(*r) : 0);
     PDGB_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r->block), block_bytes, S->pool, s));
+    PDGB_CUDA_TRY(cudaMemcpyAsync(r->block, me.layout.p, me.layout_bytes, cudaMemcpyHostToDevice, s));
     unsigned char* p = r->block;
     uint16_t* inc_ent = carve<uint16_t>(p, L.inc_ent.size());
     uint16_t* inc_end = carve<uint16_t>(p, L.inc_end.size());
@@ -495,6 +640,7 @@ void admit(pdgb_server* S, Request* r) {
     r->vperm = carve<int>(p, L.vperm.size());
     float4* coef = carve<float4>(p, L.coef.size());
     float4* pin = carve<float4>(p, L.pin_rhs.size());
+    if ((size_t)(p - r->block) != me.layout_bytes) throw Error{PDGB_ERR_CUDA, "server: layout image mismatch"};
     r->coef = coef;
     r->pin = pin;
     r->x = carve<float4>(p, nv);
@@ -509,15 +655,6 @@ void admit(pdgb_server* S, Request* r) {
     }
     r->staging = carve<float>(p, 6 * (size_t)nv);
     r->flag = carve<int>(p, 1);
-    put(s, inc_ent, L.inc_ent);
-    put(s, inc_end, L.inc_end);
-    put(s, geo, L.geo);
-    put(s, ttp, L.tile_tet_ptr);
-    put(s, tvp, L.tile_vptr);
-    put(s, tv, L.tile_verts);
-    put(s, r->vperm, L.vperm);
-    put(s, coef, L.coef);
-    put(s, pin, L.pin_rhs);
     PDGB_CUDA_TRY(cudaMemsetAsync(r->flag, 0, sizeof(int), s));
     PDGB_CUDA_TRY(cudaMemsetAsync(r->prev, 0, (size_t)nv * sizeof(float4), s));
     PDGB_CUDA_TRY(cudaMemcpyAsync(r->staging, r->X.data(), 3 * (size_t)nv * sizeof(float), cudaMemcpyHostToDevice, s));
@@ -529,46 +666,61 @@ void admit(pdgb_server* S, Request* r) {
     PDGB_CUDA_TRY(cudaGetLastError());
     r->la = LocalArgs{sn, b, inc_ent, inc_end, geo, ttp, tvp, tv, L.nt_pad, nullptr};
     if (chol) {
-        MeshEntry& me = *r->me;
         const CholFactor& f = *me.f;
-        int64_t v0, m0, r0, z0, tmp;
+        int64_t v0, m0, r0, z0, io, tmp;
+        const int64_t nitems = me.kbase[kItemKinds];
         bool moved = S->va_sn.take(nv, v0, s);
         moved |= S->va_b.take(nv, tmp, s);
         moved |= S->va_y.take(nv, tmp, s);
         moved |= S->ar_mval.take(f.mval_size, m0, s);
         moved |= S->ar_rows.take((int64_t)f.rows.size(), r0, s);
         moved |= S->ar_zbuf.take(f.zrows, z0, s);
-        if (moved) S->graph_dirty = true;  // every request's arena pointers change
+        moved |= S->ar_items.take(nitems, io, s);
+        if (moved) S->lists_dirty = true;  // every request's arena pointers change
         r->v0 = v0;
         r->m0 = m0;
         r->r0 = r0;
         r->z0 = z0;
-        // row lists as arena vertex ids
-        std::vector<int> rows(f.rows.size());
-        for (size_t i = 0; i < rows.size(); ++i) rows[i] = f.rows[i] + (int)v0;
-        if (!rows.empty())
-            PDGB_CUDA_TRY(cudaMemcpyAsync(S->ar_rows.p + r0, rows.data(), rows.size() * sizeof(int),
+        r->io = io;
+        const int64_t nrows = (int64_t)f.rows.size();
+        if (nrows) {
+            PDGB_CUDA_TRY(cudaMemcpyAsync(S->ar_rows.p + r0, me.rows.p, (size_t)nrows * sizeof(int),
                                           cudaMemcpyHostToDevice, s));
+            k_add_offset<<<(unsigned)((nrows + 255) / 256), 256, 0, s>>>(S->ar_rows.p + r0, nrows, (int)v0);
+        }
+        if (nitems) {
+            PDGB_CUDA_TRY(cudaMemcpyAsync(S->ar_items.p + io, me.items.p, (size_t)nitems * sizeof(int),
+                                          cudaMemcpyHostToDevice, s));
+            ItemShift sh{};
+            sh.m0 = m0;
+            sh.r0 = (int)r0;
+            sh.z0 = (int)z0;
+            for (int k = 0; k <= kItemKinds; ++k) sh.kb[k] = me.kbase[k] / kItemInts;
+            const long long n = sh.kb[kItemKinds];
+            if (n) k_shift_items<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(S->ar_items.p + io, sh);
+        }
         PDGB_CUDA_TRY(cudaMemsetAsync(S->va_y.p + v0, 0, (size_t)nv * sizeof(float4), s));
         // the numeric factor: computed on the GPU the first time the mesh is
-        // seen, uploaded from the host copy after that
+        // seen, uploaded from the page-locked copy after that
         if (me.numeric) {
-            if (!me.mval.empty())
-                PDGB_CUDA_TRY(cudaMemcpyAsync(S->ar_mval.p + m0, me.mval.data(), me.mval.size() * sizeof(float),
+            if (f.mval_size)
+                PDGB_CUDA_TRY(cudaMemcpyAsync(S->ar_mval.p + m0, me.mval.p, (size_t)f.mval_size * sizeof(float),
                                               cudaMemcpyHostToDevice, s));
             S->factor_hits++;
         } else {
             S->factor_ms += gpu_factor(f, S->ar_mval.p + m0, s);
             S->factors++;
             if (S->cache_cap > 0) {
-                me.mval.resize((size_t)f.mval_size);
-                if (!me.mval.empty())
-                    PDGB_CUDA_TRY(cudaMemcpy(me.mval.data(), S->ar_mval.p + m0, me.mval.size() * sizeof(float),
-                                             cudaMemcpyDeviceToHost));
+                me.mval.reserve((size_t)f.mval_size);
+                if (f.mval_size)
+                    PDGB_CUDA_TRY(cudaMemcpyAsync(me.mval.p, S->ar_mval.p + m0, (size_t)f.mval_size * sizeof(float),
+                                                  cudaMemcpyDeviceToHost, s));
+                PDGB_CUDA_TRY(cudaStreamSynchronize(s));
                 me.numeric = true;
                 me.f->fp = FrontPlan();  // the front plan is not needed again
             }
         }
+        PDGB_CUDA_TRY(cudaGetLastError());
     }
     set_args(S, r);
     r->state = kRunning;
@@ -586,6 +738,7 @@ void release_arenas(pdgb_server* S, Request* r) {
     S->ar_mval.give(r->m0, f.mval_size);
     S->ar_rows.give(r->r0, (int64_t)f.rows.size());
     S->ar_zbuf.give(r->z0, f.zrows);
+    S->ar_items.give(r->io, r->me->kbase[kItemKinds]);
 }
 
 void ensure_capacity(pdgb_server* S, int nreq, int ntiles, int nchunks) {
@@ -627,10 +780,9 @@ void ensure_capacity(pdgb_server* S, int nreq, int ntiles, int nchunks) {
     S->graph_dirty = true;  // the step graph bakes the list pointers and grid sizes
 }
 
-// The step graph.  Jacobi: grids sized by the list capacities (CTAs past the
-// current counts exit), so it survives changes of the active set.  Cholesky:
-// the per-level solve launches follow the active requests' trees, so it is
-// captured again whenever the set changes.
+// Jacobi: the step as a CUDA graph, grids sized by the list capacities
+// (CTAs past the current counts exit), so it survives changes of the active
+// set; captured again only when the capacities grow.
 void capture_step(pdgb_server* S) {
     if (S->gexec) cudaGraphExecDestroy(S->gexec);
     if (S->graph) cudaGraphDestroy(S->graph);
@@ -638,40 +790,17 @@ void capture_step(pdgb_server* S) {
     S->graph = nullptr;
     cudaStream_t s = S->stream;
     const int n = S->cfg.params.num_iterations;
+    const std::vector<float> omega = chebyshev_omegas(n, S->cfg.params.rho);
     PDGB_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     try {
         launch_begin_multi(S->d_ba, S->d_chunks, S->d_counts + 1, S->cap_chunks, s);
-        if (!S->chol) {
-            const std::vector<float> omega = chebyshev_omegas(n, S->cfg.params.rho);
-            for (int i = 0; i < n; ++i) {
-                launch_local_multi(S->d_la, S->d_tiles, S->d_counts, S->cap_tiles, s, true);
-                int mode = 0;
-                if (i >= 11) mode |= kReadPrev;
-                if (i >= 10 && i + 1 < n) mode |= kWritePrev;
-                if (i + 1 == n) mode |= kFinal;
-                launch_jacobi_vertex_multi(S->d_va, S->d_chunks, S->d_counts + 1, S->cap_chunks, mode, omega[i], s);
-            }
-        } else {
-            CholArgs ca{};
-            ca.rows = S->ar_rows.p;
-            ca.mval = S->ar_mval.p;
-            ca.r = S->va_b.p;
-            ca.y = S->va_y.p;
-            ca.x = S->va_sn.p;
-            ca.done = nullptr;
-            ca.fwd_blocks = S->d_fwdb.p;
-            ca.bwd_blocks = S->d_bwdb.p;
-            ca.fwd_small = S->d_fwds.p;
-            ca.bwd_small = S->d_bwds.p;
-            ca.tiny = S->d_tiny.p;
-            ca.zstage = S->d_zst.p;
-            ca.zbuf = S->ar_zbuf.p;
-            for (int i = 0; i < n; ++i) {
-                launch_local_multi(S->d_la, S->d_tiles, S->d_counts, S->cap_tiles, s, false);
-                launch_chol_solve_levels(ca, S->step_levels, s);
-                launch_chol_vertex_multi(S->d_cv, S->d_chunks, S->d_counts + 1, S->cap_chunks, s);
-            }
-            launch_chol_finish_multi(S->d_cv, S->d_chunks, S->d_counts + 1, S->cap_chunks, s);
+        for (int i = 0; i < n; ++i) {
+            launch_local_multi(S->d_la, S->d_tiles, S->d_counts, S->cap_tiles, s, true);
+            int mode = 0;
+            if (i >= 11) mode |= kReadPrev;
+            if (i >= 10 && i + 1 < n) mode |= kWritePrev;
+            if (i + 1 == n) mode |= kFinal;
+            launch_jacobi_vertex_multi(S->d_va, S->d_chunks, S->d_counts + 1, S->cap_chunks, mode, omega[i], s);
         }
     } catch (...) {
         cudaGraph_t g = nullptr;
@@ -685,70 +814,125 @@ void capture_step(pdgb_server* S) {
     S->graph_dirty = false;
 }
 
-// Per-level solve items of all active Cholesky requests: level L of every
-// request's tree in the same lists (levels counted from the leaves), with
-// each request's offsets into the arenas (factor, rows, staging) added.
+// One PD step for every active request.  Cholesky: direct launches, since
+// the per-level solve launches follow the active requests' trees and the
+// set changes from one step to the next (the host issues them while the GPU
+// works through them).
+void launch_step(pdgb_server* S) {
+    cudaStream_t s = S->stream;
+    if (!S->chol) {
+        PDGB_CUDA_TRY(cudaGraphLaunch(S->gexec, s));
+        return;
+    }
+    const int n = S->cfg.params.num_iterations;
+    CholArgs ca{};
+    ca.rows = S->ar_rows.p;
+    ca.mval = S->ar_mval.p;
+    ca.r = S->va_b.p;
+    ca.y = S->va_y.p;
+    ca.x = S->va_sn.p;
+    ca.done = nullptr;
+    ca.fwd_blocks = S->d_comb[0].p;
+    ca.bwd_blocks = S->d_comb[1].p;
+    ca.fwd_small = S->d_comb[2].p;
+    ca.bwd_small = S->d_comb[3].p;
+    ca.tiny = S->d_comb[4].p;
+    ca.zstage = S->d_comb[5].p;
+    ca.zbuf = S->ar_zbuf.p;
+    launch_begin_multi(S->d_ba, S->d_chunks, S->d_counts + 1, S->cap_chunks, s);
+    for (int i = 0; i < n; ++i) {
+        launch_local_multi(S->d_la, S->d_tiles, S->d_counts, S->cap_tiles, s, false);
+        launch_chol_solve_levels(ca, S->step_levels, s);
+        launch_chol_vertex_multi(S->d_cv, S->d_chunks, S->d_counts + 1, S->cap_chunks, s);
+    }
+    launch_chol_finish_multi(S->d_cv, S->d_chunks, S->d_counts + 1, S->cap_chunks, s);
+    PDGB_CUDA_TRY(cudaGetLastError());
+}
+
+// Per-level solve lists of all active Cholesky requests: level L of every
+// request's tree in the same lists (levels counted from the leaves).  The
+// host writes one segment per (level, request, kind) -- where the request's
+// items of that level lie in the items arena (its offsets already applied)
+// and where they go -- and a kernel gathers the items on the device.
 void build_solve_lists(pdgb_server* S) {
-    std::vector<int> fwdb, bwdb, fwds, bwds, tiny, zst;
     int nl = 0;
     for (Request* r : S->active) nl = std::max(nl, (int)r->me->f->step_levels.size());
     S->step_levels.assign(nl, SolveLevel{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0});
-    auto append = [](std::vector<int>& dst, const std::vector<int>& src, int b0, int b1, int64_t m0, int64_t r0,
-                     int64_t z0, bool zfield) {
-        for (int it = b0; it < b1; ++it) {
-            const int* w = &src[(size_t)kItemInts * it];
-            const int64_t mo = ((int64_t)(uint32_t)w[0] | ((int64_t)w[1] << 32)) + m0;
-            dst.push_back((int)(mo & 0xffffffff));
-            dst.push_back((int)(mo >> 32));
-            dst.push_back(w[2] + (int)r0);
-            for (int j = 3; j < kItemInts - 1; ++j) dst.push_back(w[j]);
-            dst.push_back(w[kItemInts - 1] + (zfield ? (int)z0 : 0));
+    std::vector<ItemSeg> seg;
+    seg.reserve((size_t)nl * S->active.size() * 2);
+    int64_t tot[kItemKinds] = {0};
+    auto range = [](const SolveLevel& q, int k, int& b, int& e) {
+        switch (k) {
+            case 0: b = q.fwdb_begin; e = q.fwdb_end; break;
+            case 1: b = q.bwdb_begin; e = q.bwdb_end; break;
+            case 2: b = q.fwdw_begin; e = q.fwdw_end; break;
+            case 3: b = q.bwdw_begin; e = q.bwdw_end; break;
+            case 4: b = q.tiny_begin; e = q.tiny_end; break;
+            default: b = q.zst_begin; e = q.zst_end; break;
         }
     };
     for (int L = 0; L < nl; ++L) {
-        SolveLevel& lv = S->step_levels[L];
-        lv.fwdb_begin = (int)(fwdb.size() / kItemInts);
-        lv.bwdb_begin = (int)(bwdb.size() / kItemInts);
-        lv.fwdw_begin = (int)(fwds.size() / kItemInts);
-        lv.bwdw_begin = (int)(bwds.size() / kItemInts);
-        lv.tiny_begin = (int)(tiny.size() / kItemInts);
-        lv.zst_begin = (int)(zst.size() / kItemInts);
+        int begin[kItemKinds];
+        for (int k = 0; k < kItemKinds; ++k) begin[k] = (int)(tot[k] / kItemInts);
         for (Request* r : S->active) {
             const CholFactor& f = *r->me->f;
             if (L >= (int)f.step_levels.size()) continue;
             const SolveLevel& q = f.step_levels[L];
-            append(fwdb, f.fwd_blocks, q.fwdb_begin, q.fwdb_end, r->m0, r->r0, r->z0, false);
-            append(bwdb, f.bwd_blocks, q.bwdb_begin, q.bwdb_end, r->m0, r->r0, r->z0, true);
-            append(fwds, f.fwd_small, q.fwdw_begin, q.fwdw_end, r->m0, r->r0, r->z0, false);
-            append(bwds, f.bwd_small, q.bwdw_begin, q.bwdw_end, r->m0, r->r0, r->z0, false);
-            append(tiny, f.tiny, q.tiny_begin, q.tiny_end, r->m0, r->r0, r->z0, false);
-            append(zst, f.zstage, q.zst_begin, q.zst_end, r->m0, r->r0, r->z0, true);
+            for (int k = 0; k < kItemKinds; ++k) {
+                int b, e;
+                range(q, k, b, e);
+                if (e <= b) continue;
+                const int cnt = (e - b) * kItemInts;
+                seg.push_back(ItemSeg{(long long)(r->io + r->me->kbase[k] + (int64_t)b * kItemInts), cnt,
+                                      (int)tot[k], k, 0});
+                tot[k] += cnt;
+            }
         }
-        lv.fwdb_end = (int)(fwdb.size() / kItemInts);
-        lv.bwdb_end = (int)(bwdb.size() / kItemInts);
-        lv.fwdw_end = (int)(fwds.size() / kItemInts);
-        lv.bwdw_end = (int)(bwds.size() / kItemInts);
-        lv.tiny_end = (int)(tiny.size() / kItemInts);
-        lv.zst_end = (int)(zst.size() / kItemInts);
+        SolveLevel& lv = S->step_levels[L];
+        int end[kItemKinds];
+        for (int k = 0; k < kItemKinds; ++k) end[k] = (int)(tot[k] / kItemInts);
+        lv.fwdb_begin = begin[0]; lv.fwdb_end = end[0];
+        lv.bwdb_begin = begin[1]; lv.bwdb_end = end[1];
+        lv.fwdw_begin = begin[2]; lv.fwdw_end = end[2];
+        lv.bwdw_begin = begin[3]; lv.bwdw_end = end[3];
+        lv.tiny_begin = begin[4]; lv.tiny_end = end[4];
+        lv.zst_begin = begin[5]; lv.zst_end = end[5];
     }
     cudaStream_t s = S->stream;
-    S->d_fwdb.upload(fwdb, s);
-    S->d_bwdb.upload(bwdb, s);
-    S->d_fwds.upload(fwds, s);
-    S->d_bwds.upload(bwds, s);
-    S->d_tiny.upload(tiny, s);
-    S->d_zst.upload(zst, s);
-    S->graph_dirty = true;
+    bool grow = seg.size() > S->h_seg.n || seg.size() > S->d_seg.n;
+    for (int k = 0; k < kItemKinds; ++k) grow |= (size_t)tot[k] > S->d_comb[k].n;
+    if (grow) {
+        // the buffers may be in use by the step in flight
+        PDGB_CUDA_TRY(cudaStreamSynchronize(s));
+        if (seg.size() > S->h_seg.n) S->h_seg.reserve(seg.size() * 2);
+        if (seg.size() > S->d_seg.n) S->d_seg.alloc(seg.size() * 2);
+        for (int k = 0; k < kItemKinds; ++k)
+            if ((size_t)tot[k] > S->d_comb[k].n) S->d_comb[k].alloc((size_t)tot[k] * 2);
+    }
+    if (!seg.empty()) {
+        std::memcpy(S->h_seg.p, seg.data(), seg.size() * sizeof(ItemSeg));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_seg.p, S->h_seg.p, seg.size() * sizeof(ItemSeg), cudaMemcpyHostToDevice, s));
+        CombPtrs cp;
+        for (int k = 0; k < kItemKinds; ++k) cp.p[k] = S->d_comb[k].p;
+        k_gather_items<<<(unsigned)seg.size(), 256, 0, s>>>(S->ar_items.p, S->d_seg.p, cp);
+        PDGB_CUDA_TRY(cudaGetLastError());
+    }
 }
 
+// Work lists of the next step.  Uploads are ordered on the stream after any
+// step in flight; the page-locked mirrors they read were last read by the
+// uploads of an earlier tick, which the wait at the start of this tick has
+// completed -- unless the lists were already rebuilt since that wait, in
+// which case their uploads may be pending and the stream is waited for.
 void rebuild_lists(pdgb_server* S) {
+    if (S->rebuilt) PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));
+    S->rebuilt = true;
     int ntiles = 0, nchunks = 0;
     for (Request* r : S->active) {
         ntiles += r->L->ntiles;
         nchunks += (r->nv + 255) / 256;
     }
     ensure_capacity(S, (int)S->active.size(), ntiles, nchunks);
-    PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));  // host mirrors and lists may still be in flight
     if (S->chol) {
         for (Request* r : S->active) set_args(S, r);  // arenas may have moved
         build_solve_lists(S);
@@ -776,8 +960,103 @@ void rebuild_lists(pdgb_server* S) {
         PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_chunks, S->h_chunks, c * sizeof(int2), cudaMemcpyHostToDevice, s));
     }
     PDGB_CUDA_TRY(cudaMemcpyAsync(S->d_counts, S->h_counts, 2 * sizeof(int), cudaMemcpyHostToDevice, s));
-    if (S->graph_dirty) capture_step(S);
+    if (!S->chol && S->graph_dirty) capture_step(S);
+    if (S->chol) S->graph_dirty = false;  // no graph: the step is launched directly
     S->lists_dirty = false;
+}
+
+// Admission in arrival order, by HBM budget and slot limit (server lock held).
+void admit_ready(pdgb_server* S) {
+    while (!S->ready_queue.empty()) {
+        if (S->cfg.max_active > 0 && (int)S->active.size() >= S->cfg.max_active) break;
+        auto it = S->reqs.find(S->ready_queue.front());
+        if (it == S->reqs.end()) {
+            S->ready_queue.pop_front();
+            continue;
+        }
+        Request* r = it->second.get();
+        if (S->bytes_in_use + r->bytes > S->cfg.hbm_budget_bytes) {
+            if (S->active.empty() && S->retiring.empty() && r->bytes > S->cfg.hbm_budget_bytes) {
+                r->state = kFailed;  // can never fit
+                r->error = "request larger than the HBM budget";
+                S->failed++;
+                S->ready_queue.pop_front();
+                continue;
+            }
+            break;
+        }
+        S->ready_queue.pop_front();
+        try {
+            admit(S, r);
+        } catch (const Error& e) {
+            // a factor that is not positive definite fails the request
+            // alone; anything else fails the tick
+            if (e.status != PDGB_ERR_NOT_SPD) throw;
+            if (r->block) PDGB_CUDA_TRY(cudaFreeAsync(r->block, S->stream));
+            r->block = nullptr;
+            release_arenas(S, r);
+            r->state = kFailed;
+            r->error = e.msg;
+            S->failed++;
+            continue;
+        }
+        S->active.push_back(r);
+        S->lists_dirty = true;
+    }
+}
+
+// Requests that reached their step count with the step just launched: their
+// state is copied to the host and their memory released, ordered after the
+// step; they are handed out once the next tick has waited for it.
+void retire_finished(pdgb_server* S) {
+    std::vector<Request*> keep;
+    for (Request* r : S->active) {
+        r->steps_done++;
+        S->tet_iterations += (double)r->nt * S->cfg.params.num_iterations;
+        if (r->steps_done < r->nsteps) {
+            keep.push_back(r);
+            continue;
+        }
+        const size_t n3 = 3 * (size_t)r->nv;
+        r->X_out.resize(n3);
+        r->V_out.resize(n3);
+        launch_scatter_state(r->nv, r->vperm, r->x, r->v, r->staging, r->staging + n3, S->stream);
+        PDGB_CUDA_TRY(
+            cudaMemcpyAsync(r->X_out.data(), r->staging, n3 * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
+        PDGB_CUDA_TRY(
+            cudaMemcpyAsync(r->V_out.data(), r->staging + n3, n3 * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(&r->flag_host, r->flag, sizeof(int), cudaMemcpyDeviceToHost, S->stream));
+        PDGB_CUDA_TRY(cudaFreeAsync(r->block, S->stream));
+        r->block = nullptr;
+        release_arenas(S, r);  // reused only by uploads ordered after this step
+        S->bytes_in_use -= r->bytes;
+        S->lists_dirty = true;
+        S->retiring.push_back(r);
+    }
+    S->active.swap(keep);
+}
+
+// After the wait for the step: the retired requests' results are on the host.
+int hand_out(pdgb_server* S, Clock::time_point now) {
+    int n = 0;
+    for (Request* r : S->retiring) {
+        r->t_done = now;
+        S->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
+        if (r->flag_host) {
+            // the iteration left the finite range: a failed request, not a
+            // silent NaN result
+            r->state = kFailed;
+            r->error = "the state became non-finite";
+            S->failed++;
+            S->nonfinite++;
+        } else {
+            r->state = kDone;
+            S->completed++;
+        }
+        ++n;
+    }
+    S->retiring.clear();
+    return n;
 }
 
 }  // namespace
@@ -868,106 +1147,44 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
     if (!S) return PDGB_ERR_INVALID_ARGUMENT;
     return guarded_s([&] {
         // The server lock is held for admission and bookkeeping only, not
-        // while the step runs: the layout workers and the submitting threads
-        // need it to make progress.  Only pdgb_server_tick changes the active
-        // set, the arenas and the step graph, so they need no lock of their own.
+        // while waiting for the GPU: the layout workers and the submitting
+        // threads need it to make progress.  Only pdgb_server_tick changes
+        // the active set, the arenas and the step lists, so they need no
+        // lock of their own.
         const auto t0 = Clock::now();
         std::unique_lock<std::mutex> lk(S->mu);
-        // 1. admission in arrival order, by HBM budget and slot limit
-        while (!S->ready_queue.empty()) {
-            if (S->cfg.max_active > 0 && (int)S->active.size() >= S->cfg.max_active) break;
-            auto it = S->reqs.find(S->ready_queue.front());
-            if (it == S->reqs.end()) {
-                S->ready_queue.pop_front();
-                continue;
-            }
-            Request* r = it->second.get();
-            if (S->bytes_in_use + r->bytes > S->cfg.hbm_budget_bytes) {
-                if (S->active.empty() && r->bytes > S->cfg.hbm_budget_bytes) {  // can never fit
-                    r->state = kFailed;
-                    r->error = "request larger than the HBM budget";
-                    S->failed++;
-                    S->ready_queue.pop_front();
-                    continue;
-                }
-                break;
-            }
-            S->ready_queue.pop_front();
-            try {
-                admit(S, r);
-            } catch (const Error& e) {
-                // a factor that is not positive definite fails the request
-                // alone; anything else fails the tick
-                if (e.status != PDGB_ERR_NOT_SPD) throw;
-                if (r->block) PDGB_CUDA_TRY(cudaFreeAsync(r->block, S->stream));
-                r->block = nullptr;
-                release_arenas(S, r);
-                r->state = kFailed;
-                r->error = e.msg;
-                S->failed++;
-                continue;
-            }
-            S->active.push_back(r);
-            S->lists_dirty = true;
-        }
-        const auto t1 = Clock::now();
-        S->admit_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
         int done_now = 0;
-        if (!S->active.empty()) {
-            S->ticks++;
-            if (S->lists_dirty || S->graph_dirty) rebuild_lists(S);
-            // 2. one PD step for every active request
-            PDGB_CUDA_TRY(cudaGraphLaunch(S->gexec, S->stream));
-            // 3. retire finished requests (copies ordered after the step)
-            std::vector<Request*> keep, retired;
-            for (Request* r : S->active) {
-                r->steps_done++;
-                S->tet_iterations += (double)r->nt * S->cfg.params.num_iterations;
-                if (r->steps_done >= r->nsteps) {
-                    const size_t n3 = 3 * (size_t)r->nv;
-                    r->X_out.resize(n3);
-                    r->V_out.resize(n3);
-                    launch_scatter_state(r->nv, r->vperm, r->x, r->v, r->staging, r->staging + n3, S->stream);
-                    PDGB_CUDA_TRY(cudaMemcpyAsync(r->X_out.data(), r->staging, n3 * sizeof(float),
-                                                  cudaMemcpyDeviceToHost, S->stream));
-                    PDGB_CUDA_TRY(cudaMemcpyAsync(r->V_out.data(), r->staging + n3, n3 * sizeof(float),
-                                                  cudaMemcpyDeviceToHost, S->stream));
-                    PDGB_CUDA_TRY(cudaMemcpyAsync(&r->flag_host, r->flag, sizeof(int), cudaMemcpyDeviceToHost,
-                                                  S->stream));
-                    PDGB_CUDA_TRY(cudaFreeAsync(r->block, S->stream));
-                    r->block = nullptr;
-                    release_arenas(S, r);  // reused only by later ticks, after this step
-                    S->bytes_in_use -= r->bytes;
-                    S->lists_dirty = true;
-                    retired.push_back(r);
-                    done_now++;
-                } else {
-                    keep.push_back(r);
-                }
-            }
-            S->active.swap(keep);
+        // 1. wait for the step launched by the previous tick; hand out the
+        //    results of the requests it finished
+        if (S->inflight) {
             lk.unlock();
             PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));
             const auto now = Clock::now();
             lk.lock();
-            S->step_ms += std::chrono::duration<double, std::milli>(now - t1).count();
-            for (Request* r : retired) {  // results are on the host now
-                r->t_done = now;
-                S->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
-                if (r->flag_host) {
-                    // the iteration left the finite range: a failed request,
-                    // not a silent NaN result
-                    r->state = kFailed;
-                    r->error = "the state became non-finite";
-                    S->failed++;
-                    S->nonfinite++;
-                } else {
-                    r->state = kDone;
-                    S->completed++;
-                }
-            }
-            PDGB_CUDA_TRY(cudaGetLastError());
+            S->step_ms += std::chrono::duration<double, std::milli>(now - t0).count();
+            done_now = hand_out(S, now);
+            S->inflight = false;
         }
+        S->rebuilt = false;
+        // 2. admission (requests that became ready while nothing was in flight)
+        const auto t1 = Clock::now();
+        admit_ready(S);
+        double admit = std::chrono::duration<double, std::milli>(Clock::now() - t1).count();
+        if (!S->active.empty()) {
+            S->ticks++;
+            // 3. one PD step for every active request
+            if (S->lists_dirty || S->graph_dirty) rebuild_lists(S);
+            launch_step(S);
+            retire_finished(S);
+            S->inflight = true;
+            // 4. while it runs: the next admissions and the next step's lists
+            const auto t2 = Clock::now();
+            admit_ready(S);
+            if (!S->active.empty() && (S->lists_dirty || S->graph_dirty)) rebuild_lists(S);
+            admit += std::chrono::duration<double, std::milli>(Clock::now() - t2).count();
+        }
+        S->admit_ms += admit;
+        PDGB_CUDA_TRY(cudaGetLastError());
         S->busy_ms += std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
         if (active) *active = (int)S->active.size();
         if (completed) *completed = done_now;
@@ -1035,6 +1252,7 @@ int pdgb_server_get_stats(pdgb_server* S, pdgb_server_stats* out) {
     out->factors = S->factors;
     out->factor_cache_hits = S->factor_hits;
     out->factor_ms = S->factor_ms;
+    out->finishing = (int)S->retiring.size();
     return PDGB_OK;
 }
 

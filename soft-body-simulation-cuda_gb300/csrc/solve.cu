@@ -14,6 +14,8 @@
 
 #include <cooperative_groups.h>
 
+#include <cstdlib>
+
 namespace pdgb {
 
 // The per-level kernels are launched with programmatic dependent launch
@@ -190,10 +192,17 @@ __device__ __forceinline__ void bwd_warp_item_pre(const CholArgs& a, const int* 
 // streams its row of M_s (column-major, so a warp's loads of one column are
 // contiguous), 8 independent loads in flight.  Pivot rows add into y,
 // off-diagonal rows subtract from r (ancestor pivots, read at a later level).
-__global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, int item0) {
-    __shared__ float4 rs[kFwdBlockCols];
-    pdl_trigger();
-    const int* w = a.fwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
+// Static part of a forward block item (no vector reads): the thread's row of
+// M_s (at most kFwdBlockCols columns, zero past cend), its vertex id and
+// the staging index.
+struct FwdBlockPre {
+    float mv[kFwdBlockCols];
+    int vid, sv, ncols, row, k;
+    bool active;
+};
+
+__device__ __forceinline__ void fwd_block_load(const CholArgs& a, int item, FwdBlockPre& p) {
+    const int* w = a.fwd_blocks + (size_t)kItemInts * item;
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
@@ -203,30 +212,43 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
     const bool active = row < m && row < r0 + kFwdBlockRows;
     const int cend = !active ? c0 : (row < k ? min(c1, row + 1) : c1);
     const float* Mr = a.mval + moff + row;
-    // the thread's row of the item (at most kFwdBlockCols columns, zero past
-    // cend) and the staging indices are static: loaded before the wait
-    float mv[kFwdBlockCols];
 #pragma unroll
-    for (int q = 0; q < kFwdBlockCols; ++q) mv[q] = (c0 + q < cend) ? __ldg(Mr + (size_t)(c0 + q) * m) : 0.f;
-    const int vid = active ? __ldg(&rows[row]) : 0;
-    const int ncols = c1 - c0;
-    const int sv = (int)threadIdx.x < ncols ? __ldg(&rows[c0 + threadIdx.x]) : 0;
-    pdl_wait();
-    if (a.done && *a.done) return;
+    for (int q = 0; q < kFwdBlockCols; ++q) p.mv[q] = (c0 + q < cend) ? __ldg(Mr + (size_t)(c0 + q) * m) : 0.f;
+    p.vid = active ? __ldg(&rows[row]) : 0;
+    p.ncols = c1 - c0;
+    p.sv = (int)threadIdx.x < p.ncols ? __ldg(&rows[c0 + threadIdx.x]) : 0;
+    p.row = row;
+    p.k = k;
+    p.active = active;
+}
+
+// Vector part: stage the pivot right-hand sides (one barrier of the whole
+// CTA), then the thread's row sum into y (pivot rows) or r (ancestor rows).
+__device__ __forceinline__ void fwd_block_run(const CholArgs& a, const FwdBlockPre& p, float4* rs) {
     if (threadIdx.x < kFwdBlockCols)
-        rs[threadIdx.x] = (int)threadIdx.x < ncols ? a.r[sv] : make_float4(0.f, 0.f, 0.f, 0.f);
+        rs[threadIdx.x] = (int)threadIdx.x < p.ncols ? a.r[p.sv] : make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
-    if (!active) return;
+    if (!p.active) return;
     float ax = 0.f, ay = 0.f, az = 0.f;
 #pragma unroll
     for (int q = 0; q < kFwdBlockCols; ++q) {
         const float4 v = rs[q];
-        ax = fmaf(mv[q], v.x, ax);
-        ay = fmaf(mv[q], v.y, ay);
-        az = fmaf(mv[q], v.z, az);
+        ax = fmaf(p.mv[q], v.x, ax);
+        ay = fmaf(p.mv[q], v.y, ay);
+        az = fmaf(p.mv[q], v.z, az);
     }
-    if (row < k) atomicAdd(&a.y[vid], make_float4(ax, ay, az, 0.f));
-    else atomicAdd(&a.r[vid], make_float4(-ax, -ay, -az, 0.f));
+    if (p.row < p.k) atomicAdd(&a.y[p.vid], make_float4(ax, ay, az, 0.f));
+    else atomicAdd(&a.r[p.vid], make_float4(-ax, -ay, -az, 0.f));
+}
+
+__global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, int item0) {
+    __shared__ float4 rs[kFwdBlockCols];
+    pdl_trigger();
+    FwdBlockPre p;
+    fwd_block_load(a, item0 + blockIdx.x, p);  // static data before the wait
+    pdl_wait();
+    if (a.done && *a.done) return;
+    fwd_block_run(a, p, rs);
 }
 
 // Backward z staging {roff, m, k, r0, zoff}: z = [y_pivots ; -x_offdiag]
@@ -235,17 +257,18 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_block(CholArgs a, in
 // read it contiguously.  For a supernode whose columns are split into row
 // chunks, x at the pivot rows is cleared here: the backward blocks of the
 // level add their chunk sums into it.
-__global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, int item0) {
-    pdl_trigger();
-    const int* w = a.zstage + (size_t)kItemInts * (item0 + blockIdx.x);
+__device__ __forceinline__ void zstage_item(const CholArgs& a, int item, bool pdl) {
+    const int* w = a.zstage + (size_t)kItemInts * item;
     const int roff = __ldg(w + 2), m = __ldg(w + 3), k = __ldg(w + 4), r0 = __ldg(w + 5), split = __ldg(w + 6),
               zoff = __ldg(w + 7);
     const int* rows = a.rows + roff;
     const int r1 = min(m, r0 + kStageRows);
     const int i0 = r0 + threadIdx.x;
     const int vid0 = i0 < r1 ? __ldg(&rows[i0]) : 0;
-    pdl_wait();
-    if (a.done && *a.done) return;
+    if (pdl) {
+        pdl_wait();
+        if (a.done && *a.done) return;
+    }
     for (int i = i0; i < r1; i += kStageThreads) {
         const int vid = i == i0 ? vid0 : __ldg(&rows[i]);
         float4 z;
@@ -260,68 +283,82 @@ __global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, i
     }
 }
 
-// Backward block {moff, roff, m, r0, c0 | ncols, r1, zoff}: warp w owns the
-// kBwdWarpCols consecutive columns c0 + kBwdWarpCols w .. over the rows
-// r0 .. r1; lanes stride the rows, each z (staged,
-// contiguous) is loaded once and used for all of the warp's columns
-// (contiguous loads of M_s, one per column), then a warp reduction per
-// column whose sum is added into x.  Column c uses rows i >= c only.
-__global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
+__global__ void __launch_bounds__(kStageThreads) k_chol_bwd_zstage(CholArgs a, int item0) {
     pdl_trigger();
-    const int* w = a.bwd_blocks + (size_t)kItemInts * (item0 + blockIdx.x);
+    zstage_item(a, item0 + blockIdx.x, true);
+}
+
+// Static part of a backward block item: the warp's first 256 rows of each
+// of its columns in registers (a whole 256-row chunk).
+constexpr int kBwdPre = 8;
+struct BwdBlockPre {
+    float mpre[kBwdPre][kBwdWarpCols];
+    const float* Mc;
+    const int* rows;
+    const float4* z;
+    int m, r0, rend, cw, nc, ib;
+    bool live;
+};
+
+__device__ __forceinline__ void bwd_block_load(const CholArgs& a, int item, BwdBlockPre& p) {
+    const int* w = a.bwd_blocks + (size_t)kItemInts * item;
     const int4 h0 = __ldg(reinterpret_cast<const int4*>(w));
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
     const int roff = h0.z, m = h0.w, r0 = h1.x, c0 = h1.y & ((1 << kBwdColShift) - 1),
               c1 = c0 + (h1.y >> kBwdColShift), rend = h1.z, zoff = h1.w;
-    const int* rows = a.rows + roff;
-    const float4* z = a.zbuf + zoff;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cw = c0 + kBwdWarpCols * warp;  // first column of this warp
-    const int nc = min(kBwdWarpCols, c1 - cw);
-    const float* Mc = a.mval + moff + (size_t)cw * m;
-    // The warp's first 256 rows of each of its columns (a whole 256-row
-    // chunk) are loaded into registers before the wait; longer columns of
-    // whole-column items stream the rest afterwards.
-    constexpr int kPre = 8;
-    const bool live = cw < c1 && cw < rend;
-    const int ib = max(cw, r0) + lane;
-    float mpre[kPre][kBwdWarpCols];
+    p.nc = min(kBwdWarpCols, c1 - cw);
+    p.Mc = a.mval + moff + (size_t)cw * m;
+    p.rows = a.rows + roff;
+    p.z = a.zbuf + zoff;
+    p.m = m;
+    p.r0 = r0;
+    p.rend = rend;
+    p.cw = cw;
+    p.live = cw < c1 && cw < rend;
+    p.ib = max(cw, r0) + lane;
 #pragma unroll
-    for (int t = 0; t < kPre; ++t) {
-        const int i = ib + 32 * t;
+    for (int t = 0; t < kBwdPre; ++t) {
+        const int i = p.ib + 32 * t;
 #pragma unroll
         for (int j = 0; j < kBwdWarpCols; ++j)
-            mpre[t][j] = (live && j < nc && i < rend && i >= cw + j) ? __ldg(Mc + (size_t)j * m + i) : 0.f;
+            p.mpre[t][j] =
+                (p.live && j < p.nc && i < rend && i >= cw + j) ? __ldg(p.Mc + (size_t)j * m + i) : 0.f;
     }
-    pdl_wait();
-    if (a.done && *a.done) return;
-    if (!live) return;
+}
+
+// Vector part: the staged z against the warp's columns, warp reductions,
+// sums stored (whole column) or added (row chunk) into x.  Warp-level only.
+__device__ __forceinline__ void bwd_block_run(const CholArgs& a, const BwdBlockPre& p) {
+    if (!p.live) return;
+    const int lane = threadIdx.x & 31;
     float acc[kBwdWarpCols][3];
 #pragma unroll
     for (int j = 0; j < kBwdWarpCols; ++j) acc[j][0] = acc[j][1] = acc[j][2] = 0.f;
 #pragma unroll
-    for (int t = 0; t < kPre; ++t) {
-        const int i = ib + 32 * t;
-        if (i < rend) {
-            const float4 zz = z[i];
+    for (int t = 0; t < kBwdPre; ++t) {
+        const int i = p.ib + 32 * t;
+        if (i < p.rend) {
+            const float4 zz = p.z[i];
 #pragma unroll
             for (int j = 0; j < kBwdWarpCols; ++j) {
-                if (j < nc && i >= cw + j) {
-                    acc[j][0] = fmaf(mpre[t][j], zz.x, acc[j][0]);
-                    acc[j][1] = fmaf(mpre[t][j], zz.y, acc[j][1]);
-                    acc[j][2] = fmaf(mpre[t][j], zz.z, acc[j][2]);
+                if (j < p.nc && i >= p.cw + j) {
+                    acc[j][0] = fmaf(p.mpre[t][j], zz.x, acc[j][0]);
+                    acc[j][1] = fmaf(p.mpre[t][j], zz.y, acc[j][1]);
+                    acc[j][2] = fmaf(p.mpre[t][j], zz.z, acc[j][2]);
                 }
             }
         }
     }
 #pragma unroll 2
-    for (int i = ib + 32 * kPre; i < rend; i += 32) {
-        const float4 zz = z[i];
+    for (int i = p.ib + 32 * kBwdPre; i < p.rend; i += 32) {
+        const float4 zz = p.z[i];
 #pragma unroll
         for (int j = 0; j < kBwdWarpCols; ++j) {
-            if (j < nc && i >= cw + j) {
-                const float mv = __ldg(Mc + (size_t)j * m + i);
+            if (j < p.nc && i >= p.cw + j) {
+                const float mv = __ldg(p.Mc + (size_t)j * p.m + i);
                 acc[j][0] = fmaf(mv, zz.x, acc[j][0]);
                 acc[j][1] = fmaf(mv, zz.y, acc[j][1]);
                 acc[j][2] = fmaf(mv, zz.z, acc[j][2]);
@@ -336,13 +373,30 @@ __global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, in
             acc[j][1] += __shfl_xor_sync(0xffffffffu, acc[j][1], off);
             acc[j][2] += __shfl_xor_sync(0xffffffffu, acc[j][2], off);
         }
-        if (lane == 0 && j < nc) {
-            float4* xc = &a.x[__ldg(&rows[cw + j])];
+        if (lane == 0 && j < p.nc) {
+            float4* xc = &a.x[__ldg(&p.rows[p.cw + j])];
             const float4 sum = make_float4(acc[j][0], acc[j][1], acc[j][2], 0.f);
-            if (r0 == 0 && rend == m) *xc = sum;  // the whole column in one item
+            if (p.r0 == 0 && p.rend == p.m) *xc = sum;  // the whole column in one item
             else atomicAdd(xc, sum);
         }
     }
+}
+
+// Backward block {moff, roff, m, r0, c0 | ncols, r1, zoff}: warp w owns the
+// kBwdWarpCols consecutive columns c0 + kBwdWarpCols w .. over the rows
+// r0 .. r1; lanes stride the rows, each z (staged, contiguous) is loaded
+// once and used for all of the warp's columns (contiguous loads of M_s, one
+// per column), then a warp reduction per column whose sum is added into x.
+// Column c uses rows i >= c only.  The warp's first 256 rows of each column
+// are loaded into registers before the wait; longer columns of whole-column
+// items stream the rest afterwards.
+__global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_block(CholArgs a, int item0) {
+    pdl_trigger();
+    BwdBlockPre p;
+    bwd_block_load(a, item0 + blockIdx.x, p);
+    pdl_wait();
+    if (a.done && *a.done) return;
+    bwd_block_run(a, p);
 }
 
 // Small supernodes of a level (per-level launches): one warp item per warp,
@@ -380,15 +434,9 @@ __device__ __forceinline__ void tiny_prefetch(const CholArgs& a, int item) {
 // each instead of one warp per item.  Forward: pivot rows store y (only this
 // supernode writes them), off-diagonal rows subtract from r.  Backward:
 // x_c = sum_{i >= c} M[i, c] z_i over the supernode's rows.
-__global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_tiny(CholArgs a, int t0, int n) {
-    pdl_trigger();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) tiny_prefetch(a, t0 + t);
-    pdl_wait();
-    if (a.done && *a.done) return;
-    if (t >= n) return;
-    const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * (t0 + t)));
-    const int k = __ldg(a.tiny + (size_t)kItemInts * (t0 + t) + 4);
+__device__ __forceinline__ void fwd_tiny_item(const CholArgs& a, int item) {
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * item));
+    const int k = __ldg(a.tiny + (size_t)kItemInts * item + 4);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
     const int m = h0.w;
     const int* rows = a.rows + h0.z;
@@ -414,15 +462,9 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_tiny(CholArgs a, int
     }
 }
 
-__global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int t0, int n) {
-    pdl_trigger();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) tiny_prefetch(a, t0 + t);
-    pdl_wait();
-    if (a.done && *a.done) return;
-    if (t >= n) return;
-    const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * (t0 + t)));
-    const int k = __ldg(a.tiny + (size_t)kItemInts * (t0 + t) + 4);
+__device__ __forceinline__ void bwd_tiny_item(const CholArgs& a, int item) {
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(a.tiny + (size_t)kItemInts * item));
+    const int k = __ldg(a.tiny + (size_t)kItemInts * item + 4);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
     const int m = h0.w;
     const int* rows = a.rows + h0.z;
@@ -454,6 +496,24 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int
         if (c < k) a.x[__ldg(&rows[c])] = make_float4(acc[c][0], acc[c][1], acc[c][2], 0.f);
 }
 
+__global__ void __launch_bounds__(kSmallThreads) k_chol_fwd_tiny(CholArgs a, int t0, int n) {
+    pdl_trigger();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) tiny_prefetch(a, t0 + t);
+    pdl_wait();
+    if (a.done && *a.done) return;
+    if (t < n) fwd_tiny_item(a, t0 + t);
+}
+
+__global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int t0, int n) {
+    pdl_trigger();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) tiny_prefetch(a, t0 + t);
+    pdl_wait();
+    if (a.done && *a.done) return;
+    if (t < n) bwd_tiny_item(a, t0 + t);
+}
+
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
     constexpr int kWarps = kSmallThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
@@ -472,6 +532,164 @@ void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& 
         if (nw > 0) launch_pdl(k_chol_bwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, 0, s, a, v.bwdw_begin, nw);
         if (nt > 0) launch_pdl(k_chol_bwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s, a, v.tiny_begin, nt);
     }
+}
+
+// ---- the whole solve in one persistent launch over the GPU.
+// All CTAs are resident (cooperative launch), 128 threads each.  Per
+// forward level the CTAs stride over the level's units -- one block item,
+// four warp items or 128 tiny supernodes per unit -- and meet at a
+// grid-wide barrier; per backward level the z staging (when the level has
+// block items) and the backward items are separated by barriers as well.
+// The barrier spins for a bounded time: past the limit it sets a sticky
+// timeout word and every CTA returns at its next barrier (the step's result
+// is then invalid and the engine reports PDGB_ERR_TIMEOUT).
+__device__ __forceinline__ bool grid_sync(GridSync* g, unsigned& gen, unsigned expect, long long spin_limit) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned target = gen + 1;
+        bool good = true;
+        __threadfence();  // this CTA's writes before the arrival (cumulative over the CTA barrier)
+        const unsigned prev = atomicAdd(&g->arrive, 1u);
+        if (prev == expect - 1) {
+            atomicExch(&g->arrive, 0u);
+            __threadfence();
+            atomicExch(&g->gen, target);
+        } else {
+            long long n = 0;
+            for (;;) {
+                if (*reinterpret_cast<volatile unsigned*>(&g->gen) == target) break;
+                if (*reinterpret_cast<volatile int*>(&g->timeout)) {
+                    good = false;
+                    break;
+                }
+                if (++n > spin_limit) {
+                    atomicExch(&g->timeout, 1);
+                    good = false;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();  // the other CTAs' writes before any read after the barrier
+        gen = target;
+        ok = good && !*reinterpret_cast<volatile int*>(&g->timeout);
+    }
+    __syncthreads();
+    return ok;
+}
+
+__global__ void __launch_bounds__(kBlockThreads) k_chol_solve_persistent(CholArgs a, const SolveLevel* __restrict__ lv,
+                                                                         int nl, GridSync* bar, long long spin) {
+    __shared__ float4 rs[kFwdBlockCols];
+    __shared__ float4 stage[kBlockThreads / 32][32];
+    if (a.done && *a.done) return;  // set before this launch: the same for every CTA
+    constexpr int kWarps = kBlockThreads / 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned expect = gridDim.x;
+    unsigned gen = 0;
+    for (int L = 0; L < nl; ++L) {
+        const SolveLevel v = lv[L];
+        const int nb = v.fwdb_end - v.fwdb_begin, nw = v.fwdw_end - v.fwdw_begin, nt = v.tiny_end - v.tiny_begin;
+        const int nwu = (nw + kWarps - 1) / kWarps, ntu = (nt + kBlockThreads - 1) / kBlockThreads;
+        for (int u = blockIdx.x; u < nb + nwu + ntu; u += gridDim.x) {
+            if (u < nb) {
+                __syncthreads();  // rs of the previous block item is read
+                FwdBlockPre p;
+                fwd_block_load(a, v.fwdb_begin + u, p);
+                fwd_block_run(a, p, rs);
+            } else if (u < nb + nwu) {
+                const int it = (u - nb) * kWarps + warp;
+                if (it < nw) fwd_warp_item(a, a.fwd_small + (size_t)kItemInts * (v.fwdw_begin + it), stage[warp], lane);
+            } else {
+                const int t = (u - nb - nwu) * kBlockThreads + threadIdx.x;
+                if (t < nt) fwd_tiny_item(a, v.tiny_begin + t);
+            }
+        }
+        if (!grid_sync(bar, gen, expect, spin)) return;
+    }
+    for (int L = nl - 1; L >= 0; --L) {
+        const SolveLevel v = lv[L];
+        const int nz = v.zst_end - v.zst_begin;
+        if (nz > 0) {
+            for (int u = blockIdx.x; u < nz; u += gridDim.x) zstage_item(a, v.zst_begin + u, false);
+            if (!grid_sync(bar, gen, expect, spin)) return;
+        }
+        const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin, nt = v.tiny_end - v.tiny_begin;
+        const int nwu = (nw + kWarps - 1) / kWarps, ntu = (nt + kBlockThreads - 1) / kBlockThreads;
+        for (int u = blockIdx.x; u < nb + nwu + ntu; u += gridDim.x) {
+            if (u < nb) {
+                BwdBlockPre p;
+                bwd_block_load(a, v.bwdb_begin + u, p);
+                bwd_block_run(a, p);
+            } else if (u < nb + nwu) {
+                const int it = (u - nb) * kWarps + warp;
+                if (it < nw) bwd_warp_item(a, a.bwd_small + (size_t)kItemInts * (v.bwdw_begin + it), stage[warp], lane);
+            } else {
+                const int t = (u - nb - nwu) * kBlockThreads + threadIdx.x;
+                if (t < nt) bwd_tiny_item(a, v.tiny_begin + t);
+            }
+        }
+        if (L > 0 && !grid_sync(bar, gen, expect, spin)) return;
+    }
+}
+
+// CTAs of the persistent solve: the resident CTAs per SM (at most
+// PDGB_PERSIST_CTAS_PER_SM, default 8) times the SMs.
+int persistent_grid() {
+    static int grid[64] = {0};
+    int dev = 0;
+    PDGB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw Error{PDGB_ERR_CUDA, "device index out of range"};
+    if (!grid[dev]) {
+        int sms = 0, per = 0;
+        PDGB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        PDGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_chol_solve_persistent, kBlockThreads, 0));
+        int cap = 8;
+        if (const char* e = std::getenv("PDGB_PERSIST_CTAS_PER_SM")) cap = std::max(1, std::atoi(e));
+        grid[dev] = sms * std::max(1, std::min(per, cap));
+    }
+    return grid[dev];
+}
+
+void launch_chol_solve_persistent(const CholArgs& a, const SolveLevel* levels, int nl, GridSync* bar,
+                                  long long spin_limit, cudaStream_t s) {
+    if (nl <= 0) return;
+    PDGB_CUDA_TRY(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));  // arrival count and generation
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(persistent_grid());
+    cfg.blockDim = dim3(kBlockThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PDGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_chol_solve_persistent, a, levels, nl, bar, spin_limit));
+}
+
+// Check of the grid barrier on its own: `rounds` barriers of a cooperative
+// launch of `ctas` CTAs that wait for `missing` more arrivals than there are
+// CTAs (0: the barrier completes; > 0: it can only time out).
+__global__ void k_grid_sync_check(GridSync* bar, int rounds, int missing, long long spin) {
+    unsigned gen = 0;
+    for (int r = 0; r < rounds; ++r)
+        if (!grid_sync(bar, gen, gridDim.x + (unsigned)missing, spin)) return;
+}
+
+void launch_grid_sync_check(GridSync* bar, int ctas, int rounds, int missing, long long spin_limit, cudaStream_t s) {
+    PDGB_CUDA_TRY(cudaMemsetAsync(bar, 0, sizeof(GridSync), s));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(kBlockThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    PDGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_grid_sync_check, bar, rounds, missing, spin_limit));
 }
 
 // ---- one body per CTA: warps stride over the items of a level,

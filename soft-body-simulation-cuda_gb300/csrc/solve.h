@@ -40,6 +40,16 @@ constexpr int kBlockThreads = 128;      // block-item kernels: 4 warps
 constexpr int kSmallThreads = 256;      // small-supernode kernels: one warp item per warp
 constexpr int kStageThreads = 128;      // backward z staging: one CTA per 128-row chunk (kStageRows)
 
+// Grid-wide barrier of the persistent solve (device memory): arrivals and
+// generation are cleared before each launch; timeout is set when a wait
+// ran out of its spin limit and stays set until the state is set again.
+struct GridSync {
+    unsigned arrive;
+    unsigned gen;
+    int timeout;
+    int pad;
+};
+
 // Convergence state of one step of the Cholesky path (device memory).
 struct StepState {
     int done;            // set once sqrt(err) < tol: later iterations are skipped
@@ -47,6 +57,8 @@ struct StepState {
     unsigned count;      // blocks that added their partial error sum
     float err_acc;       // sum of squared changes (float, as the reference)
     int nonfinite;       // a step ended with a non-finite position or velocity (sticky)
+    int pad;
+    GridSync bar;        // barrier of the persistent solve
 };
 
 struct CholVertexArgs {
@@ -69,6 +81,16 @@ struct CholVertexArgs {
 
 // One launch per level and direction (large systems).
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s);
+// The whole solve in one persistent cooperative launch over the GPU (all
+// bodies of a batch), levels separated by a bounded grid barrier; levels is
+// the device copy of the per-level item ranges.
+void launch_chol_solve_persistent(const CholArgs& a, const SolveLevel* levels, int nl, GridSync* bar,
+                                  long long spin_limit, cudaStream_t s);
+// The grid barrier on its own (check entry point).
+void launch_grid_sync_check(GridSync* bar, int ctas, int rounds, int missing, long long spin_limit, cudaStream_t s);
+int persistent_grid();
+// Spin iterations (about 100 ns each) before a barrier wait gives up.
+constexpr long long kPersistSpinLimit = 1ll << 24;
 // The whole solve of one body in one CTA, levels separated by
 // __syncthreads; one CTA per body (small systems and batches of bodies).
 void launch_chol_solve_cta(const CholArgs& a, int nbodies, cudaStream_t s);

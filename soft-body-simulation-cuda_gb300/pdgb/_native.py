@@ -37,6 +37,7 @@ PDGB_SOLVE_CTA = 1
 PDGB_SOLVE_CLUSTER = 2
 PDGB_SOLVE_LEVELS = 3
 PDGB_SOLVE_DSM = 4
+PDGB_SOLVE_PERSISTENT = 5
 PDGB_FACTOR_GPU = 0
 PDGB_FACTOR_HOST = 1
 PDGB_TIMING_OFF = 0
@@ -137,6 +138,8 @@ class pdgb_server_stats(C.Structure):
         ("factors", C.c_longlong),
         ("factor_cache_hits", C.c_longlong),
         ("factor_ms", C.c_double),
+        ("finishing", C.c_int),
+        ("reserved", C.c_int),
     ]
 
 
@@ -245,6 +248,7 @@ SIGNATURES = {
     "pdgb_last_step_iterations": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "pdgb_synchronize": (C.c_int, [C.c_void_p]),
     "pdgb_last_step_status": (C.c_int, [C.c_void_p]),
+    "pdgb_grid_sync_check": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_longlong]),
     "pdgb_enable_kernel_timing": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_read_timing": (C.c_int, [C.c_void_p, C.POINTER(pdgb_timing)]),
     "pdgb_local_step_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),

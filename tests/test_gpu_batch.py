@@ -78,3 +78,46 @@ def test_batch_solve_schedules():
         lo = sum(x.num_verts for x in bodies[:b])
         for mode in (N.PDGB_SOLVE_CLUSTER, N.PDGB_SOLVE_LEVELS):
             assert rel_l2(out[mode][lo:lo + body.num_verts], Xo) < TOL
+
+
+@pytest.mark.parametrize("case", ["batch", "c1", "hetero14"])
+def test_persistent_solve_matches_per_level_launches(case):
+    """The whole Cholesky solve in one persistent cooperative launch (levels
+    separated by a bounded grid barrier) gives the per-level launches'
+    result, and the FP64 oracle's, on a batch and on single bodies."""
+    from pdgb import _native as N
+
+    if case == "batch":
+        bodies = mesh.batch_c4(nbodies=9, seed=11, lo=2, hi=9)
+    elif case == "c1":
+        bodies = mesh.make_grid_body(10, 10, 10, young=1e5, poisson=0.4)
+    else:
+        bodies = mesh.cube_c3(n=14, seed=5)
+    params = SolverParams(num_iterations=10, solver=1)
+    out = {}
+    for mode in (N.PDGB_SOLVE_LEVELS, N.PDGB_SOLVE_PERSISTENT):
+        with PdSolver(bodies, params) as e:
+            e.set_solve_mode(mode)
+            e.update(4)
+            assert e.solve_mode() == mode
+            assert e.step_status() == N.PDGB_OK
+            out[mode] = e.download_state()[0]
+    assert rel_l2(out[N.PDGB_SOLVE_PERSISTENT], out[N.PDGB_SOLVE_LEVELS]) < 1e-5
+    for b, body in enumerate(bodies if isinstance(bodies, list) else [bodies]):
+        Xo, _, _ = O.simulate(body, params, 4, precision=64)
+        lo = sum(x.num_verts for x in bodies[:b]) if isinstance(bodies, list) else 0
+        assert rel_l2(out[N.PDGB_SOLVE_PERSISTENT][lo:lo + body.num_verts], Xo) < TOL
+
+
+def test_grid_barrier_wait_is_bounded():
+    """The persistent solve's grid barrier on its own: it completes when every
+    CTA arrives; when one arrival can never come (a participant that nothing
+    provides), every wait gives up after its bound, the kernel returns with a
+    timeout status and the context stays usable."""
+    from pdgb import _native as N
+
+    lib = N.lib()
+    assert lib.pdgb_grid_sync_check(0, 20, 0, 1 << 24) == N.PDGB_OK
+    assert lib.pdgb_grid_sync_check(64, 3, 1, 20000) == N.PDGB_ERR_TIMEOUT
+    assert lib.pdgb_grid_sync_check(64, 3, 0, 1 << 24) == N.PDGB_OK
+    assert lib.pdgb_grid_sync_check(0, 5, 0, 1 << 24) == N.PDGB_OK
