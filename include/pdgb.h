@@ -305,10 +305,15 @@ typedef struct pdgb_layout_info {
 int pdgb_inspect_layout(const pdgb_mesh_desc* mesh, pdgb_layout_info* info, int* vperm, int* tperm);
 
 /* Ordering of the Cholesky factor (default AMD, as the reference's
- * cusolverSpXcsrsymamdHost, cholesky.cu:88-91).  Takes effect at the next
- * prepare. */
+ * cusolverSpXcsrsymamdHost, cholesky.cu:88-91).  PDGB_ORDER_DENSE keeps
+ * the AMD order but stores the factor as one dense supernode (all n pivots,
+ * n^2 FP32 entries of L^-1): the solve is then a few wide dense launches
+ * instead of one launch per tree level, which pays off for small single
+ * bodies (the autotuner tries it up to 4096 vertices).  Takes effect at the
+ * next prepare. */
 #define PDGB_ORDER_AMD 0
 #define PDGB_ORDER_ND 1 /* geometric nested dissection */
+#define PDGB_ORDER_DENSE 2
 int pdgb_set_ordering(pdgb_engine* e, int ordering);
 
 /* Rotation of the local step.  QUAT (default): the closest proper rotation
@@ -368,7 +373,7 @@ typedef struct pdgb_tune_report {
     int tile_tets;       /* chosen most tets per tile                        */
     int solve_mode;      /* chosen PDGB_SOLVE_* (AUTO on the Jacobi path)    */
     int candidates;      /* configurations timed                             */
-    int reserved;
+    int ordering;        /* chosen PDGB_ORDER_* (Cholesky path)              */
     double best_ms;      /* device time per step, chosen configuration       */
     double default_ms;   /* device time per step before tuning               */
 } pdgb_tune_report;

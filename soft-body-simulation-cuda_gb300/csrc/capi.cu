@@ -122,6 +122,10 @@ struct pdgb_engine {
 
 namespace {
 
+// Single bodies up to this many vertices: the autotuner also tries the
+// factor as one dense supernode.
+constexpr int kDenseTuneMaxVerts = 4096;
+
 // Factors up to this many stored entries use the single-CTA solve.
 constexpr size_t kCtaSolveMaxEntries = 1u << 15;
 
@@ -768,7 +772,7 @@ int pdgb_set_params(pdgb_engine* e, const pdgb_params* params) {
 }
 
 int pdgb_set_ordering(pdgb_engine* e, int ordering) {
-    if (!e || (ordering != PDGB_ORDER_AMD && ordering != PDGB_ORDER_ND)) {
+    if (!e || (ordering != PDGB_ORDER_AMD && ordering != PDGB_ORDER_ND && ordering != PDGB_ORDER_DENSE)) {
         set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or ordering");
         return PDGB_ERR_INVALID_ARGUMENT;
     }
@@ -909,26 +913,41 @@ int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
         if (e->prm.solver == PDGB_SOLVER_CHOLESKY) {
             modes = {PDGB_SOLVE_CTA, PDGB_SOLVE_CLUSTER, PDGB_SOLVE_LEVELS, PDGB_SOLVE_PERSISTENT};
         }
+        // orderings: the current one, and for a small single body on the
+        // Cholesky path the one dense supernode (a few wide solve launches)
+        std::vector<int> ords = {e->ordering};
+        if (e->prm.solver == PDGB_SOLVER_CHOLESKY && e->nbodies == 1 && e->nv <= kDenseTuneMaxVerts &&
+            e->ordering != PDGB_ORDER_DENSE)
+            ords.push_back(PDGB_ORDER_DENSE);
+        const int ord0 = e->ordering;
         double best = t0;
-        int best_cap = cap0, best_mode = req0, tried = 1;
-        for (int cap : caps)
-            for (int mode : modes) {
-                set_tile_cap(e, cap);
-                if (mode != e->solve_req) {
-                    e->solve_req = mode;
-                    e->prepared = false;
-                }
-                const double t = time_steps(e, steps);
-                copy_state(true);
-                ++tried;
-                if (t < best) {
-                    best = t;
-                    best_cap = cap;
-                    best_mode = mode;
-                }
+        int best_cap = cap0, best_mode = req0, best_ord = ord0, tried = 1;
+        for (int ord : ords) {
+            if (ord != e->ordering) {
+                e->ordering = ord;
+                e->prepared = false;
             }
+            for (int cap : caps)
+                for (int mode : modes) {
+                    set_tile_cap(e, cap);
+                    if (mode != e->solve_req) {
+                        e->solve_req = mode;
+                        e->prepared = false;
+                    }
+                    const double t = time_steps(e, steps);
+                    copy_state(true);
+                    ++tried;
+                    if (t < best) {
+                        best = t;
+                        best_cap = cap;
+                        best_mode = mode;
+                        best_ord = ord;
+                    }
+                }
+        }
         set_tile_cap(e, best_cap);
         e->solve_req = best_mode;
+        e->ordering = best_ord;
         e->prepared = false;
         prepare(e);
         copy_state(true);
@@ -936,7 +955,7 @@ int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
             rep->tile_tets = best_cap;
             rep->solve_mode = e->prm.solver == PDGB_SOLVER_CHOLESKY ? e->solve_mode : PDGB_SOLVE_AUTO;
             rep->candidates = tried;
-            rep->reserved = 0;
+            rep->ordering = e->ordering;
             rep->best_ms = best;
             rep->default_ms = t0;
         }

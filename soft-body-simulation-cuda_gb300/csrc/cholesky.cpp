@@ -514,6 +514,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
             if (s == 0 || !merged[s - 1]) sf.push_back(sfirst[s]);
         sfirst.swap(sf);
     }
+    if (ordering == 2) sfirst.assign(1, 0);  // one dense supernode: every pivot, every row
     const int ns = (int)sfirst.size();
     sfirst.push_back(n);
     std::vector<int> col2s(n);

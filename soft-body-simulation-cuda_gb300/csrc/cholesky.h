@@ -198,7 +198,7 @@ struct DsmPlan {
 void build_dsm_plan(const CholFactor& f, int ctas, int warps_per_cta, size_t max_smem, DsmPlan& plan);
 
 // Factors K (vertex-indexed, n x n SPD).  ordering: 0 = AMD, 1 = nested
-// dissection (xyz required).  Throws Error(PDGB_ERR_NOT_SPD) if a pivot is
+// dissection (xyz required), 2 = AMD order stored as one dense supernode.  Throws Error(PDGB_ERR_NOT_SPD) if a pivot is
 // not positive.  bwd_chunk_rows: rows per backward block item (0: whole
 // columns).
 // gpu_numeric: stop after the symbolic analysis and fill out.fp for the

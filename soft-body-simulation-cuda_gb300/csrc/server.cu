@@ -204,6 +204,7 @@ struct Request {
     int* vperm = nullptr;
     int* flag = nullptr;                  // non-finite state (device)
     int flag_host = 0;
+    int64_t hin = -1, hout = -1;          // page-locked staging ranges (input state, results)
     // arena ranges of a Cholesky request
     int64_t v0 = 0, m0 = 0, r0 = 0, z0 = 0, io = 0;
     float4 *x = nullptr, *v = nullptr, *prev = nullptr, *base = nullptr;
@@ -335,6 +336,12 @@ struct pdgb_server {
     Arena<int> ar_items;               // every request's work items, its offsets applied
     DBuf<int> d_comb[kItemKinds];       // the step's combined per-level lists, by kind
     Pinned<ItemSeg> h_seg;              // segments gathered into them
+    // page-locked staging of the requests' states: inputs at admission,
+    // results at retirement (copies to and from pageable memory would make
+    // the host wait for the step in flight)
+    Pinned<float> hst;
+    RangeAlloc hst_ra;
+    std::vector<std::pair<int64_t, int64_t>> hst_free_after_wait;
     DBuf<ItemSeg> d_seg;
     std::vector<SolveLevel> step_levels;
     // pipelining: the step launched by the last tick and the requests it finishes
@@ -523,6 +530,26 @@ template <class T> void put(cudaStream_t s, T* dst, const std::vector<T>& src) {
     if (!src.empty()) PDGB_CUDA_TRY(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
 }
 
+// A range of the page-locked staging buffer (floats).  Growing it waits for
+// the stream (no copy may be reading or writing the old buffer) and keeps
+// its contents.
+float* host_stage(pdgb_server* S, int64_t n, int64_t& off) {
+    off = S->hst_ra.take(std::max<int64_t>(n, 1));
+    if ((size_t)S->hst_ra.top > S->hst.n || !S->hst.p) {
+        PDGB_CUDA_TRY(cudaStreamSynchronize(S->stream));
+        const size_t ncap = std::max<size_t>((size_t)S->hst_ra.top, 2 * S->hst.n + (1u << 20));
+        float* q = nullptr;
+        PDGB_CUDA_TRY(cudaMallocHost(reinterpret_cast<void**>(&q), ncap * sizeof(float)));
+        if (S->hst.p) {
+            std::memcpy(q, S->hst.p, S->hst.n * sizeof(float));
+            cudaFreeHost(S->hst.p);
+        }
+        S->hst.p = q;
+        S->hst.n = ncap;
+    }
+    return S->hst.p + off;
+}
+
 SceneArgs request_scene(const pdgb_server* S, Request* r) {
     SceneArgs sc{};
     sc.dt2 = S->cfg.params.dt * S->cfg.params.dt;
@@ -657,11 +684,15 @@ void admit(pdgb_server* S, Request* r) {
     r->flag = carve<int>(p, 1);
     PDGB_CUDA_TRY(cudaMemsetAsync(r->flag, 0, sizeof(int), s));
     PDGB_CUDA_TRY(cudaMemsetAsync(r->prev, 0, (size_t)nv * sizeof(float4), s));
-    PDGB_CUDA_TRY(cudaMemcpyAsync(r->staging, r->X.data(), 3 * (size_t)nv * sizeof(float), cudaMemcpyHostToDevice, s));
     const bool hasV = !r->V.empty();
-    if (hasV)
-        PDGB_CUDA_TRY(cudaMemcpyAsync(r->staging + 3 * (size_t)nv, r->V.data(), 3 * (size_t)nv * sizeof(float),
-                                      cudaMemcpyHostToDevice, s));
+    {
+        const int64_t n = (hasV ? 6 : 3) * (int64_t)nv;
+        float* h = host_stage(S, n, r->hin);
+        std::memcpy(h, r->X.data(), 3 * (size_t)nv * sizeof(float));
+        if (hasV) std::memcpy(h + 3 * (size_t)nv, r->V.data(), 3 * (size_t)nv * sizeof(float));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(r->staging, h, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, s));
+        S->hst_free_after_wait.emplace_back(r->hin, n);  // read by the copy: free once the stream is waited for
+    }
     launch_gather_state(nv, r->vperm, r->staging, hasV ? r->staging + 3 * (size_t)nv : nullptr, r->x, r->v, s);
     PDGB_CUDA_TRY(cudaGetLastError());
     r->la = LocalArgs{sn, b, inc_ent, inc_end, geo, ttp, tvp, tv, L.nt_pad, nullptr};
@@ -1018,14 +1049,10 @@ void retire_finished(pdgb_server* S) {
             continue;
         }
         const size_t n3 = 3 * (size_t)r->nv;
-        r->X_out.resize(n3);
-        r->V_out.resize(n3);
         launch_scatter_state(r->nv, r->vperm, r->x, r->v, r->staging, r->staging + n3, S->stream);
-        PDGB_CUDA_TRY(
-            cudaMemcpyAsync(r->X_out.data(), r->staging, n3 * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
-        PDGB_CUDA_TRY(
-            cudaMemcpyAsync(r->V_out.data(), r->staging + n3, n3 * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
-        PDGB_CUDA_TRY(cudaMemcpyAsync(&r->flag_host, r->flag, sizeof(int), cudaMemcpyDeviceToHost, S->stream));
+        float* h = host_stage(S, 2 * (int64_t)n3 + 1, r->hout);
+        PDGB_CUDA_TRY(cudaMemcpyAsync(h, r->staging, 2 * n3 * sizeof(float), cudaMemcpyDeviceToHost, S->stream));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(h + 2 * n3, r->flag, sizeof(int), cudaMemcpyDeviceToHost, S->stream));
         PDGB_CUDA_TRY(cudaFreeAsync(r->block, S->stream));
         r->block = nullptr;
         release_arenas(S, r);  // reused only by uploads ordered after this step
@@ -1039,7 +1066,15 @@ void retire_finished(pdgb_server* S) {
 // After the wait for the step: the retired requests' results are on the host.
 int hand_out(pdgb_server* S, Clock::time_point now) {
     int n = 0;
+    for (auto& fr : S->hst_free_after_wait) S->hst_ra.give(fr.first, fr.second);
+    S->hst_free_after_wait.clear();
     for (Request* r : S->retiring) {
+        const size_t n3 = 3 * (size_t)r->nv;
+        const float* h = S->hst.p + r->hout;
+        r->X_out.assign(h, h + n3);
+        r->V_out.assign(h + n3, h + 2 * n3);
+        std::memcpy(&r->flag_host, h + 2 * n3, sizeof(int));
+        S->hst_ra.give(r->hout, 2 * (int64_t)n3 + 1);
         r->t_done = now;
         S->latencies_ms.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
         if (r->flag_host) {
@@ -1166,9 +1201,10 @@ int pdgb_server_tick(pdgb_server* S, int* active, int* completed) {
             S->inflight = false;
         }
         S->rebuilt = false;
-        // 2. admission (requests that became ready while nothing was in flight)
+        // 2. admission when the server is idle (otherwise requests are
+        //    admitted while the step runs, step 4)
         const auto t1 = Clock::now();
-        admit_ready(S);
+        if (S->active.empty()) admit_ready(S);
         double admit = std::chrono::duration<double, std::milli>(Clock::now() - t1).count();
         if (!S->active.empty()) {
             S->ticks++;

@@ -32,6 +32,7 @@ PDGB_ROTATION_QUAT = 0
 PDGB_ROTATION_SVD = 1
 PDGB_ORDER_AMD = 0
 PDGB_ORDER_ND = 1
+PDGB_ORDER_DENSE = 2
 PDGB_SOLVE_AUTO = 0
 PDGB_SOLVE_CTA = 1
 PDGB_SOLVE_CLUSTER = 2
@@ -214,7 +215,7 @@ class pdgb_tune_report(C.Structure):
         ("tile_tets", C.c_int),
         ("solve_mode", C.c_int),
         ("candidates", C.c_int),
-        ("reserved", C.c_int),
+        ("ordering", C.c_int),
         ("best_ms", C.c_double),
         ("default_ms", C.c_double),
     ]

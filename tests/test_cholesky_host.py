@@ -30,7 +30,7 @@ def factor_check(body, ordering=0, b=None, dt=1 / 120, pw=1e6):
     return st, info, x
 
 
-@pytest.mark.parametrize("ordering", [N.PDGB_ORDER_AMD, N.PDGB_ORDER_ND])
+@pytest.mark.parametrize("ordering", [N.PDGB_ORDER_AMD, N.PDGB_ORDER_ND, N.PDGB_ORDER_DENSE])
 @pytest.mark.parametrize("case", ["tet", "grid3", "c1", "grid_aniso"])
 def test_factor_solves_like_the_oracle(case, ordering):
     body = {"tet": lambda: mesh.single_tet(),

@@ -214,3 +214,28 @@ def test_gpu_factor_reports_not_positive_definite():
         with pytest.raises(PdgbError) as err:
             e.update(1)
         assert err.value.status == N.PDGB_ERR_NOT_SPD
+
+
+@pytest.mark.parametrize("name", ["c1_chol", "grid3_chol_tol", "grid3_chol"])
+def test_dense_supernode_ordering_matches_fixture(name):
+    """The factor stored as one dense supernode (PDGB_ORDER_DENSE, for small
+    single bodies) gives the same steps: the reference's own kernels'
+    fixtures, the FP64 oracle and the early-exit iteration counts."""
+    body, params, steps, Xg, Vg, itg = load_golden(name)
+    with PdSolver(body, params) as e:
+        e.set_ordering(N.PDGB_ORDER_DENSE)
+        its = []
+        for _ in range(steps):
+            e.update(1)
+            its.append(e.last_step_iterations())
+        X, _ = e.download_state()
+        info = e.factor_info()
+    assert info["num_supernodes"] == 1 and info["num_levels"] == 1
+    assert info["m_entries"] == body.num_verts * body.num_verts
+    assert np.isfinite(X).all()
+    assert rel_l2(X, Xg) < TOL
+    if params.tol > 0:
+        d = np.abs(np.asarray(its) - itg)
+        assert d.max() <= 1 and (d > 0).sum() <= max(1, steps // 10), (its, list(itg))
+    Xo, _, _ = O.simulate(body, params, steps, precision=64)
+    assert rel_l2(X, Xo) < TOL
