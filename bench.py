@@ -578,6 +578,9 @@ def main():
                     "(cuSOLVER Cholesky / Jacobi) timed beside the engine")
     ap.add_argument("--collision", action="store_true", help="run continuous collision between bodies after every "
                     "step (inside the timed region)")
+    ap.add_argument("--ordering", default="", choices=["", "amd", "nd", "dense"],
+                    help="Cholesky factor ordering (default: AMD, or the autotuner's choice)")
+    ap.add_argument("--tile", type=int, default=0, help="most tets per local-step tile (0: default / autotuned)")
     ap.add_argument("--no-legs", action="store_true", help="default run: report the 64^3 Jacobi workload only, "
                     "without the legs of the other workloads")
     ap.add_argument("--solver", default="", choices=["", "jacobi", "cholesky"],
@@ -675,8 +678,12 @@ def run_engine(args, workload_name: str, nsteps: int, nwarmup: int, leg: bool = 
     from pdgb import _native as N
 
     eng = PdSolver(body if bodies is None else bodies, params)
-    if args.solve_mode:
+    if args.solve_mode and not leg:
         eng.set_solve_mode(args.solve_mode)
+    if args.ordering and not leg:
+        eng.set_ordering({"amd": N.PDGB_ORDER_AMD, "nd": N.PDGB_ORDER_ND, "dense": N.PDGB_ORDER_DENSE}[args.ordering])
+    if args.tile and not leg:
+        eng.set_tile_size(args.tile)
     stream = torch.cuda.ExternalStream(eng._lib.pdgb_stream(eng.handle))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
