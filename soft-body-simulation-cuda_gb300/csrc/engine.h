@@ -85,7 +85,7 @@ struct HostLayout {
     // tiles
     std::vector<int> tile_tet_ptr;   // [ntiles+1]
     std::vector<int> tile_vptr;      // [ntiles+1]
-    std::vector<uint32_t> tile_verts;  // internal vertex ids of each patch (sorted) | kPinnedBit
+    std::vector<uint32_t> tile_verts;  // internal vertex ids of each patch (longest run first) | kPinnedBit
     // Slots of a tile: one per tet corner, ordered by patch vertex (then tet,
     // then corner), so patch vertex k owns the slots inc_end[k-1] ..
     // inc_end[k] (inc_end[-1] = 0).  inc_ent[4 t + c] = k | r << kPatchBits

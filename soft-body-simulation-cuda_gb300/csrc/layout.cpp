@@ -70,8 +70,13 @@ std::vector<float> chebyshev_omegas(int n, float rho) {
 
 // Tiles: greedy runs of the Morton-ordered tets, cut at max_tile_tets tets
 // (at most kTileTets), when the patch would exceed kMaxPatch vertices, or
-// at a body boundary.  Each tile gets its sorted vertex patch (pinned bit
-// from the caller-order pin flags) and its incidence lists.
+// at a body boundary.  Each tile gets its vertex patch (pinned bit from the
+// caller-order pin flags) and its incidence lists.  The patch is ordered by
+// run length (the vertex's corners in the tile), longest first, then by
+// vertex id: the local step sums one patch vertex's run per thread, and a warp
+// loops as long as its longest run, so neighbouring threads should have runs
+// of nearly the same length (in id order a warp mixes interior vertices, ~20
+// corners, with patch-boundary vertices of 1 to 5).
 void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
     const int nv = L.nv, nt = L.nt, nbodies = L.nbodies;
     const int cap = max_tile_tets > 0 ? std::min(max_tile_tets, kTileTets) : kTileTets;
@@ -89,7 +94,8 @@ void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
     int tile = 0, start = 0;
     int body_cursor = 0, next_body_start = nbodies > 1 ? L.body_itstart[1] : nt;
     auto close_tile = [&](int end) {
-        std::sort(patch.begin(), patch.end());
+        std::sort(patch.begin(), patch.end(),
+                  [&](int a, int b) { return vcount[a] != vcount[b] ? vcount[a] > vcount[b] : a < b; });
         const int np = (int)patch.size();
         for (int k = 0; k < np; ++k) loc[patch[k]] = k;
         // incidence lists in patch order

@@ -168,11 +168,16 @@ __device__ __forceinline__ void closest_rotation(const float F[9], float R[9]) {
 // eigenvector of N's largest eigenvalue.  It is found as the dominant
 // eigenvector of A = N + c I (c = 0.6 |F|_F > |sigma_3| keeps the top
 // eigenvalue dominant even for inverted F) by repeated squaring: P = A^4
-// after 2 squarings, then, while P is not rank one to float precision
-// (trace(P^2) = |P|_F^2 < (1 - 4e-7) trace(P)^2), up to kTail normalised
-// squarings.  Mildly deformed elements (the common case) stop at A^4.  The
-// column of P with the largest diagonal entry, multiplied once more by P
-// (which squares the remaining error), is q.
+// after 2 squarings, then, while P is not close to rank one, up to kTail
+// normalised squarings.  For eigenvalues 1 >= r_2, r_3, r_4 of the scaled P,
+// trace(P^2) / trace(P)^2 = 1 - 2 sum r_i + O(r^2); P counts as rank one when
+// that ratio is at least 1 - 5e-4 (sum r_i <~ 2.5e-4).  The column of P with
+// the largest diagonal entry, multiplied once more by P (which squares the
+// remaining error, to ~1e-7), is q.  Elements within a few percent of a
+// rotation stop at A^4.  A test at float resolution (1 - 4e-7) gave the same
+// rotations to ~6e-7 but, being decided by the rounding of trace(P^2), sent
+// ~7 % of the elements at 1 % strain into an extra squaring -- and a warp
+// pays for one when any of its lanes does.
 __device__ __forceinline__ void sym4_square(float a[10]) {
     // a = {ww, xx, yy, zz, wx, wy, wz, xy, xz, yz}
     const float ww = a[0], xx = a[1], yy = a[2], zz = a[3], wx = a[4], wy = a[5], wz = a[6], xy = a[7], xz = a[8],
@@ -219,7 +224,7 @@ __device__ __forceinline__ void closest_rotation_horn(const float F[9], float R[
     sym4_square(a);
     sym4_square(a);
     float t = a[0] + a[1] + a[2] + a[3];
-    for (int k = 0; k < kTail && sym4_frob2(a) < (1.0f - 4e-7f) * t * t; ++k) {
+    for (int k = 0; k < kTail && sym4_frob2(a) < (1.0f - 5e-4f) * t * t; ++k) {
         const float it = __fdividef(1.0f, t);
 #pragma unroll
         for (int i = 0; i < 10; ++i) a[i] *= it;
