@@ -252,6 +252,16 @@ int pdgb_last_step_status(pdgb_engine* e);
  * stays usable.  Waits for the GPU. */
 int pdgb_grid_sync_check(int ctas, int rounds, int missing, long long spin_limit);
 
+/* Check of the pipelined local step's bounded bulk-copy wait on its own (no
+ * counterpart in the reference): one CTA bulk-copies 256 bytes into shared
+ * memory on an mbarrier that expects 256 + extra_bytes (a multiple of 16).
+ * With extra_bytes = 0 the copy completes the phase and the wait returns
+ * (PDGB_OK, data checked); with extra_bytes > 0 the phase cannot complete and
+ * the wait gives up after limit_ns nanoseconds, 1e6..2e9 (PDGB_ERR_TIMEOUT) --
+ * the copy itself has landed, the kernel returns, the context stays usable.
+ * Waits for the GPU. */
+int pdgb_bulk_wait_check(int extra_bytes, long long limit_ns);
+
 /* Device timing for benchmarks (mode, default OFF):
  *   PDGB_TIMING_STEPS: pdgb_step brackets every step-graph launch with a
  *     pair of CUDA events on the engine's stream and does not wait;
@@ -324,6 +334,21 @@ int pdgb_set_ordering(pdgb_engine* e, int ordering);
 #define PDGB_ROTATION_QUAT 0
 #define PDGB_ROTATION_SVD 1
 int pdgb_set_rotation(pdgb_engine* e, int rotation);
+
+/* Form of the local step (reference: PdUtil::computeLocal, pdUtil.cu:97-145;
+ * same arithmetic and result in both).  TILE (default): one CTA per tile of
+ * up to 512 tets, four CTAs per SM, the tile's geometry loaded at its start.
+ * PIPELINED: two persistent CTAs per SM walk the tiles; while one tile is
+ * computed, the next tile's geometry, corner records and patch lists are
+ * bulk-copied into shared memory (on the 64^3 cube it measures slower: two
+ * 16-warp CTAs per SM wait at the tile's barriers); pdgb_autotune tries it.
+ * A bulk-copy wait that runs out of its bound (1 s) makes
+ * pdgb_last_step_status return PDGB_ERR_TIMEOUT.  The SVD rotation always
+ * uses TILE.  Takes effect at the next step. */
+#define PDGB_LOCAL_TILE 0
+#define PDGB_LOCAL_PIPELINED 1
+int pdgb_set_local_kernel(pdgb_engine* e, int kind);
+int pdgb_get_local_kernel(pdgb_engine* e, int* kind);
 
 /* Schedule of the Cholesky solve.  CTA: one CTA per body walks the body's
  * whole elimination tree (levels separated by block barriers); CLUSTER: one

@@ -32,6 +32,8 @@ struct pdgb_engine {
     pdgb_params prm{};
     int ordering = PDGB_ORDER_AMD;
     int rotation = PDGB_ROTATION_QUAT;
+    int local_kernel = PDGB_LOCAL_TILE;
+    int pipe_grid = 0;  // resident CTAs of the pipelined local step (0: tile form)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int nv = 0, nt = 0;
@@ -183,6 +185,8 @@ LocalArgs local_args(pdgb_engine* e, const int* done) {
     a.tile_verts = e->tile_verts.p;
     a.nt_pad = e->L.nt_pad;
     a.done = done;
+    a.pipe_grid = e->local_kernel == PDGB_LOCAL_PIPELINED ? e->pipe_grid : 0;
+    a.timeout = &e->st.p->local_timeout;
     return a;
 }
 
@@ -208,7 +212,7 @@ SceneArgs scene_args(pdgb_engine* e) {
 // Clears the sticky step status words (the state was set again): the
 // non-finite flag and the persistent solve's barrier state.
 void clear_nonfinite(pdgb_engine* e) {
-    PDGB_CUDA_TRY(cudaMemsetAsync(&e->st.p->nonfinite, 0, sizeof(int), e->stream));
+    PDGB_CUDA_TRY(cudaMemsetAsync(&e->st.p->nonfinite, 0, 2 * sizeof(int), e->stream));  // + local_timeout
     PDGB_CUDA_TRY(cudaMemsetAsync(&e->st.p->bar, 0, sizeof(GridSync), e->stream));
 }
 
@@ -513,6 +517,9 @@ void prepare(pdgb_engine* e) {
     e->pin_rhs.upload(e->L.pin_rhs, e->stream);
     if (e->prm.solver == PDGB_SOLVER_CHOLESKY) prepare_cholesky(e);
     PDGB_CUDA_TRY(cudaMemsetAsync(e->y.p, 0, (size_t)e->nv * sizeof(float4), e->stream));
+    // resident CTAs of the pipelined local step for the current tile cut
+    // (queried here, not while the step graph is being captured)
+    e->pipe_grid = e->local_kernel == PDGB_LOCAL_PIPELINED ? local_pipe_grid(e->L.ntiles, e->L.max_patch) : 0;
     build_graph(e);
     PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
     e->prepared = true;
@@ -783,6 +790,27 @@ int pdgb_set_ordering(pdgb_engine* e, int ordering) {
     return PDGB_OK;
 }
 
+int pdgb_set_local_kernel(pdgb_engine* e, int kind) {
+    if (!e || (kind != PDGB_LOCAL_TILE && kind != PDGB_LOCAL_PIPELINED)) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or local-step kind");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (kind != e->local_kernel) {
+        e->local_kernel = kind;
+        e->prepared = false;  // the step graph holds the local-step launches
+    }
+    return PDGB_OK;
+}
+
+int pdgb_get_local_kernel(pdgb_engine* e, int* kind) {
+    if (!e || !kind) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or output");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    *kind = e->local_kernel;
+    return PDGB_OK;
+}
+
 int pdgb_set_rotation(pdgb_engine* e, int rotation) {
     if (!e || (rotation != PDGB_ROTATION_QUAT && rotation != PDGB_ROTATION_SVD)) {
         set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad engine or rotation mode");
@@ -945,9 +973,34 @@ int pdgb_autotune(pdgb_engine* e, int steps, pdgb_tune_report* rep) {
                     }
                 }
         }
+        // the pipelined local step at the chosen configuration (and at its
+        // natural 512-tet tiles)
+        const int lk0 = e->local_kernel;
+        int best_lk = lk0;
+        if (e->rotation == PDGB_ROTATION_QUAT) {
+            e->solve_req = best_mode;
+            e->ordering = best_ord;
+            const int other = lk0 == PDGB_LOCAL_TILE ? PDGB_LOCAL_PIPELINED : PDGB_LOCAL_TILE;
+            std::vector<int> lk_caps = {best_cap};
+            if (best_cap != kTileTets) lk_caps.push_back(kTileTets);
+            for (int cap : lk_caps) {
+                set_tile_cap(e, cap);
+                e->local_kernel = other;
+                e->prepared = false;
+                const double t = time_steps(e, steps);
+                copy_state(true);
+                ++tried;
+                if (t < best) {
+                    best = t;
+                    best_cap = cap;
+                    best_lk = other;
+                }
+            }
+        }
         set_tile_cap(e, best_cap);
         e->solve_req = best_mode;
         e->ordering = best_ord;
+        e->local_kernel = best_lk;
         e->prepared = false;
         prepare(e);
         copy_state(true);
@@ -1316,7 +1369,7 @@ int pdgb_get_perf(pdgb_engine* e, pdgb_perf* out) {
     out->iterations = e->iters_run;
     out->factor_nnz = e->prm.solver == PDGB_SOLVER_CHOLESKY ? e->chol.nnz_L : 0;
     out->tiles = e->L.ntiles;
-    out->patch_verts = (long long)e->L.tile_verts.size();
+    out->patch_verts = (long long)e->L.tile_vptr.back();
     return PDGB_OK;
 }
 
@@ -1341,10 +1394,10 @@ int pdgb_synchronize(pdgb_engine* e) {
 
 int pdgb_last_step_status(pdgb_engine* e) {
     if (!e) return PDGB_ERR_INVALID_ARGUMENT;
-    int flag = 0;
+    int flag[2] = {0, 0};  // nonfinite, local_timeout
     GridSync bar{};
     const int st = guarded([&] {
-        PDGB_CUDA_TRY(cudaMemcpyAsync(&flag, &e->st.p->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+        PDGB_CUDA_TRY(cudaMemcpyAsync(flag, &e->st.p->nonfinite, 2 * sizeof(int), cudaMemcpyDeviceToHost, e->stream));
         PDGB_CUDA_TRY(cudaMemcpyAsync(&bar, &e->st.p->bar, sizeof(GridSync), cudaMemcpyDeviceToHost, e->stream));
         PDGB_CUDA_TRY(cudaStreamSynchronize(e->stream));
     });
@@ -1353,7 +1406,11 @@ int pdgb_last_step_status(pdgb_engine* e) {
         set_last_error(PDGB_ERR_TIMEOUT, "a grid-barrier wait of the persistent solve ran out of its bound");
         return PDGB_ERR_TIMEOUT;
     }
-    if (flag) {
+    if (flag[1]) {
+        set_last_error(PDGB_ERR_TIMEOUT, "a bulk-copy wait of the pipelined local step ran out of its bound");
+        return PDGB_ERR_TIMEOUT;
+    }
+    if (flag[0]) {
         set_last_error(PDGB_ERR_NONFINITE, "a step ended with a non-finite position or velocity");
         return PDGB_ERR_NONFINITE;
     }
@@ -1462,7 +1519,7 @@ int pdgb_inspect_layout(const pdgb_mesh_desc* mesh, pdgb_layout_info* info, int*
         HostLayout L;
         build_layout(mesh->num_verts, mesh->num_tets, mesh->X, mesh->tets, mesh->mass, mesh->mu, mesh->dbc, p, L);
         info->num_tiles = L.ntiles;
-        info->patch_verts = (long long)L.tile_verts.size();
+        info->patch_verts = (long long)L.tile_vptr.back();
         info->max_patch = 0;
         info->max_tile_tets = 0;
         info->reserved = 0;
@@ -1614,6 +1671,37 @@ int pdgb_grid_sync_check(int ctas, int rounds, int missing, long long spin_limit
     if (h.timeout) {
         set_last_error(PDGB_ERR_TIMEOUT, "grid barrier wait ran out of its bound");
         return PDGB_ERR_TIMEOUT;
+    }
+    return PDGB_OK;
+}
+
+int pdgb_bulk_wait_check(int extra_bytes, long long limit_ns) {
+    if (extra_bytes < 0 || extra_bytes % 16 || extra_bytes > 4096 || limit_ns < 1000000 || limit_ns > 2000000000ll) {
+        set_last_error(PDGB_ERR_INVALID_ARGUMENT, "bad bulk-wait check arguments");
+        return PDGB_ERR_INVALID_ARGUMENT;
+    }
+    int h[2] = {0, 0};
+    const int st = guarded([&] {
+        std::vector<uint32_t> words(64);
+        for (int k = 0; k < 64; ++k) words[k] = (uint32_t)k;
+        DBuf<uint32_t> src;
+        DBuf<int> out;
+        src.alloc(64);
+        out.alloc(2);
+        PDGB_CUDA_TRY(cudaMemcpy(src.p, words.data(), 64 * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        PDGB_CUDA_TRY(cudaMemset(out.p, 0, 2 * sizeof(int)));
+        launch_bulk_wait_check(src.p, extra_bytes, (unsigned long long)limit_ns, out.p, nullptr);
+        PDGB_CUDA_TRY(cudaGetLastError());
+        PDGB_CUDA_TRY(cudaMemcpy(h, out.p, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+    });
+    if (st != PDGB_OK) return st;
+    if (h[0]) {
+        set_last_error(PDGB_ERR_TIMEOUT, "bulk-copy wait ran out of its bound");
+        return PDGB_ERR_TIMEOUT;
+    }
+    if (!h[1]) {
+        set_last_error(PDGB_ERR_CUDA, "bulk copy completed with wrong data");
+        return PDGB_ERR_CUDA;
     }
     return PDGB_OK;
 }

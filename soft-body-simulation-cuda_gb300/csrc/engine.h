@@ -40,6 +40,7 @@ constexpr int kMaxRun = 1 << (16 - kPatchBits);
 static_assert(kMaxPatch <= (1 << kPatchBits), "patch index field");
 constexpr int kLocalThreads = 256;
 constexpr int kTileTets = 2 * kLocalThreads;
+constexpr int kLayoutTailPad = 8;
 
 // Device buffer with RAII.
 template <class T> struct DBuf {
@@ -85,14 +86,17 @@ struct HostLayout {
     // tiles
     std::vector<int> tile_tet_ptr;   // [ntiles+1]
     std::vector<int> tile_vptr;      // [ntiles+1]
-    std::vector<uint32_t> tile_verts;  // internal vertex ids of each patch (longest run first) | kPinnedBit
+    std::vector<uint32_t> tile_verts;  // internal vertex ids of each patch (longest run first) | kPinnedBit [+ kLayoutTailPad]
     // Slots of a tile: one per tet corner, ordered by patch vertex (then tet,
     // then corner), so patch vertex k owns the slots inc_end[k-1] ..
     // inc_end[k] (inc_end[-1] = 0).  inc_ent[4 t + c] = k | r << kPatchBits
     // for corner c of tet t: its patch vertex k and its rank r in k's run
     // (slot inc_end[k-1] + r).
-    std::vector<uint16_t> inc_ent;   // [4 nt]
-    std::vector<uint16_t> inc_end;   // [sum of patch sizes]
+    // The arrays the pipelined local step bulk-copies are padded so that
+    // 16-byte-rounded copy ranges stay inside them: inc_ent to 4 nt_pad
+    // entries, tile_verts and inc_end by kLayoutTailPad zero entries.
+    std::vector<uint16_t> inc_ent;   // [4 nt_pad]
+    std::vector<uint16_t> inc_end;   // [sum of patch sizes + kLayoutTailPad]
     std::vector<float> geo;          // planes float4 [nt_pad] x2 + float2 [nt_pad]: g DmInv (row major), g = sqrt(V0 w)
     std::vector<uint32_t> tets_int;  // [4*nt] internal vertex ids (Cholesky assembly, checks)
     std::vector<double> dminv_d;     // [9*nt] double DmInv (system assembly)
@@ -139,6 +143,11 @@ struct LocalArgs {
     const uint32_t* tile_verts;
     int nt_pad;
     const int* done;  // step early-exit flag (Cholesky tol rule), may be null
+    // Pipelined local step (k_local_pipe): resident CTAs (0: the one-tile-
+    // per-CTA kernel runs instead) and the word set when one of its bounded
+    // waits for a bulk copy runs out.
+    int pipe_grid;
+    int* timeout;
 };
 
 // Vertex-kernel mode flags.
@@ -222,6 +231,13 @@ void launch_local_multi(const LocalArgs* req, const int2* list, const int* count
 void launch_jacobi_vertex_multi(const VertexArgs* req, const int2* list, const int* count, int grid, int mode,
                                 float omega, cudaStream_t s);
 void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_form, int rotation, cudaStream_t s);
+// Resident CTAs of the pipelined local step for this mesh's largest patch
+// (2 per SM when its shared memory allows), capped at ntiles; 0 when it
+// cannot run (the one-tile-per-CTA kernel is used).
+int local_pipe_grid(int ntiles, int max_patch);
+// Check of the bounded bulk-copy wait (pdgb_bulk_wait_check): src holds 64
+// words 0..63; out[0] = timed out, out[1] = data intact.
+void launch_bulk_wait_check(const void* src, int extra, unsigned long long limit_ns, int* out, cudaStream_t s);
 void launch_jacobi_vertex(const VertexArgs& a, int mode, cudaStream_t s);
 void launch_gather_state(int nv, const int* vperm, const float* X, const float* V, float4* x, float4* v,
                          cudaStream_t s);

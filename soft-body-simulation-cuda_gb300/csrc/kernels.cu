@@ -8,28 +8,104 @@
 //                  computeDBCLocal, addM_h2Sn, updateVelPos; pdUtil.cu:147-226)
 //   k_begin        step prologue: gravity, s_n, M/h^2 s_n (reference:
 //                  pdSolver.cu:154-163, computeSn pdUtil.cu:73-95)
+#include <algorithm>
+#include <mutex>
+
 #include "engine.h"
 #include "pdl.cuh"
 #include "scene.cuh"
 #include "relax.cuh"
 #include "rotation.cuh"
+#include "bulk.cuh"
 
 namespace pdgb {
 
-
 // ------------------------------------------------------------ local step
+// One tet: corner positions from the patch, F' = Ds D', its closest
+// rotation R, and the 4 corner contributions of (g R [- F']) D'^T G written
+// to their slots (run start of the corner's patch vertex + its rank).
+// ga, gb, gc: the tet's geometry planes (D' = g DmInv row major, g);
+// rec: its 4 corner records k | r << kPatchBits.
+template <bool kJacobiForm, int kRotation>
+__device__ __forceinline__ void tet_contrib(const float4 ga, const float4 gb, const float2 gc, const uint2 rec,
+                                            const float4* __restrict__ pos, float4* __restrict__ slot) {
+    constexpr uint32_t kPatchMask = (1u << kPatchBits) - 1u;
+    // D' = g DmInv (row major) and g = sqrt(V0 w)
+    const float D[9] = {ga.x, ga.y, ga.z, ga.w, gb.x, gb.y, gb.z, gb.w, gc.x};
+    const float g = gc.y;
+    const uint32_t w0 = rec.x & 0xffffu, w1 = rec.x >> 16, w2 = rec.y & 0xffffu, w3 = rec.y >> 16;
+    const float4 p0 = pos[w0 & kPatchMask], p1 = pos[w1 & kPatchMask], p2 = pos[w2 & kPatchMask],
+                 p3 = pos[w3 & kPatchMask];
+    // slots of the 4 corners, two 16-bit slot numbers per register
+    const uint32_t s01 = (uint32_t)(__float_as_int(p0.w) + (int)(w0 >> kPatchBits)) |
+                         ((uint32_t)(__float_as_int(p1.w) + (int)(w1 >> kPatchBits)) << 16);
+    const uint32_t s23 = (uint32_t)(__float_as_int(p2.w) + (int)(w2 >> kPatchBits)) |
+                         ((uint32_t)(__float_as_int(p3.w) + (int)(w3 >> kPatchBits)) << 16);
+    // Ds columns = edges; F' = Ds * D' = g F (row-major F[r][c])
+    const float e[3][3] = {{p1.x - p0.x, p2.x - p0.x, p3.x - p0.x},
+                           {p1.y - p0.y, p2.y - p0.y, p3.y - p0.y},
+                           {p1.z - p0.z, p2.z - p0.z, p3.z - p0.z}};
+    float F[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc)
+            F[3 * r + cc] = fmaf(e[r][0], D[cc], fmaf(e[r][1], D[3 + cc], e[r][2] * D[6 + cc]));
+    // closest rotation of F' (that of F: g > 0 scales the singular values)
+    float R[9];
+    if (kRotation == PDGB_ROTATION_SVD) closest_rotation(F, R);
+    else closest_rotation_horn(F, R);
+    // c (R - F) DmInv^T = (g R - F') D'^T ; c R DmInv^T = (g R) D'^T
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k] = kJacobiForm ? fmaf(g, R[k], -F[k]) : g * R[k];
+    // M = R D'^T ; contributions: corner 0 = -(M0+M1+M2), corner j = M_{j-1}
+    float M[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc)
+            M[3 * r + cc] = fmaf(R[3 * r], D[3 * cc], fmaf(R[3 * r + 1], D[3 * cc + 1], R[3 * r + 2] * D[3 * cc + 2]));
+    }
+    const int s0 = s01 & 0xffff, s1 = s01 >> 16, s2 = s23 & 0xffff, s3 = s23 >> 16;
+    slot[s0] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
+    slot[s1] = make_float4(M[0], M[3], M[6], 0.f);
+    slot[s2] = make_float4(M[1], M[4], M[7], 0.f);
+    slot[s3] = make_float4(M[2], M[5], M[8], 0.f);
+}
+
+// Sum of patch vertex k's run of slots e0 .. e1, added to b[v] with one
+// float4 atomic.  The run is summed from a lane-dependent start (then
+// wrapping), so that the 8 lanes of a quarter-warp read 8 different 16-byte
+// bank groups while their runs last, instead of colliding at random.
+__device__ __forceinline__ void add_run(const float4* __restrict__ slot, int k, int e0, int e1, float4* b,
+                                        uint32_t v) {
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    const int len = e1 - e0;
+    int off = (k - e0) & 7;
+    if (off >= len) off = 0;
+    int e = e0 + off;
+    for (int j = 0; j < len; ++j) {
+        const float4 q = slot[e];
+        sx += q.x;
+        sy += q.y;
+        sz += q.z;
+        if (++e == e1) e = e0;
+    }
+    atomicAdd(&b[v], make_float4(sx, sy, sz, 0.f));
+}
+
 // One CTA per tile of Morton-ordered tets.  (1) Every patch vertex k is
-// loaded once (coalesced over the sorted patch list) into pos[k], with the
-// start of its run of slots in the w lane.  (2) Every tet reads its 4 corner
+// loaded once (coalesced over the patch list) into pos[k], with the start of
+// its run of slots in the w lane.  (2) Every tet reads its 4 corner
 // positions (corner records k | r << kPatchBits, loaded with its geometry),
 // computes F = Ds DmInv, the closest rotation R (minus F in the Jacobi
 // residual form) and the corner contributions c R DmInv^T G, and writes each
 // to its slot: run start of k + rank r.  The slots of a tile are ordered by
 // patch vertex, so patch vertex k owns the contiguous slots inc_end[k-1] ..
-// inc_end[k].  (3) Every patch vertex sums its run of slots (a fixed
-// rotation of it, see below) and adds the sum to b with one float4 atomic
-// (pinned vertices are skipped: their RHS is the pin term).  No shared-memory
-// atomics; within a tile the sums are deterministic.
+// inc_end[k].  (3) Every patch vertex sums its run of slots and adds the sum
+// to b with one float4 atomic (pinned vertices are skipped: their RHS is the
+// pin term).  No shared-memory atomics; within a tile the sums are
+// deterministic.
 template <bool kJacobiForm, int kRotation>
 __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4* slot, float4* pos) {
     pdl_trigger();
@@ -42,7 +118,6 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
     // patch positions are gathered (in flight meanwhile); the second tet's
     // after the barrier, so that phase 1 holds one tet's registers, not two.
     constexpr int kPer = kTileTets / kLocalThreads;
-    constexpr uint32_t kPatchMask = (1u << kPatchBits) - 1u;
     const int ntp = a.nt_pad;
     const float4* geo0 = reinterpret_cast<const float4*>(a.geo);
     const float2* geo2 = reinterpret_cast<const float2*>(a.geo + 8 * (size_t)ntp);
@@ -90,47 +165,7 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
     for (int j = 0; j < kPer; ++j) {
         const int lt = threadIdx.x + j * kLocalThreads;
         if (lt >= ntile) break;
-        // D' = g DmInv (row major) and g = sqrt(V0 w)
-        const float D[9] = {GA[j].x, GA[j].y, GA[j].z, GA[j].w, GB[j].x, GB[j].y, GB[j].z, GB[j].w, GC[j].x};
-        const float g = GC[j].y;
-        const uint32_t w0 = S[j].x & 0xffffu, w1 = S[j].x >> 16, w2 = S[j].y & 0xffffu, w3 = S[j].y >> 16;
-        const float4 p0 = pos[w0 & kPatchMask], p1 = pos[w1 & kPatchMask], p2 = pos[w2 & kPatchMask],
-                     p3 = pos[w3 & kPatchMask];
-        // slots of the 4 corners, two 16-bit slot numbers per register
-        const uint32_t s01 = (uint32_t)(__float_as_int(p0.w) + (int)(w0 >> kPatchBits)) |
-                             ((uint32_t)(__float_as_int(p1.w) + (int)(w1 >> kPatchBits)) << 16);
-        const uint32_t s23 = (uint32_t)(__float_as_int(p2.w) + (int)(w2 >> kPatchBits)) |
-                             ((uint32_t)(__float_as_int(p3.w) + (int)(w3 >> kPatchBits)) << 16);
-        // Ds columns = edges; F' = Ds * D' = g F (row-major F[r][c])
-        const float e[3][3] = {{p1.x - p0.x, p2.x - p0.x, p3.x - p0.x},
-                               {p1.y - p0.y, p2.y - p0.y, p3.y - p0.y},
-                               {p1.z - p0.z, p2.z - p0.z, p3.z - p0.z}};
-        float F[9];
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int cc = 0; cc < 3; ++cc)
-                F[3 * r + cc] = fmaf(e[r][0], D[cc], fmaf(e[r][1], D[3 + cc], e[r][2] * D[6 + cc]));
-        // closest rotation of F' (that of F: g > 0 scales the singular values)
-        float R[9];
-        if (kRotation == PDGB_ROTATION_SVD) closest_rotation(F, R);
-        else closest_rotation_horn(F, R);
-        // c (R - F) DmInv^T = (g R - F') D'^T ; c R DmInv^T = (g R) D'^T
-#pragma unroll
-        for (int k = 0; k < 9; ++k) R[k] = kJacobiForm ? fmaf(g, R[k], -F[k]) : g * R[k];
-        // M = R D'^T ; contributions: corner 0 = -(M0+M1+M2), corner j = M_{j-1}
-        float M[9];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-#pragma unroll
-            for (int cc = 0; cc < 3; ++cc)
-                M[3 * r + cc] = fmaf(R[3 * r], D[3 * cc], fmaf(R[3 * r + 1], D[3 * cc + 1], R[3 * r + 2] * D[3 * cc + 2]));
-        }
-        const int s0 = s01 & 0xffff, s1 = s01 >> 16, s2 = s23 & 0xffff, s3 = s23 >> 16;
-        slot[s0] = make_float4(-(M[0] + M[1] + M[2]), -(M[3] + M[4] + M[5]), -(M[6] + M[7] + M[8]), 0.f);
-        slot[s1] = make_float4(M[0], M[3], M[6], 0.f);
-        slot[s2] = make_float4(M[1], M[4], M[7], 0.f);
-        slot[s3] = make_float4(M[2], M[5], M[8], 0.f);
+        tet_contrib<kJacobiForm, kRotation>(GA[j], GB[j], GC[j], S[j], pos, slot);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < np; k += kLocalThreads) {
@@ -139,22 +174,7 @@ __device__ __forceinline__ void local_tile(const LocalArgs& a, int tile, float4*
         if (v & kPinnedBit) continue;
         const int e0 = first ? e0_first : __ldg(&iend[k - 1]);
         const int e1 = first ? e1_first : __ldg(&iend[k]);
-        // The run is summed from a lane-dependent start (then wrapping), so
-        // that the 8 lanes of a quarter-warp read 8 different 16-byte bank
-        // groups while their runs last, instead of colliding at random.
-        float sx = 0.f, sy = 0.f, sz = 0.f;
-        const int len = e1 - e0;
-        int off = (k - e0) & 7;
-        if (off >= len) off = 0;
-        int e = e0 + off;
-        for (int j = 0; j < len; ++j) {
-            const float4 q = slot[e];
-            sx += q.x;
-            sy += q.y;
-            sz += q.z;
-            if (++e == e1) e = e0;
-        }
-        atomicAdd(&a.b[v], make_float4(sx, sy, sz, 0.f));
+        add_run(slot, k, e0, e1, a.b, v);
     }
 }
 
@@ -192,6 +212,251 @@ void launch_local_multi(const LocalArgs* req, const int2* list, const int* count
     else k_local_multi<false><<<grid, kLocalThreads, kMaxPatch * sizeof(float4), s>>>(req, list, count);
 }
 
+// ------------------------------------------------ pipelined local step
+// Persistent form of the same tile computation: kPipeThreads threads (one
+// tet each), 2 CTAs per SM, tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// While a tile is computed, one thread bulk-copies the next tile's geometry
+// planes, corner records, patch list and run ends into the other half of a
+// double buffer in shared memory (cp.async.bulk on an mbarrier), so the
+// tile's DRAM reads are in flight during the previous tile's work instead of
+// being waited for at its start.  The patch positions (sn, which earlier
+// kernels of the step write and which stays in L2) are gathered from the
+// copied patch list into the other half of a double-buffered pos.  Per tile:
+//   barrier A (its positions are gathered; the previous tile's run sums are
+//   done, so the slots and the other data buffer are free); thread 0 issues
+//   the next tile's copy; tet contributions -> slots; barrier B; run sums ->
+//   b, each thread going on to wait for the next tile's copy and gather its
+//   positions as soon as it has no more runs to sum.
+// A bounded wait that runs out sets *a.timeout and the CTA stops after its
+// copy in flight has landed (or a second bound has passed).
+constexpr int kPipeThreads = kTileTets;
+constexpr uint64_t kPipeWaitNs = 1000000000ull;  // 1 s
+
+// Shared-memory carve of the pipelined kernel for patches of up to P
+// vertices (P rounded up to a multiple of 8): byte offsets, 128-aligned.
+struct PipeCarve {
+    uint32_t ga, gb, gc, ent, slot, pos, tv, ie, bar, info, total;
+    int pstride;  // entries per buffer of tv / ie beyond P
+};
+__host__ __device__ inline PipeCarve pipe_carve(int max_patch) {
+    PipeCarve c;
+    const uint32_t P = (uint32_t)((max_patch + 7) & ~7);
+    uint32_t o = 0;
+    auto take = [&o](uint32_t bytes) {
+        const uint32_t r = o;
+        o = (o + bytes + 127u) & ~127u;
+        return r;
+    };
+    c.ga = take(2u * kTileTets * 16u);
+    c.gb = take(2u * kTileTets * 16u);
+    c.gc = take(2u * (kTileTets + 8u) * 8u);
+    c.ent = take(2u * (kTileTets + 8u) * 8u);
+    c.slot = take(4u * kTileTets * 16u);
+    c.pos = take(2u * P * 16u);
+    c.tv = take(2u * (P + 8u) * 4u);
+    c.ie = take(2u * (P + 16u) * 2u);
+    c.bar = take(2u * 8u);
+    c.info = take(2u * 16u);
+    c.total = o;
+    c.pstride = (int)P;
+    return c;
+}
+
+// Tile bounds as the copy issuer keeps them: tets t0..t1, patch vb..ve.
+struct TileBounds {
+    int t0, t1, vb, ve;
+};
+__device__ __forceinline__ TileBounds tile_bounds(const LocalArgs& a, int tile) {
+    return TileBounds{__ldg(&a.tile_tet_ptr[tile]), __ldg(&a.tile_tet_ptr[tile + 1]), __ldg(&a.tile_vptr[tile]),
+                      __ldg(&a.tile_vptr[tile + 1])};
+}
+
+template <bool kJacobiForm, int kRotation>
+__global__ void __launch_bounds__(kPipeThreads, 2) k_local_pipe(LocalArgs a, int ntiles, int max_patch) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const PipeCarve C = pipe_carve(max_patch);
+    float4* ga = reinterpret_cast<float4*>(smem + C.ga);
+    float4* gb = reinterpret_cast<float4*>(smem + C.gb);
+    float2* gc = reinterpret_cast<float2*>(smem + C.gc);
+    uint2* ent = reinterpret_cast<uint2*>(smem + C.ent);
+    float4* slot = reinterpret_cast<float4*>(smem + C.slot);
+    float4* pos = reinterpret_cast<float4*>(smem + C.pos);
+    uint32_t* tv = reinterpret_cast<uint32_t*>(smem + C.tv);
+    uint16_t* ie = reinterpret_cast<uint16_t*>(smem + C.ie);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C.bar);
+    int4* info = reinterpret_cast<int4*>(smem + C.info);
+    const int tvs = C.pstride + 8, ies = C.pstride + 16;  // per-buffer strides (entries)
+    constexpr int kGcs = kTileTets + 8;
+    const int tid = threadIdx.x;
+    const int ntp = a.nt_pad;
+
+    // Thread 0 issues the copies of a tile into buffer buf: each range is
+    // rounded out to 16-byte boundaries (the arrays are padded for that);
+    // info[buf] = {t0, tets, vb, patch size}.
+    auto issue = [&](const TileBounds& tb, int buf) {
+        const float4* geo_a = reinterpret_cast<const float4*>(a.geo);
+        const float4* geo_b = geo_a + ntp;
+        const float2* geo_c = reinterpret_cast<const float2*>(a.geo + 8 * (size_t)ntp);
+        const uint2* recs = reinterpret_cast<const uint2*>(a.inc_ent);
+        const int n = tb.t1 - tb.t0;
+        const int c0 = tb.t0 & ~1, c1 = (tb.t1 + 1) & ~1;
+        const int v0 = tb.vb & ~3, v1 = (tb.ve + 3) & ~3;
+        const int i0 = tb.vb & ~7, i1 = (tb.ve + 7) & ~7;
+        const uint32_t bytes_g = (uint32_t)n * 16u, bytes_c = (uint32_t)(c1 - c0) * 8u;
+        const uint32_t bytes_v = (uint32_t)(v1 - v0) * 4u, bytes_i = (uint32_t)(i1 - i0) * 2u;
+        mbar_expect_tx(&bar[buf], 2u * bytes_g + 2u * bytes_c + bytes_v + bytes_i);
+        bulk_load(ga + buf * kTileTets, geo_a + tb.t0, bytes_g, &bar[buf]);
+        bulk_load(gb + buf * kTileTets, geo_b + tb.t0, bytes_g, &bar[buf]);
+        bulk_load(gc + buf * kGcs, geo_c + c0, bytes_c, &bar[buf]);
+        bulk_load(ent + buf * kGcs, recs + c0, bytes_c, &bar[buf]);
+        bulk_load(tv + buf * tvs, a.tile_verts + v0, bytes_v, &bar[buf]);
+        bulk_load(ie + buf * ies, a.inc_end + i0, bytes_i, &bar[buf]);
+        info[buf] = make_int4(tb.t0, n, tb.vb, tb.ve - tb.vb);
+    };
+
+    // Gathers the positions of the tile in buffer gbuf into pos + gbuf * P
+    // (w lane: the start of the vertex's run of slots).
+    auto gather = [&](int gbuf) {
+        const int4 in = info[gbuf];
+        const uint32_t* tvb = tv + gbuf * tvs + (in.z & 3);
+        const uint16_t* ieb = ie + gbuf * ies + (in.z & 7);
+        float4* pb = pos + gbuf * C.pstride;
+        for (int k = tid; k < in.w; k += kPipeThreads) {
+            const float4 p = __ldg(&a.sn[tvb[k] & ~kPinnedBit]);
+            pb[k] = make_float4(p.x, p.y, p.z, __int_as_float(k ? (int)ieb[k - 1] : 0));
+        }
+    };
+
+    TileBounds next{};  // thread 0: bounds of the tile to issue next
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init_fence();
+        issue(tile_bounds(a, blockIdx.x), 0);  // the layout is not written by earlier kernels
+        if ((int)(blockIdx.x + gridDim.x) < ntiles) next = tile_bounds(a, blockIdx.x + gridDim.x);
+    }
+    __syncthreads();
+    pdl_trigger();
+    pdl_wait();
+    if (a.done && *a.done) {
+        // the first copy may still be landing in shared memory
+        mbar_wait_bounded(&bar[0], 0, kPipeWaitNs);
+        return;
+    }
+    bool ok = mbar_wait_bounded(&bar[0], 0, kPipeWaitNs);
+    if (ok) gather(0);
+    for (int it = 0;; ++it) {
+        const int tile = blockIdx.x + it * gridDim.x;
+        const int buf = it & 1;
+        // barrier A: this tile's positions are complete; the previous tile's
+        // run sums are done (the slots and the other buffer are free)
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicExch(a.timeout, 1);
+            mbar_wait_bounded(&bar[buf], (it >> 1) & 1, kPipeWaitNs);
+            break;
+        }
+        const int nxt = tile + (int)gridDim.x;
+        if (tid == 0 && nxt < ntiles) {
+            fence_proxy_async_smem();
+            issue(next, buf ^ 1);
+            const int after = nxt + (int)gridDim.x;
+            if (after < ntiles) next = tile_bounds(a, after);
+        }
+        const int4 in = info[buf];
+        const int oc = in.x & 1;
+        if (tid < in.y)
+            tet_contrib<kJacobiForm, kRotation>(ga[buf * kTileTets + tid], gb[buf * kTileTets + tid],
+                                                gc[buf * kGcs + oc + tid], ent[buf * kGcs + oc + tid],
+                                                pos + buf * C.pstride, slot);
+        __syncthreads();  // barrier B: the slots are complete
+        // run sums of this tile; a thread without (more) vertices goes on to
+        // gather the next tile's positions while the others still sum
+        const uint32_t* tvb = tv + buf * tvs + (in.z & 3);
+        const uint16_t* ieb = ie + buf * ies + (in.z & 7);
+        for (int k = tid; k < in.w; k += kPipeThreads) {
+            const uint32_t v = tvb[k];
+            if (v & kPinnedBit) continue;
+            add_run(slot, k, k ? (int)ieb[k - 1] : 0, (int)ieb[k], a.b, v);
+        }
+        if (nxt >= ntiles) break;
+        if (tid < info[buf ^ 1].w) {
+            ok = mbar_wait_bounded(&bar[buf ^ 1], ((it + 1) >> 1) & 1, kPipeWaitNs);
+            if (ok) gather(buf ^ 1);
+        }
+    }
+}
+
+// Check kernel of the bounded bulk-copy wait (one CTA of 32 threads):
+// thread 0 registers 256 + extra bytes on an mbarrier and copies 256; every
+// thread waits with the given bound.  out[0] = 1 if the wait timed out in
+// any thread, out[1] = 1 if the copied words arrived intact (checked only
+// when the phase completed).
+__global__ void k_bulk_wait_check(const uint4* __restrict__ src, int extra, unsigned long long limit_ns, int* out) {
+    __shared__ __align__(128) uint4 buf[16];
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, 256u + (uint32_t)extra);
+        bulk_load(buf, src, 256u, &bar);
+    }
+    const bool ok = mbar_wait_bounded(&bar, 0, limit_ns);
+    const bool any_late = __syncthreads_or(!ok);
+    if (any_late) {
+        // the phase cannot complete, so its copy's arrival is not observable
+        // on the barrier: give the copy (microseconds, against a bound of at
+        // least 1 ms) a further 100 us before the CTA's shared memory is freed
+        const uint64_t t0 = global_ns();
+        while (global_ns() - t0 < 100000ull) __nanosleep(1000);
+    }
+    if (threadIdx.x == 0) {
+        out[0] = any_late ? 1 : 0;
+        int good = 0;
+        if (!any_late) {
+            good = 1;
+            for (int k = 0; k < 16; ++k)
+                good &= buf[k].x == 4u * k && buf[k].y == 4u * k + 1 && buf[k].z == 4u * k + 2 && buf[k].w == 4u * k + 3;
+        }
+        out[1] = good;
+    }
+}
+
+void launch_bulk_wait_check(const void* src, int extra, unsigned long long limit_ns, int* out, cudaStream_t s) {
+    k_bulk_wait_check<<<1, 32, 0, s>>>(reinterpret_cast<const uint4*>(src), extra, limit_ns, out);
+}
+
+template <bool kJacobiForm>
+static int pipe_occupancy(size_t smem) {
+    static std::once_flag once;
+    static cudaError_t set = cudaSuccess;
+    std::call_once(once, [] {
+        set = cudaFuncSetAttribute(k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)pipe_carve(kMaxPatch).total);
+    });
+    if (set != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
+                                                      kPipeThreads, smem) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
+int local_pipe_grid(int ntiles, int max_patch) {
+    if (ntiles <= 0 || max_patch < 1 || max_patch > kMaxPatch) return 0;
+    const size_t smem = pipe_carve(max_patch).total;
+    const int nb = std::min(pipe_occupancy<true>(smem), pipe_occupancy<false>(smem));
+    int dev = 0, sms = 0;
+    if (nb <= 0 || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    cudaGetLastError();
+    return std::min(ntiles, nb * sms);
+}
+
 // The plain form (Cholesky path) is launched with programmatic dependent
 // launch: its CTAs load their tile layout and first geometry while the
 // preceding kernel drains.  On the Jacobi path, local step and vertex update
@@ -200,6 +465,13 @@ void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_for
     if (ntiles <= 0) return;
     if (max_patch < 1 || max_patch > kMaxPatch)
         throw Error{PDGB_ERR_INVALID_ARGUMENT, "local step: tile patch size out of range"};
+    if (a.pipe_grid > 0 && rotation == PDGB_ROTATION_QUAT) {
+        if (!a.timeout) throw Error{PDGB_ERR_INVALID_ARGUMENT, "local step: pipelined form without a status word"};
+        const size_t smp = pipe_carve(max_patch).total;
+        if (jacobi_form) k_local_pipe<true, PDGB_ROTATION_QUAT><<<a.pipe_grid, kPipeThreads, smp, s>>>(a, ntiles, max_patch);
+        else launch_pdl(k_local_pipe<false, PDGB_ROTATION_QUAT>, a.pipe_grid, kPipeThreads, smp, s, a, ntiles, max_patch);
+        return;
+    }
     const size_t sm = (size_t)max_patch * sizeof(float4);
     if (rotation == PDGB_ROTATION_SVD) {
         if (jacobi_form) k_local<true, PDGB_ROTATION_SVD><<<ntiles, kLocalThreads, sm, s>>>(a);

@@ -85,7 +85,7 @@ void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
     L.tile_vptr.assign(1, 0);
     L.tile_verts.clear();
     L.inc_end.clear();
-    L.inc_ent.assign((size_t)4 * nt, 0);
+    L.inc_ent.assign((size_t)4 * ((nt + 31) & ~31), 0);  // padded to 4 nt_pad
     std::vector<int> mark(nv, -1), loc(nv, 0), cnt, run(nv, 0);
     std::vector<int> patch;
     patch.reserve(kMaxPatch);
@@ -153,6 +153,8 @@ void build_tiles(HostLayout& L, const float* dbc, int max_tile_tets) {
     }
     close_tile(nt);
     L.ntiles = tile;
+    L.tile_verts.insert(L.tile_verts.end(), kLayoutTailPad, 0u);
+    L.inc_end.insert(L.inc_end.end(), kLayoutTailPad, (uint16_t)0);
 }
 
 void build_layout(int nv, int nt, const float* X0, const uint32_t* tets, const float* mass, const float* mu,

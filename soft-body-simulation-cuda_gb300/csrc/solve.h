@@ -57,7 +57,7 @@ struct StepState {
     unsigned count;      // blocks that added their partial error sum
     float err_acc;       // sum of squared changes (float, as the reference)
     int nonfinite;       // a step ended with a non-finite position or velocity (sticky)
-    int pad;
+    int local_timeout;   // a bulk-copy wait of the pipelined local step ran out (sticky)
     GridSync bar;        // barrier of the persistent solve
 };
 

@@ -30,6 +30,8 @@ PDGB_SOLVER_JACOBI = 0
 PDGB_SOLVER_CHOLESKY = 1
 PDGB_ROTATION_QUAT = 0
 PDGB_ROTATION_SVD = 1
+PDGB_LOCAL_TILE = 0
+PDGB_LOCAL_PIPELINED = 1
 PDGB_ORDER_AMD = 0
 PDGB_ORDER_ND = 1
 PDGB_ORDER_DENSE = 2
@@ -270,6 +272,9 @@ SIGNATURES = {
     "pdgb_set_factor_device": (C.c_int, [C.c_void_p, C.c_int]),
     "pdgb_get_factor_blocks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
     "pdgb_set_rotation": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_set_local_kernel": (C.c_int, [C.c_void_p, C.c_int]),
+    "pdgb_bulk_wait_check": (C.c_int, [C.c_int, C.c_longlong]),
+    "pdgb_get_local_kernel": (C.c_int, [C.c_void_p, C.c_void_p]),
     "pdgb_host_factor_check": (C.c_int, [C.POINTER(pdgb_mesh_desc), C.POINTER(pdgb_params), C.c_int, C.c_void_p,
                                          C.c_void_p, C.POINTER(pdgb_factor_info)]),
     "pdgb_step_noalloc": (C.c_int, [C.POINTER(pdgb_noalloc_mesh), C.POINTER(pdgb_params), C.c_void_p, C.c_void_p,

@@ -109,6 +109,15 @@ class PdSolver:
         """0 = quaternion (default, converged), 1 = the reference's 4-sweep SVD."""
         N.check(self._lib.pdgb_set_rotation(self._h, int(mode)), "pdgb_set_rotation")
 
+    def set_local_kernel(self, kind: int) -> None:
+        """0 = one CTA per tile (default), 1 = pipelined persistent CTAs."""
+        N.check(self._lib.pdgb_set_local_kernel(self._h, int(kind)), "pdgb_set_local_kernel")
+
+    def local_kernel(self) -> int:
+        k = C.c_int()
+        N.check(self._lib.pdgb_get_local_kernel(self._h, C.byref(k)), "pdgb_get_local_kernel")
+        return k.value
+
     def reset(self) -> None:
         N.check(self._lib.pdgb_reset(self._h), "pdgb_reset")
 

@@ -36,10 +36,14 @@ def test_batch_equals_bodies_alone(solver):
         assert rel_l2(Xb, Xo) < TOL, (b, rel_l2(Xb, Xo))
         # displacement diagnostic: stiff bodies placed ~1 m from the origin move
         # ~1e-4 m, and float32 rounding of the coordinates alone is ~1e-3 of
-        # that motion, so the bound is relative or 1e-6 m rms, whichever is larger
+        # that motion, so the bound is relative or 2e-6 m rms, whichever is
+        # larger.  The floor is float32 noise: the cross-tile float atomics add
+        # in no fixed order, and repeated runs of this batch put the rms error
+        # of its last body anywhere from 5.8e-7 to 1.08e-6 m (30 float32 ulp
+        # at 1 m at most).
         d_err = float(np.linalg.norm(Xb - Xo) / np.sqrt(body.num_verts))
         disp = float(np.linalg.norm(Xo - body.X) / np.sqrt(body.num_verts))
-        assert d_err < max(2e-3 * disp, 1e-6), (b, d_err, disp)
+        assert d_err < max(2e-3 * disp, 2e-6), (b, d_err, disp)
 
 
 def test_batch_uneven_sizes_cholesky():
@@ -121,3 +125,18 @@ def test_grid_barrier_wait_is_bounded():
     assert lib.pdgb_grid_sync_check(64, 3, 1, 20000) == N.PDGB_ERR_TIMEOUT
     assert lib.pdgb_grid_sync_check(64, 3, 0, 1 << 24) == N.PDGB_OK
     assert lib.pdgb_grid_sync_check(0, 5, 0, 1 << 24) == N.PDGB_OK
+
+
+@pytest.mark.gpu
+def test_bulk_copy_wait_is_bounded():
+    """The pipelined local step's bulk-copy wait on its own: a copy that
+    completes its phase is waited for and its data is intact; a phase that
+    expects bytes nobody copies makes the wait give up after its bound with
+    PDGB_ERR_TIMEOUT, and the context stays usable."""
+    from pdgb import _native as N
+
+    lib = N.lib()
+    assert lib.pdgb_bulk_wait_check(0, 1_000_000_000) == N.PDGB_OK
+    assert lib.pdgb_bulk_wait_check(16, 2_000_000) == N.PDGB_ERR_TIMEOUT
+    assert lib.pdgb_bulk_wait_check(0, 1_000_000_000) == N.PDGB_OK
+    assert lib.pdgb_bulk_wait_check(8, 2_000_000) == N.PDGB_ERR_INVALID_ARGUMENT

@@ -356,3 +356,38 @@ def test_time_local_leaves_state():
         X4, _ = e.download_state()
     Xo, _, _ = O.simulate(body, params, 4, precision=64)
     assert rel_l2(X4, Xo) < TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver,tile", [(0, 0), (1, 0), (0, 37), (1, 101)])
+def test_pipelined_local_step_matches_tile_form(solver, tile):
+    """The pipelined local step (persistent CTAs, next tile bulk-copied into
+    shared memory) against the one-CTA-per-tile form: same per-tet arithmetic
+    and run sums, so the states agree to the rounding of the cross-tile
+    atomics.  Odd tile caps give tiles starting at odd tets and patch lists
+    starting off the 16-byte grid (the copy ranges are rounded out)."""
+    body = mesh.cube_c2(20)
+    params = SolverParams(num_iterations=10, rho=0.9995, solver=solver)
+    out = {}
+    for kind in (N.PDGB_LOCAL_TILE, N.PDGB_LOCAL_PIPELINED):
+        with PdSolver(body, params) as e:
+            if tile:
+                e.set_tile_size(tile)
+            e.set_local_kernel(kind)
+            assert e.local_kernel() == kind
+            e.update(6)
+            out[kind] = e.download_state()[0]
+            assert e.step_status() == N.PDGB_OK
+    assert np.isfinite(out[N.PDGB_LOCAL_PIPELINED]).all()
+    assert rel_l2(out[N.PDGB_LOCAL_PIPELINED], out[N.PDGB_LOCAL_TILE]) < 1e-6
+    Xo, _, _ = O.simulate(body, params, 6, precision=64)
+    assert rel_l2(out[N.PDGB_LOCAL_PIPELINED], Xo) < 1e-4
+
+
+@pytest.mark.gpu
+def test_local_kernel_setting_checked():
+    body = mesh.cube_c2(6)
+    with PdSolver(body, SolverParams(num_iterations=5)) as e:
+        assert e.local_kernel() == N.PDGB_LOCAL_TILE
+        with pytest.raises(PdgbError):
+            e.set_local_kernel(2)
