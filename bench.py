@@ -581,6 +581,9 @@ def main():
     ap.add_argument("--ordering", default="", choices=["", "amd", "nd", "dense"],
                     help="Cholesky factor ordering (default: AMD, or the autotuner's choice)")
     ap.add_argument("--tile", type=int, default=0, help="most tets per local-step tile (0: default / autotuned)")
+    ap.add_argument("--local-kernel", choices=["", "tile", "pipelined"], default="",
+                    help="form of the local step (default: one CTA per tile, or the autotuner's choice; "
+                         "the autotuner tries both, so fix it together with --no-autotune)")
     ap.add_argument("--no-legs", action="store_true", help="default run: report the 64^3 Jacobi workload only, "
                     "without the legs of the other workloads")
     ap.add_argument("--solver", default="", choices=["", "jacobi", "cholesky"],
@@ -621,7 +624,7 @@ def compact_leg(line: dict) -> dict:
     """The fields of a workload's line that the default run reports as a leg."""
     keep = ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "config", "e2e", "roofline", "kernels",
             "accuracy", "reference_gpu", "plain_drop_in", "batched_vs_plain", "factor", "cpu_baseline",
-            "gpu_launches", "clocks", "finite", "autotune")
+            "gpu_launches", "clocks", "finite", "autotune", "local_kernel")
     return {k: line[k] for k in keep if k in line}
 
 
@@ -684,6 +687,8 @@ def run_engine(args, workload_name: str, nsteps: int, nwarmup: int, leg: bool = 
         eng.set_ordering({"amd": N.PDGB_ORDER_AMD, "nd": N.PDGB_ORDER_ND, "dense": N.PDGB_ORDER_DENSE}[args.ordering])
     if args.tile and not leg:
         eng.set_tile_size(args.tile)
+    if args.local_kernel and not leg:
+        eng.set_local_kernel({"tile": N.PDGB_LOCAL_TILE, "pipelined": N.PDGB_LOCAL_PIPELINED}[args.local_kernel])
     stream = torch.cuda.ExternalStream(eng._lib.pdgb_stream(eng.handle))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
 
@@ -710,6 +715,7 @@ def run_engine(args, workload_name: str, nsteps: int, nwarmup: int, leg: bool = 
     tune = None
     if not args.no_autotune:
         tune = eng.autotune(steps=3)  # set-up, outside the timed region; the state is restored
+    local_kernel = "pipelined" if eng.local_kernel() == N.PDGB_LOCAL_PIPELINED else "tile"
     # Workloads timed as repeated runs of a fixed length from rest: the rest
     # state is uploaded from device memory (one gather launch) at the start
     # of every run, between step graphs.
@@ -901,6 +907,7 @@ def run_engine(args, workload_name: str, nsteps: int, nwarmup: int, leg: bool = 
         "dtype": "f32",
         "data": "synthetic",
         "config": dict(WORKLOAD, parallelism=f"replicas{world}" if world > 1 else "single"),
+        "local_kernel": local_kernel,
         "roofline": roofline,
         "kernels": kernels,
         "autotune": tune,
