@@ -338,13 +338,13 @@ int pdgb_set_rotation(pdgb_engine* e, int rotation);
 /* Form of the local step (reference: PdUtil::computeLocal, pdUtil.cu:97-145;
  * same arithmetic and result in both).  TILE (default): one CTA per tile of
  * up to 512 tets, four CTAs per SM, the tile's geometry loaded at its start.
- * PIPELINED: two persistent CTAs per SM walk the tiles; while one tile is
- * computed, the next tile's geometry, corner records and patch lists are
- * bulk-copied into shared memory (on the 64^3 cube it measures slower: two
- * 16-warp CTAs per SM wait at the tile's barriers); pdgb_autotune tries it.
- * A bulk-copy wait that runs out of its bound (1 s) makes
- * pdgb_last_step_status return PDGB_ERR_TIMEOUT.  The SVD rotation always
- * uses TILE.  Takes effect at the next step. */
+ * PIPELINED: four persistent CTAs per SM walk the tiles; while one tile is
+ * computed, the next tile's patch list and the geometry of its first 256
+ * tets are bulk-copied into shared memory (on the 64^3 cube it measures
+ * slower than TILE, whose independent CTAs already overlap one another's
+ * loads); pdgb_autotune tries it.  A bulk-copy wait that runs out of its
+ * bound (1 s) makes pdgb_last_step_status return PDGB_ERR_TIMEOUT.  The SVD
+ * rotation always uses TILE.  Takes effect at the next step. */
 #define PDGB_LOCAL_TILE 0
 #define PDGB_LOCAL_PIPELINED 1
 int pdgb_set_local_kernel(pdgb_engine* e, int kind);

@@ -213,23 +213,24 @@ void launch_local_multi(const LocalArgs* req, const int2* list, const int* count
 }
 
 // ------------------------------------------------ pipelined local step
-// Persistent form of the same tile computation: kPipeThreads threads (one
-// tet each), 2 CTAs per SM, tiles blockIdx.x, blockIdx.x + gridDim.x, ...
-// While a tile is computed, one thread bulk-copies the next tile's geometry
-// planes, corner records, patch list and run ends into the other half of a
-// double buffer in shared memory (cp.async.bulk on an mbarrier), so the
-// tile's DRAM reads are in flight during the previous tile's work instead of
-// being waited for at its start.  The patch positions (sn, which earlier
-// kernels of the step write and which stays in L2) are gathered from the
-// copied patch list into the other half of a double-buffered pos.  Per tile:
-//   barrier A (its positions are gathered; the previous tile's run sums are
-//   done, so the slots and the other data buffer are free); thread 0 issues
-//   the next tile's copy; tet contributions -> slots; barrier B; run sums ->
-//   b, each thread going on to wait for the next tile's copy and gather its
-//   positions as soon as it has no more runs to sum.
+// Persistent form of the same tile computation, with the tile form's shape
+// (kLocalThreads threads, two tets each, 4 CTAs per SM): the CTAs of the grid
+// walk the tiles blockIdx.x, blockIdx.x + gridDim.x, ...  What a tile needs
+// at its start -- its patch list and run ends (double-buffered) and the
+// geometry planes and corner records of its first kLocalThreads tets (single
+// buffer) -- is bulk-copied into shared memory (cp.async.bulk on mbarriers)
+// during the previous tile, so a tile no longer starts with a chain of
+// waits for its bounds, its patch list and its geometry.  The second half's
+// geometry is loaded into registers after barrier A, as in the tile form.
+// Per tile:
+//   gather pos from the copied patch list (sn stays in L2); barrier A (pos
+//   complete; the previous tile's run sums are done, so the other patch
+//   buffer is free): thread 0 issues the next tile's patch copy; wait for
+//   this tile's geometry copy; tet contributions -> slots; barrier B (the
+//   geometry buffer has been read): thread 0 issues the next tile's geometry
+//   copy; run sums -> b.
 // A bounded wait that runs out sets *a.timeout and the CTA stops after its
-// copy in flight has landed (or a second bound has passed).
-constexpr int kPipeThreads = kTileTets;
+// copies in flight have landed (or a second bound has passed).
 constexpr uint64_t kPipeWaitNs = 1000000000ull;  // 1 s
 
 // Shared-memory carve of the pipelined kernel for patches of up to P
@@ -247,15 +248,15 @@ __host__ __device__ inline PipeCarve pipe_carve(int max_patch) {
         o = (o + bytes + 127u) & ~127u;
         return r;
     };
-    c.ga = take(2u * kTileTets * 16u);
-    c.gb = take(2u * kTileTets * 16u);
-    c.gc = take(2u * (kTileTets + 8u) * 8u);
-    c.ent = take(2u * (kTileTets + 8u) * 8u);
+    c.ga = take(kLocalThreads * 16u);
+    c.gb = take(kLocalThreads * 16u);
+    c.gc = take((kLocalThreads + 8u) * 8u);
+    c.ent = take((kLocalThreads + 8u) * 8u);
     c.slot = take(4u * kTileTets * 16u);
-    c.pos = take(2u * P * 16u);
+    c.pos = take(P * 16u);
     c.tv = take(2u * (P + 8u) * 4u);
     c.ie = take(2u * (P + 16u) * 2u);
-    c.bar = take(2u * 8u);
+    c.bar = take(3u * 8u);
     c.info = take(2u * 16u);
     c.total = o;
     c.pstride = (int)P;
@@ -272,7 +273,8 @@ __device__ __forceinline__ TileBounds tile_bounds(const LocalArgs& a, int tile) 
 }
 
 template <bool kJacobiForm, int kRotation>
-__global__ void __launch_bounds__(kPipeThreads, 2) k_local_pipe(LocalArgs a, int ntiles, int max_patch) {
+__global__ void __launch_bounds__(kLocalThreads, PDGB_LOCAL_MIN_BLOCKS) k_local_pipe(LocalArgs a, int ntiles,
+                                                                                     int max_patch) {
     extern __shared__ __align__(128) unsigned char smem[];
     const PipeCarve C = pipe_carve(max_patch);
     float4* ga = reinterpret_cast<float4*>(smem + C.ga);
@@ -283,107 +285,155 @@ __global__ void __launch_bounds__(kPipeThreads, 2) k_local_pipe(LocalArgs a, int
     float4* pos = reinterpret_cast<float4*>(smem + C.pos);
     uint32_t* tv = reinterpret_cast<uint32_t*>(smem + C.tv);
     uint16_t* ie = reinterpret_cast<uint16_t*>(smem + C.ie);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C.bar);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C.bar);  // [0], [1]: patch buffers; [2]: geometry
     int4* info = reinterpret_cast<int4*>(smem + C.info);
     const int tvs = C.pstride + 8, ies = C.pstride + 16;  // per-buffer strides (entries)
-    constexpr int kGcs = kTileTets + 8;
     const int tid = threadIdx.x;
     const int ntp = a.nt_pad;
+    const float4* geo_a = reinterpret_cast<const float4*>(a.geo);
+    const float4* geo_b = geo_a + ntp;
+    const float2* geo_c = reinterpret_cast<const float2*>(a.geo + 8 * (size_t)ntp);
+    const uint2* recs = reinterpret_cast<const uint2*>(a.inc_ent);
 
-    // Thread 0 issues the copies of a tile into buffer buf: each range is
-    // rounded out to 16-byte boundaries (the arrays are padded for that);
-    // info[buf] = {t0, tets, vb, patch size}.
-    auto issue = [&](const TileBounds& tb, int buf) {
-        const float4* geo_a = reinterpret_cast<const float4*>(a.geo);
-        const float4* geo_b = geo_a + ntp;
-        const float2* geo_c = reinterpret_cast<const float2*>(a.geo + 8 * (size_t)ntp);
-        const uint2* recs = reinterpret_cast<const uint2*>(a.inc_ent);
-        const int n = tb.t1 - tb.t0;
-        const int c0 = tb.t0 & ~1, c1 = (tb.t1 + 1) & ~1;
+    // Thread 0: copies of a tile's patch list and run ends into patch buffer
+    // pbuf (ranges rounded out to 16 bytes; the arrays are padded for that),
+    // info[pbuf] = {t0, tets, vb, patch size}.
+    auto issue_patch = [&](const TileBounds& tb, int pbuf) {
         const int v0 = tb.vb & ~3, v1 = (tb.ve + 3) & ~3;
         const int i0 = tb.vb & ~7, i1 = (tb.ve + 7) & ~7;
-        const uint32_t bytes_g = (uint32_t)n * 16u, bytes_c = (uint32_t)(c1 - c0) * 8u;
         const uint32_t bytes_v = (uint32_t)(v1 - v0) * 4u, bytes_i = (uint32_t)(i1 - i0) * 2u;
-        mbar_expect_tx(&bar[buf], 2u * bytes_g + 2u * bytes_c + bytes_v + bytes_i);
-        bulk_load(ga + buf * kTileTets, geo_a + tb.t0, bytes_g, &bar[buf]);
-        bulk_load(gb + buf * kTileTets, geo_b + tb.t0, bytes_g, &bar[buf]);
-        bulk_load(gc + buf * kGcs, geo_c + c0, bytes_c, &bar[buf]);
-        bulk_load(ent + buf * kGcs, recs + c0, bytes_c, &bar[buf]);
-        bulk_load(tv + buf * tvs, a.tile_verts + v0, bytes_v, &bar[buf]);
-        bulk_load(ie + buf * ies, a.inc_end + i0, bytes_i, &bar[buf]);
-        info[buf] = make_int4(tb.t0, n, tb.vb, tb.ve - tb.vb);
+        mbar_expect_tx(&bar[pbuf], bytes_v + bytes_i);
+        bulk_load(tv + pbuf * tvs, a.tile_verts + v0, bytes_v, &bar[pbuf]);
+        bulk_load(ie + pbuf * ies, a.inc_end + i0, bytes_i, &bar[pbuf]);
+        info[pbuf] = make_int4(tb.t0, tb.t1 - tb.t0, tb.vb, tb.ve - tb.vb);
     };
-
-    // Gathers the positions of the tile in buffer gbuf into pos + gbuf * P
-    // (w lane: the start of the vertex's run of slots).
-    auto gather = [&](int gbuf) {
-        const int4 in = info[gbuf];
-        const uint32_t* tvb = tv + gbuf * tvs + (in.z & 3);
-        const uint16_t* ieb = ie + gbuf * ies + (in.z & 7);
-        float4* pb = pos + gbuf * C.pstride;
-        for (int k = tid; k < in.w; k += kPipeThreads) {
+    // Thread 0: copies of the geometry and corner records of a tile's first
+    // kLocalThreads tets into the geometry buffer.
+    auto issue_geo = [&](const TileBounds& tb) {
+        const int n = min(tb.t1 - tb.t0, kLocalThreads);
+        const int c0 = tb.t0 & ~1, c1 = (tb.t0 + n + 1) & ~1;
+        const uint32_t bytes_g = (uint32_t)n * 16u, bytes_c = (uint32_t)(c1 - c0) * 8u;
+        mbar_expect_tx(&bar[2], 2u * bytes_g + 2u * bytes_c);
+        bulk_load(ga, geo_a + tb.t0, bytes_g, &bar[2]);
+        bulk_load(gb, geo_b + tb.t0, bytes_g, &bar[2]);
+        bulk_load(gc, geo_c + c0, bytes_c, &bar[2]);
+        bulk_load(ent, recs + c0, bytes_c, &bar[2]);
+    };
+    // Gathers the positions of the tile in patch buffer pbuf into pos (w
+    // lane: the start of the vertex's run of slots).
+    auto gather = [&](int pbuf) {
+        const int4 in = info[pbuf];
+        const uint32_t* tvb = tv + pbuf * tvs + (in.z & 3);
+        const uint16_t* ieb = ie + pbuf * ies + (in.z & 7);
+        for (int k = tid; k < in.w; k += kLocalThreads) {
             const float4 p = __ldg(&a.sn[tvb[k] & ~kPinnedBit]);
-            pb[k] = make_float4(p.x, p.y, p.z, __int_as_float(k ? (int)ieb[k - 1] : 0));
+            pos[k] = make_float4(p.x, p.y, p.z, __int_as_float(k ? (int)ieb[k - 1] : 0));
         }
     };
 
-    TileBounds next{};  // thread 0: bounds of the tile to issue next
+    TileBounds next{};  // thread 0: bounds of the next tile
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
         mbar_init_fence();
-        issue(tile_bounds(a, blockIdx.x), 0);  // the layout is not written by earlier kernels
+        const TileBounds first = tile_bounds(a, blockIdx.x);  // the layout is not written by earlier kernels
+        issue_patch(first, 0);
+        issue_geo(first);
         if ((int)(blockIdx.x + gridDim.x) < ntiles) next = tile_bounds(a, blockIdx.x + gridDim.x);
     }
     __syncthreads();
     pdl_trigger();
     pdl_wait();
     if (a.done && *a.done) {
-        // the first copy may still be landing in shared memory
+        // the first copies may still be landing in shared memory
         mbar_wait_bounded(&bar[0], 0, kPipeWaitNs);
+        mbar_wait_bounded(&bar[2], 0, kPipeWaitNs);
         return;
     }
     bool ok = mbar_wait_bounded(&bar[0], 0, kPipeWaitNs);
     if (ok) gather(0);
     for (int it = 0;; ++it) {
         const int tile = blockIdx.x + it * gridDim.x;
-        const int buf = it & 1;
-        // barrier A: this tile's positions are complete; the previous tile's
-        // run sums are done (the slots and the other buffer are free)
+        const int pb = it & 1;
+        const bool more = tile + (int)gridDim.x < ntiles;
+        // barrier A: pos is complete; the previous tile's run sums are done
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicExch(a.timeout, 1);
-            mbar_wait_bounded(&bar[buf], (it >> 1) & 1, kPipeWaitNs);
+            mbar_wait_bounded(&bar[pb], (it >> 1) & 1, kPipeWaitNs);
+            mbar_wait_bounded(&bar[2], it & 1, kPipeWaitNs);
             break;
         }
-        const int nxt = tile + (int)gridDim.x;
-        if (tid == 0 && nxt < ntiles) {
+        if (tid == 0 && more) {
             fence_proxy_async_smem();
-            issue(next, buf ^ 1);
-            const int after = nxt + (int)gridDim.x;
+            issue_patch(next, pb ^ 1);
+        }
+        const int4 in = info[pb];
+        const int t0 = in.x, ntile = in.y, oc = t0 & 1;
+        // the second half's geometry, into registers (in flight during the first tet)
+        const int lt1 = tid + kLocalThreads;
+        const int t1i = t0 + (lt1 < ntile ? lt1 : 0);
+        const float4 ga1 = __ldg(geo_a + t1i), gb1 = __ldg(geo_b + t1i);
+        const float2 gc1 = __ldg(geo_c + t1i);
+        const uint2 s1 = __ldg(recs + t1i);
+        ok = mbar_wait_bounded(&bar[2], it & 1, kPipeWaitNs);
+        if (ok && tid < ntile)
+            tet_contrib<kJacobiForm, kRotation>(ga[tid], gb[tid], gc[oc + tid], ent[oc + tid], pos, slot);
+        if (ok && lt1 < ntile) tet_contrib<kJacobiForm, kRotation>(ga1, gb1, gc1, s1, pos, slot);
+        // barrier B: the slots are complete; the geometry buffer has been read
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicExch(a.timeout, 1);
+            mbar_wait_bounded(&bar[2], it & 1, kPipeWaitNs);
+            if (more) mbar_wait_bounded(&bar[pb ^ 1], ((it + 1) >> 1) & 1, kPipeWaitNs);
+            break;
+        }
+        if (tid == 0 && more) {
+            fence_proxy_async_smem();
+            issue_geo(next);
+            const int after = tile + 2 * (int)gridDim.x;
             if (after < ntiles) next = tile_bounds(a, after);
         }
-        const int4 in = info[buf];
-        const int oc = in.x & 1;
-        if (tid < in.y)
-            tet_contrib<kJacobiForm, kRotation>(ga[buf * kTileTets + tid], gb[buf * kTileTets + tid],
-                                                gc[buf * kGcs + oc + tid], ent[buf * kGcs + oc + tid],
-                                                pos + buf * C.pstride, slot);
-        __syncthreads();  // barrier B: the slots are complete
-        // run sums of this tile; a thread without (more) vertices goes on to
-        // gather the next tile's positions while the others still sum
-        const uint32_t* tvb = tv + buf * tvs + (in.z & 3);
-        const uint16_t* ieb = ie + buf * ies + (in.z & 7);
-        for (int k = tid; k < in.w; k += kPipeThreads) {
+        const uint32_t* tvb = tv + pb * tvs + (in.z & 3);
+        const uint16_t* ieb = ie + pb * ies + (in.z & 7);
+        for (int k = tid; k < in.w; k += kLocalThreads) {
             const uint32_t v = tvb[k];
             if (v & kPinnedBit) continue;
             add_run(slot, k, k ? (int)ieb[k - 1] : 0, (int)ieb[k], a.b, v);
         }
-        if (nxt >= ntiles) break;
-        if (tid < info[buf ^ 1].w) {
-            ok = mbar_wait_bounded(&bar[buf ^ 1], ((it + 1) >> 1) & 1, kPipeWaitNs);
-            if (ok) gather(buf ^ 1);
-        }
+        if (!more) break;
+        // the next tile's positions, as soon as this thread has no more runs
+        ok = mbar_wait_bounded(&bar[pb ^ 1], ((it + 1) >> 1) & 1, kPipeWaitNs);
+        if (ok) gather(pb ^ 1);
     }
+}
+
+template <bool kJacobiForm>
+static int pipe_occupancy(size_t smem) {
+    static std::once_flag once;
+    static cudaError_t set = cudaSuccess;
+    std::call_once(once, [] {
+        set = cudaFuncSetAttribute(k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)pipe_carve(kMaxPatch).total);
+    });
+    if (set != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
+                                                      kLocalThreads, smem) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
+int local_pipe_grid(int ntiles, int max_patch) {
+    if (ntiles <= 0 || max_patch < 1 || max_patch > kMaxPatch) return 0;
+    const size_t smem = pipe_carve(max_patch).total;
+    const int nb = std::min(pipe_occupancy<true>(smem), pipe_occupancy<false>(smem));
+    int dev = 0, sms = 0;
+    if (nb <= 0 || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    cudaGetLastError();
+    return std::min(ntiles, nb * sms);
 }
 
 // Check kernel of the bounded bulk-copy wait (one CTA of 32 threads):
@@ -428,35 +478,6 @@ void launch_bulk_wait_check(const void* src, int extra, unsigned long long limit
     k_bulk_wait_check<<<1, 32, 0, s>>>(reinterpret_cast<const uint4*>(src), extra, limit_ns, out);
 }
 
-template <bool kJacobiForm>
-static int pipe_occupancy(size_t smem) {
-    static std::once_flag once;
-    static cudaError_t set = cudaSuccess;
-    std::call_once(once, [] {
-        set = cudaFuncSetAttribute(k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)pipe_carve(kMaxPatch).total);
-    });
-    if (set != cudaSuccess) return 0;
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
-                                                      kPipeThreads, smem) != cudaSuccess)
-        return 0;
-    return nb;
-}
-
-int local_pipe_grid(int ntiles, int max_patch) {
-    if (ntiles <= 0 || max_patch < 1 || max_patch > kMaxPatch) return 0;
-    const size_t smem = pipe_carve(max_patch).total;
-    const int nb = std::min(pipe_occupancy<true>(smem), pipe_occupancy<false>(smem));
-    int dev = 0, sms = 0;
-    if (nb <= 0 || cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        return 0;
-    cudaGetLastError();
-    return std::min(ntiles, nb * sms);
-}
-
 // The plain form (Cholesky path) is launched with programmatic dependent
 // launch: its CTAs load their tile layout and first geometry while the
 // preceding kernel drains.  On the Jacobi path, local step and vertex update
@@ -468,8 +489,8 @@ void launch_local(const LocalArgs& a, int ntiles, int max_patch, bool jacobi_for
     if (a.pipe_grid > 0 && rotation == PDGB_ROTATION_QUAT) {
         if (!a.timeout) throw Error{PDGB_ERR_INVALID_ARGUMENT, "local step: pipelined form without a status word"};
         const size_t smp = pipe_carve(max_patch).total;
-        if (jacobi_form) k_local_pipe<true, PDGB_ROTATION_QUAT><<<a.pipe_grid, kPipeThreads, smp, s>>>(a, ntiles, max_patch);
-        else launch_pdl(k_local_pipe<false, PDGB_ROTATION_QUAT>, a.pipe_grid, kPipeThreads, smp, s, a, ntiles, max_patch);
+        if (jacobi_form) k_local_pipe<true, PDGB_ROTATION_QUAT><<<a.pipe_grid, kLocalThreads, smp, s>>>(a, ntiles, max_patch);
+        else launch_pdl(k_local_pipe<false, PDGB_ROTATION_QUAT>, a.pipe_grid, kLocalThreads, smp, s, a, ntiles, max_patch);
         return;
     }
     const size_t sm = (size_t)max_patch * sizeof(float4);
