@@ -627,11 +627,11 @@ int pdgb_render_surface(pdgb_engine* e, const uint32_t* tris, int num_tris, floa
  *     (other streams, other host threads) race; serialise them.  Each call
  *     recomputes or clears everything it reads from the scratch.
  *   - The first call on a device looks up the scratch's device address for
- *     that device; make it before any stream capture.  The address is kept
- *     until the process exits: a cudaDeviceReset between calls is not
- *     supported.
+ *     that device.  The address is kept until the process exits: a
+ *     cudaDeviceReset between calls is not supported.
  *   - The call waits for its stream twice: after the mesh check and before
- *     returning. */
+ *     returning.  So no call can be captured into a CUDA graph: call it on
+ *     a stream that is not capturing. */
 typedef struct pdgb_noalloc_mesh {
     int num_verts;
     int num_tets;

@@ -23,9 +23,11 @@
 //   - the scratch keeps the previous call's contents; everything a call
 //     needs is recomputed or cleared by that call;
 //   - the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) once for that device; make that first call
-//     before any stream capture.  The address is kept for the life of the
-//     process, so a cudaDeviceReset between calls is not supported;
+//     (cudaGetSymbolAddress) once for that device.  The address is kept for
+//     the life of the process, so a cudaDeviceReset between calls is not
+//     supported;
+//   - every call waits for its stream (after the mesh check and before it
+//     returns), so no call can be captured into a CUDA graph;
 //   - the mesh is checked on the device (tet indices, rest volumes, weights)
 //     before any step: a bad mesh returns PDGB_ERR_BAD_MESH with X and V
 //     untouched.
