@@ -239,3 +239,25 @@ def test_dense_supernode_ordering_matches_fixture(name):
         assert d.max() <= 1 and (d > 0).sum() <= max(1, steps // 10), (its, list(itg))
     Xo, _, _ = O.simulate(body, params, steps, precision=64)
     assert rel_l2(X, Xo) < TOL
+
+
+@pytest.mark.parametrize("kind", [N.PDGB_LOCAL_TILE, N.PDGB_LOCAL_PIPELINED])
+def test_local_step_forms_with_early_exit(kind):
+    """Both forms of the local step under the Cholesky tolerance rule: once
+    the device flag says the step has converged, the remaining local launches
+    of the step return at once (the pipelined form after its first copies
+    have landed), and positions and iteration counts follow the FP64 oracle."""
+    body = mesh.make_grid_body(12, 10, 9, jitter=0.1, seed=21, young=3e4)
+    params = SolverParams(num_iterations=10, tol=1e-4, solver=1)
+    with PdSolver(body, params) as e:
+        e.set_local_kernel(kind)
+        its = []
+        for _ in range(6):
+            e.update(1)
+            its.append(e.last_step_iterations())
+        assert e.step_status() == N.PDGB_OK
+        X, _ = e.download_state()
+    Xo, _, ito = O.simulate(body, params, 6, precision=64)
+    assert min(its) < 10, its  # the early exit engaged
+    assert rel_l2(X, Xo) < TOL
+    assert np.abs(np.asarray(its) - ito).max() <= 1
