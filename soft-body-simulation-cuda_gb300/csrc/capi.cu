@@ -1537,10 +1537,13 @@ namespace {
 int solve_launches(const pdgb_engine* e) {
     if (e->solve_mode != PDGB_SOLVE_LEVELS) return 1;  // PERSISTENT: one launch (and a barrier reset)
     int n = 0;
-    for (const SolveLevel& v : e->chol.step_levels)
-        n += (v.fwdb_end > v.fwdb_begin) + (v.fwdw_end > v.fwdw_begin) + (v.bwdb_end > v.bwdb_begin) +
-             (v.bwdw_end > v.bwdw_begin) + 2 * (v.tiny_end > v.tiny_begin) +
-             (v.zst_end > v.zst_begin);
+    for (const SolveLevel& v : e->chol.step_levels) {
+        const int fb = v.fwdb_end - v.fwdb_begin, fw = v.fwdw_end - v.fwdw_begin;
+        const int bb = v.bwdb_end - v.bwdb_begin, bw = v.bwdw_end - v.bwdw_begin;
+        n += mix_level(fb, fw) ? 1 : (fb > 0) + (fw > 0);
+        n += mix_level(bb, bw) ? 1 : (bb > 0) + (bw > 0);
+        n += 2 * (v.tiny_end > v.tiny_begin) + (v.zst_end > v.zst_begin);
+    }
     return n;
 }
 }  // namespace

@@ -514,12 +514,59 @@ __global__ void __launch_bounds__(kSmallThreads) k_chol_bwd_tiny(CholArgs a, int
     if (t < n) bwd_tiny_item(a, t0 + t);
 }
 
+// A level's block items and a few warp items in one launch (128-thread
+// CTAs: CTAs 0 .. nb-1 take the block items, the others four warp items
+// each).  Items of one level are independent, so where the warp items are
+// few (the upper levels of a batch, where only some bodies still have small
+// supernodes) they run beside the block items instead of in a launch of a
+// handful of CTAs that the next level's launch would wait for.
+__global__ void __launch_bounds__(kBlockThreads) k_chol_fwd_mixed(CholArgs a, int b0, int nb, int w0, int nw) {
+    __shared__ float4 rs[kFwdBlockCols];
+    __shared__ float4 stage[kBlockThreads / 32][32];
+    pdl_trigger();
+    if ((int)blockIdx.x < nb) {
+        FwdBlockPre p;
+        fwd_block_load(a, b0 + blockIdx.x, p);  // static data before the wait
+        pdl_wait();
+        if (a.done && *a.done) return;
+        fwd_block_run(a, p, rs);
+    } else {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int it = ((int)blockIdx.x - nb) * (kBlockThreads / 32) + warp;
+        if (it < nw) fwd_warp_prefetch(a, a.fwd_small + (size_t)kItemInts * (w0 + it), lane);
+        pdl_wait();
+        if (a.done && *a.done) return;
+        if (it < nw) fwd_warp_item(a, a.fwd_small + (size_t)kItemInts * (w0 + it), stage[warp], lane);
+    }
+}
+
+__global__ void __launch_bounds__(kBlockThreads) k_chol_bwd_mixed(CholArgs a, int b0, int nb, int w0, int nw) {
+    pdl_trigger();
+    if ((int)blockIdx.x < nb) {
+        BwdBlockPre p;
+        bwd_block_load(a, b0 + blockIdx.x, p);
+        pdl_wait();
+        if (a.done && *a.done) return;
+        bwd_block_run(a, p);
+    } else {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const int it = ((int)blockIdx.x - nb) * (kBlockThreads / 32) + warp;
+        bwd_warp_item_pre(a, a.bwd_small + (size_t)kItemInts * (w0 + min(it, nw - 1)), lane, it < nw);
+    }
+}
+
 void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& levels, cudaStream_t s) {
     constexpr int kWarps = kSmallThreads / 32;
     for (size_t L = 0; L < levels.size(); ++L) {
         const SolveLevel& v = levels[L];
         const int nb = v.fwdb_end - v.fwdb_begin, nw = v.fwdw_end - v.fwdw_begin, nt = v.tiny_end - v.tiny_begin;
         if (nt > 0) launch_pdl(k_chol_fwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s, a, v.tiny_begin, nt);
+        if (mix_level(nb, nw)) {
+            constexpr int kMixWarps = kBlockThreads / 32;
+            launch_pdl(k_chol_fwd_mixed, nb + (nw + kMixWarps - 1) / kMixWarps, kBlockThreads, 0, s, a, v.fwdb_begin, nb,
+                       v.fwdw_begin, nw);
+            continue;
+        }
         if (nw > 0) launch_pdl(k_chol_fwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, 0, s, a, v.fwdw_begin, nw);
         if (nb > 0) launch_pdl(k_chol_fwd_block, nb, kBlockThreads, 0, s, a, v.fwdb_begin);
     }
@@ -528,8 +575,15 @@ void launch_chol_solve_levels(const CholArgs& a, const std::vector<SolveLevel>& 
         const int nb = v.bwdb_end - v.bwdb_begin, nw = v.bwdw_end - v.bwdw_begin, nt = v.tiny_end - v.tiny_begin;
         const int nz = v.zst_end - v.zst_begin;
         if (nz > 0) launch_pdl(k_chol_bwd_zstage, nz, kStageThreads, 0, s, a, v.zst_begin);
-        if (nb > 0) launch_pdl(k_chol_bwd_block, nb, kBlockThreads, 0, s, a, v.bwdb_begin);
-        if (nw > 0) launch_pdl(k_chol_bwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, 0, s, a, v.bwdw_begin, nw);
+        if (mix_level(nb, nw)) {
+            constexpr int kMixWarps = kBlockThreads / 32;
+            launch_pdl(k_chol_bwd_mixed, nb + (nw + kMixWarps - 1) / kMixWarps, kBlockThreads, 0, s, a, v.bwdb_begin, nb,
+                       v.bwdw_begin, nw);
+        } else {
+            if (nb > 0) launch_pdl(k_chol_bwd_block, nb, kBlockThreads, 0, s, a, v.bwdb_begin);
+            if (nw > 0)
+                launch_pdl(k_chol_bwd_small, (nw + kWarps - 1) / kWarps, kSmallThreads, 0, s, a, v.bwdw_begin, nw);
+        }
         if (nt > 0) launch_pdl(k_chol_bwd_tiny, (nt + kSmallThreads - 1) / kSmallThreads, kSmallThreads, 0, s, a, v.tiny_begin, nt);
     }
 }
