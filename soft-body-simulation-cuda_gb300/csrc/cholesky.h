@@ -205,8 +205,14 @@ void build_dsm_plan(const CholFactor& f, int ctas, int warps_per_cta, size_t max
 // GPU factorisation (factor.cu) instead of computing mval on the host;
 // finish_plan: complete it (finish_front_plan) -- a batch completes the
 // combined plan of its bodies instead.
+// amalgamation: how many explicit zeros a supernode may take on when it is
+// merged into its parent (kAmalgChain for the engine's solves, bound by
+// their chain of levels; kAmalgBytes for the serving step, bound by the
+// factor's bytes).
+enum : int { kAmalgChain = 0, kAmalgBytes = 1 };
 void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFactor& out,
-                     int bwd_chunk_rows = kBwdChunkRows, bool gpu_numeric = false, bool finish_plan = true);
+                     int bwd_chunk_rows = kBwdChunkRows, bool gpu_numeric = false, bool finish_plan = true,
+                     int amalgamation = kAmalgChain);
 
 // Factors the block-diagonal system of independent bodies, one block per
 // body (vertex range vstart[b]..vstart[b+1], tets tstart[b]..tstart[b+1] in

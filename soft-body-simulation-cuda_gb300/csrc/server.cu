@@ -483,7 +483,7 @@ void worker_loop(pdgb_server* S) {
                     // columns per backward item, as the bodies of a batch.
                     auto f = std::make_shared<CholFactor>();
                     const std::vector<float> xyz = layout_xyz(*L);
-                    cholesky_factor(layout_system(*L), PDGB_ORDER_AMD, xyz.data(), *f, 0, true);
+                    cholesky_factor(layout_system(*L), PDGB_ORDER_AMD, xyz.data(), *f, 0, true, true, kAmalgBytes);
                     f->K = SparseSym();  // no refinement residuals in the server
                     me->f = f;
                 }
