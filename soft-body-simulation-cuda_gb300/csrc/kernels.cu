@@ -407,16 +407,25 @@ __global__ void __launch_bounds__(kLocalThreads, PDGB_LOCAL_MIN_BLOCKS) k_local_
     }
 }
 
+// Raises the kernel's dynamic shared-memory limit once per device (function
+// attributes are per device), then asks for its resident CTAs per SM.
 template <bool kJacobiForm>
 static int pipe_occupancy(size_t smem) {
-    static std::once_flag once;
-    static cudaError_t set = cudaSuccess;
-    std::call_once(once, [] {
-        set = cudaFuncSetAttribute(k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)pipe_carve(kMaxPatch).total);
-    });
-    if (set != cudaSuccess) return 0;
+    constexpr int kDevices = 64;
+    static std::mutex mu;
+    static signed char set[kDevices] = {};  // 0: not yet, 1: done, -1: refused
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevices) return 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!set[dev])
+            set[dev] = cudaFuncSetAttribute(k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)pipe_carve(kMaxPatch).total) == cudaSuccess
+                           ? 1
+                           : -1;
+        if (set[dev] < 0) return 0;
+    }
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_local_pipe<kJacobiForm, PDGB_ROTATION_QUAT>,
                                                       kLocalThreads, smem) != cudaSuccess)
