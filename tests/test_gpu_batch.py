@@ -140,3 +140,28 @@ def test_bulk_copy_wait_is_bounded():
     assert lib.pdgb_bulk_wait_check(16, 2_000_000) == N.PDGB_ERR_TIMEOUT
     assert lib.pdgb_bulk_wait_check(0, 1_000_000_000) == N.PDGB_OK
     assert lib.pdgb_bulk_wait_check(8, 2_000_000) == N.PDGB_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("solver", [0, 1])
+def test_pipelined_local_step_on_a_batch(solver):
+    """The pipelined local step on a batch, whose tiles are cut at body
+    boundaries (short tiles, patch lists and tet ranges starting anywhere):
+    the same states as the one-CTA-per-tile form, to the rounding of the
+    cross-tile atomics, and the FP64 oracle per body."""
+    from pdgb import _native as N
+
+    bodies = mesh.batch_c4(nbodies=13, seed=5, lo=2, hi=9)
+    params = SolverParams(num_iterations=10, rho=0.9995, solver=solver)
+    out = {}
+    for kind in (N.PDGB_LOCAL_TILE, N.PDGB_LOCAL_PIPELINED):
+        with PdSolver(bodies, params) as e:
+            e.set_local_kernel(kind)
+            e.update(5)
+            out[kind] = e.download_state()[0]
+            assert e.step_status() == N.PDGB_OK
+    assert rel_l2(out[N.PDGB_LOCAL_PIPELINED], out[N.PDGB_LOCAL_TILE]) < 1e-5
+    lo = 0
+    for body in bodies:
+        Xo, _, _ = O.simulate(body, params, 5, precision=64)
+        assert rel_l2(out[N.PDGB_LOCAL_PIPELINED][lo:lo + body.num_verts], Xo) < TOL
+        lo += body.num_verts
