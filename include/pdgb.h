@@ -239,8 +239,9 @@ int pdgb_synchronize(pdgb_engine* e);
  * range), else PDGB_OK.  The step epilogue sets a device word; this call
  * waits for the stream and reads it.  The reference reports nothing here
  * (SolverStep returns true unconditionally, pdSolver.cu:207).  With the
- * PERSISTENT solve schedule, PDGB_ERR_TIMEOUT when a grid-barrier wait ran
- * out of its bound (the steps since then are invalid). */
+ * PERSISTENT solve schedule or the PIPELINED local step, PDGB_ERR_TIMEOUT
+ * when a grid-barrier or bulk-copy wait ran out of its bound (the steps
+ * since then are invalid). */
 int pdgb_last_step_status(pdgb_engine* e);
 
 /* Check of the persistent solve's grid barrier on its own (no counterpart
