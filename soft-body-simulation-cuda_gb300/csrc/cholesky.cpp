@@ -762,7 +762,7 @@ void cholesky_factor(const SparseSym& K, int ordering, const float* xyz, CholFac
             for (int r0 = 0; r0 < m; r0 += kStageRows)
                 out.zstage.insert(out.zstage.end(), {lo, hi, out.roff[s], m, k, r0, split, zoff});
             for (int c0 = 0; c0 < k; c0 += kBwdBlockCols) {
-                const int cpack = c0 | ((std::min(k, c0 + kBwdBlockCols) - c0) << kBwdColShift);
+                const int cpack = (int)((unsigned)c0 | ((unsigned)(std::min(k, c0 + kBwdBlockCols) - c0) << kBwdColShift));
                 for (int r0 = c0 - c0 % chunk; r0 < m; r0 += chunk)  // rows >= c0 only
                     out.bwd_blocks.insert(out.bwd_blocks.end(),
                                           {lo, hi, out.roff[s], m, r0, cpack, std::min(m, r0 + chunk), zoff});

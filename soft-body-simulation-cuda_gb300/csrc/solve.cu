@@ -306,7 +306,7 @@ __device__ __forceinline__ void bwd_block_load(const CholArgs& a, int item, BwdB
     const int4 h1 = __ldg(reinterpret_cast<const int4*>(w) + 1);
     const int64_t moff = (int64_t)(uint32_t)h0.x | ((int64_t)h0.y << 32);
     const int roff = h0.z, m = h0.w, r0 = h1.x, c0 = h1.y & ((1 << kBwdColShift) - 1),
-              c1 = c0 + (h1.y >> kBwdColShift), rend = h1.z, zoff = h1.w;
+              c1 = c0 + (int)((unsigned)h1.y >> kBwdColShift), rend = h1.z, zoff = h1.w;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int cw = c0 + kBwdWarpCols * warp;  // first column of this warp
     p.nc = min(kBwdWarpCols, c1 - cw);
